@@ -1,0 +1,100 @@
+"""Builds oracle/_ref/libreconref.so from the reference's own sources.
+
+Test infrastructure: the library pins the CPU oracle to the reference's code.
+The reference cannot be built as a whole here (OpenCV / GLEW / SDL2 / CUDA
+samples headers are missing and its kernels use texture references that CUDA
+12+ removed), but its one-thread-per-element kernels compile for the host once
+the few CUDA built-ins they use are provided.  This script
+
+  * copies the named __global__/__device__ functions out of the reference's
+    .cu files (brace matching, read-only) into oracle/_ref/frag_<file>.inc,
+  * compiles oracle/ref_shim.cpp, which includes those fragments and the
+    reference's kernels/kernelUtils.h under a small host shim, together with the
+    reference's CPU SE(3) exponential tracker/tracker/expm.c,
+  * writes everything only below oracle/_ref/ (git-ignored).
+
+Usage: python oracle/build_ref.py [reference_root]   (default /root/reference)
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+
+# (reference file, [function names]) -- one-thread-per-element kernels only
+FRAGMENTS = {
+    "tracker/kernels/warp.cu": [
+        "interpolateResidualKernel2", "precomputeJacobian4Kernel", "weightJacobianKernel",
+        "dotProduct6", "matrixMultVec6", "generateA", "linearFuseKernel", "conjugateGradientKernel",
+    ],
+    "tracker/kernels/histogram64.cu": ["discretizeResidualKernel", "seekThreshold64Kernel", "generateWeights64Kernel"],
+    "tracker/kernels/d2z.cu": [
+        "xyz2CloudKernel", "genPointsCloud6Kernel", "computeNormalsCudaKernel", "downSampleCloud6Kernel",
+        "extractGradientKernel", "addVertexAttributesWithoutNormalsKernel3", "addVertexAttributesWithoutNormalsKernel4",
+    ],
+    "tracker/kernels/rgb2gray.cu": [
+        "icpResidualKernel2", "icpResidualIndexKernel2", "packIndexKernel", "initWeightsKernel",
+        "updateWeightsKernel", "clampWeightsKernel", "convertZMapToXYZKernel", "convertZMapToXYZ6Kernel",
+    ],
+    "tracker/kernels/downSample2Cuda.cu": ["fastDownSampleHdrKernel"],
+}
+
+
+def strip_comments(src: str) -> str:
+    src = re.sub(r"/\*.*?\*/", lambda m: "\n" * m.group(0).count("\n"), src, flags=re.S)
+    return re.sub(r"//[^\n]*", "", src)
+
+
+def extract(src: str, name: str) -> str:
+    m = re.search(r"(__global__|__device__)[^;{()]*?\b" + re.escape(name) + r"\s*\(", src)
+    if not m:
+        raise RuntimeError(f"function {name} not found")
+    start = m.start()
+    i = src.index("{", m.end())
+    depth = 0
+    for j in range(i, len(src)):
+        if src[j] == "{":
+            depth += 1
+        elif src[j] == "}":
+            depth -= 1
+            if depth == 0:
+                return src[start:j + 1] + "\n"
+    raise RuntimeError(f"unbalanced braces in {name}")
+
+
+def main() -> int:
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RECON_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "tracker", "kernels")):
+        print(f"reference tree not found at {ref}; oracle/_ref not built")
+        return 1
+    os.makedirs(OUT, exist_ok=True)
+    for rel, names in FRAGMENTS.items():
+        with open(os.path.join(ref, rel), encoding="latin-1") as f:
+            src = strip_comments(f.read())
+        body = "".join(extract(src, n) for n in names)
+        base = os.path.splitext(os.path.basename(rel))[0]
+        with open(os.path.join(OUT, f"frag_{base}.inc"), "w") as f:
+            f.write(f"// extracted from {rel}: {', '.join(names)}\n" + body)
+    cxx = os.environ.get("CXX", "g++")
+    flags = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w"]
+    inc = ["-I" + OUT, "-I" + os.path.join(ref, "tracker"), "-I" + os.path.join(ref, "tracker", "kernels"),
+           "-I" + os.path.join(ref, "tracker", "tracker")]
+    objs = []
+    shim_o = os.path.join(OUT, "ref_shim.o")
+    subprocess.run([cxx, *flags, *inc, "-c", os.path.join(HERE, "ref_shim.cpp"), "-o", shim_o], check=True)
+    objs.append(shim_o)
+    expm_o = os.path.join(OUT, "expm.o")
+    subprocess.run([cxx, *flags, *inc, "-x", "c++", "-include", "cmath", "-include", "cstdio", "-c",
+                    os.path.join(ref, "tracker", "tracker", "expm.c"), "-o", expm_o], check=True)
+    objs.append(expm_o)
+    subprocess.run([cxx, "-shared", "-o", os.path.join(OUT, "libreconref.so"), *objs], check=True)
+    print("built", os.path.join(OUT, "libreconref.so"))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

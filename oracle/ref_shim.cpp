@@ -1,0 +1,229 @@
+// ref_shim.cpp -- host build of reference kernels (test infrastructure).
+//
+// Compiled only by oracle/build_ref.py into oracle/_ref/libreconref.so.  It
+// supplies the CUDA built-ins used by the reference's one-thread-per-element
+// kernels (float2/3/4, threadIdx/blockIdx/blockDim, __global__/__device__),
+// includes the reference's own kernels/kernelUtils.h and the kernel bodies
+// extracted verbatim from the reference tree into oracle/_ref/frag_*.inc, and
+// exports ref_* launchers that run each kernel over its grid sequentially.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+using std::fabs;
+using std::max;
+using std::min;
+using std::sqrt;
+
+struct float2 { float x, y; };
+struct float3 { float x, y, z; };
+struct float4 { float x, y, z, w; };
+static inline float3 make_float3(float a, float b, float c) { float3 r = {a, b, c}; return r; }
+struct uint3_ { unsigned int x, y, z; };
+static uint3_ threadIdx, blockIdx, blockDim, gridDim;
+
+#define __global__ static
+#define __device__ static inline
+#define __host__
+typedef double doublereal;
+
+#include "calib/calib.h"
+#define VERTEXBUFFER_STRIDE 24
+#define HISTOGRAM64_BIN_COUNT 64
+
+namespace refk {
+#include "kernelUtils.h"
+#include "frag_warp.inc"
+#include "frag_histogram64.inc"
+#include "frag_d2z.inc"
+#include "frag_rgb2gray.inc"
+#include "frag_downSample2Cuda.inc"
+}  // namespace refk
+
+void expm(float *x, float *Tmotion, float scaleOut);  // tracker/tracker/expm.c:2084 (C++ linkage)
+
+namespace {
+template <class F> void launch1d(int n, int block, F f) {
+    blockDim = {(unsigned)block, 1, 1};
+    int grid = (n + block - 1) / block;
+    gridDim = {(unsigned)grid, 1, 1};
+    for (int b = 0; b < grid; b++)
+        for (int t = 0; t < block; t++) {
+            blockIdx = {(unsigned)b, 0, 0};
+            threadIdx = {(unsigned)t, 0, 0};
+            if (b * block + t < n) f();
+        }
+}
+template <class F> void launch2d(int w, int h, F f) {
+    blockDim = {1, 1, 1};
+    gridDim = {(unsigned)w, (unsigned)h, 1};
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            blockIdx = {(unsigned)x, (unsigned)y, 0};
+            threadIdx = {0, 0, 0};
+            f();
+        }
+}
+}  // namespace
+
+extern "C" {
+
+void ref_convertZMapToXYZ(float *z, float *xyzw, float *calib, int W, int H) {
+    launch2d(W, H, [&] { refk::convertZMapToXYZKernel(z, (float4 *)xyzw, calib, W); });
+}
+
+void ref_convertZMapToXYZ6(float *z, float *pts, int *mask, float *calib, int W, int H) {
+    launch2d(W, H, [&] { refk::convertZMapToXYZ6Kernel(z, pts, mask, calib, W); });
+}
+
+void ref_xyz2Cloud(float *xyzw, int W, int H, float *calib, float *vdata, float *img) {
+    launch2d(W, H, [&] { refk::xyz2CloudKernel((float4 *)xyzw, W, H, calib, vdata, img, 24); });
+}
+
+void ref_extractGradient(float *vdata, int n, float *out) {
+    launch1d(n, 1024, [&] { refk::extractGradientKernel(vdata, 24, 13, out); });
+}
+
+void ref_addVertexAttributes(int *idx, int n, float *vdata, int W, int H, float *calib, float *g1, float *g2,
+                             float *g3, float *g4, int L) {
+    if (L == 3)
+        launch1d(n, 512, [&] { refk::addVertexAttributesWithoutNormalsKernel3(idx, vdata, W, H, calib, g1, g2, g3, 24); });
+    else
+        launch1d(n, 512, [&] { refk::addVertexAttributesWithoutNormalsKernel4(idx, vdata, W, H, calib, g1, g2, g3, g4, 24); });
+}
+
+void ref_precomputeJacobian4(int *idx, int n, float *vdata, float *calib, float *J1, float *J2, float *J3, float *J4,
+                             float optScaleIn) {
+    launch1d(n, 512, [&] { refk::precomputeJacobian4Kernel(idx, vdata, calib, n, J1, J2, J3, J4, 24, optScaleIn); });
+}
+
+void ref_interpolateResidual2(int *idx, int n, float *vdata, float *T, float *calib, int layer, float *img, int w,
+                              int h, float *zcur, int zw, int zh, float *residual, float *zweight) {
+    int colorOffset = layer == 0 ? 14 : (layer == 1 ? 17 : (layer == 2 ? 20 : 23));
+    int divisor = 1 << layer;
+    float a = 1.0f / float(divisor);
+    float b = 0.5f * (a - 1.0f);
+    launch1d(n, 1024, [&] {
+        refk::interpolateResidualKernel2(idx, vdata, T, calib, a, b, colorOffset, img, w, h, zcur, zweight, residual,
+                                         24, zw, zh);
+    });
+}
+
+// discretizeResidualKernel -> 64-bin histogram -> seekThreshold64Kernel ->
+// generateWeights64Kernel, histogram64.cu:115-157
+int ref_generateWeights64(float *residual, int n, float *weights, float *zweights, float *wres, int *hist64) {
+    std::vector<int> disc(n);
+    launch1d(n, 1024, [&] { refk::discretizeResidualKernel(residual, disc.data()); });
+    std::vector<int> h(64, 0);
+    for (int i = 0; i < n; i++) h[disc[i]]++;
+    if (hist64) memcpy(hist64, h.data(), 64 * sizeof(int));
+    launch1d(1, 1, [&] { refk::seekThreshold64Kernel(h.data(), n / 2); });
+    int median = h[0];
+    launch1d(n, 1024, [&] { refk::generateWeights64Kernel(residual, h.data(), weights, zweights, wres); });
+    return median;
+}
+
+void ref_weightJacobian(float *J, float *w, int n, float *Jw) {
+    launch1d(n, 1024, [&] { refk::weightJacobianKernel(J, w, n, Jw); });
+}
+
+void ref_fastDownSampleHdr(float *hi, int wlo, int hlo, float *lo) {
+    launch2d(wlo, hlo, [&] { refk::fastDownSampleHdrKernel(hi, 2 * wlo, lo, wlo); });
+}
+
+void ref_genPointsCloud6(float *z, int W, int H, float *calib, float *pts, int *mask) {
+    launch2d(W, H, [&] { refk::genPointsCloud6Kernel(z, W, H, calib, pts, mask); });
+}
+
+void ref_computeNormals(float *pts, int *mask, int W, int H) {
+    launch2d(W, H, [&] { refk::computeNormalsCudaKernel(pts, mask, W, H); });
+}
+
+void ref_downSampleCloud6(float *src, int *msrc, float *dst, int *mdst, int wlo, int hlo) {
+    launch2d(wlo, hlo, [&] { refk::downSampleCloud6Kernel(dst, mdst, wlo, hlo, src, msrc); });
+}
+
+void ref_icpResidualMask2(float *ref6, int *refmask, int w, int h, float *T, float *calib, float *cur6, int *curmask,
+                          int layer, float *residual, int *rmask) {
+    int divisor = 1 << layer;
+    float a = 1.0f / float(divisor);
+    float b = 0.5f * (a - 1.0f);
+    launch2d(w, h, [&] { refk::icpResidualKernel2(ref6, refmask, w, h, T, calib, cur6, curmask, a, b, residual, rmask); });
+}
+
+void ref_icpResidual2(float *ref6, int *select, int nsel, int w, int h, int layer, float *T, float *calib, float *cur6,
+                      int *curmask, int npadded, float *res, float *J, float *weights, float optScaleIn) {
+    int divisor = 1 << layer;
+    float a = 1.0f / float(divisor);
+    float b = 0.5f * (a - 1.0f);
+    memset(res, 0, sizeof(float) * npadded);
+    memset(J, 0, sizeof(float) * 6 * npadded);
+    launch1d(nsel, 1024, [&] {
+        refk::icpResidualIndexKernel2(ref6, select, nsel, w, h, T, calib, cur6, curmask, a, b, npadded, res, J,
+                                      weights, optScaleIn);
+    });
+}
+
+void ref_packIndex(int *select, int n, float *full, float *r, float *r2) {
+    launch1d(n, 1024, [&] { refk::packIndexKernel(select, full, n, r, r2); });
+}
+
+// generateStudentTWeights (rgb2gray.cu:854-877) with estimateVariance1024's
+// reduction order (rgb2gray.cu:478-547): int truncation per thread, float tree
+// per 1024-thread block, int sum over block partials in the last block.
+static float ref_estimate_variance(const float *r2, const float *w, int n) {
+    int grid = (n + 1023) / 1024;
+    std::vector<float> blockSum(grid);
+    auto tree = [](float *p) {
+        for (int s = 512; s >= 1; s >>= 1)
+            for (int t = 0; t < s; t++) p[t] += p[t + s];
+        return p[0];
+    };
+    for (int b = 0; b < grid; b++) {
+        float s[1024];
+        for (int t = 0; t < 1024; t++) {
+            int sum = 0;
+            for (long i = (long)b * 1024 + t; i < n; i += 1024L * grid) sum += r2[i] * w[i];
+            s[t] = sum;
+        }
+        blockSum[b] = tree(s);
+    }
+    if (grid == 1) return blockSum[0]; /* single block: no lower clamp (rgb2gray.cu:497-499) */
+    float s[1024];
+    for (int t = 0; t < 1024; t++) {
+        int sum = 0;
+        for (int i = t; i < grid; i += 1024) sum += blockSum[i];
+        s[t] = sum;
+    }
+    float v = tree(s);
+    float minVal = float(n);
+    if (v < minVal) v = minVal;
+    return v;
+}
+
+void ref_studentT(float *r2, int n, float *w) {
+    launch1d(n, 1024, [&] { refk::initWeightsKernel(r2, n, 100.0f, w); });
+    for (int it = 0; it < 3; it++) {
+        float var = ref_estimate_variance(r2, w, n);
+        launch1d(n, 1024, [&] { refk::updateWeightsKernel(r2, n, &var, w); });
+    }
+    launch1d(n, 1024, [&] { refk::clampWeightsKernel(w, n); });
+}
+
+void ref_conjugateGradient(float *A, float *b, double *x) {
+    double Adev[16];
+    launch1d(1, 1, [&] { refk::conjugateGradientKernel(A, b, 1e-8, 6, Adev); });
+    x[0] = Adev[9]; x[1] = Adev[2]; x[2] = Adev[4];
+    x[3] = Adev[3]; x[4] = Adev[7]; x[5] = Adev[11];
+}
+
+void ref_linearFuse(float *A1, float *b1, float w1, float iN1, float *A2, float *b2, float w2, float iN2) {
+    launch1d(36, 36, [&] { refk::linearFuseKernel(A1, b1, w1, iN1, A2, b2, w2, iN2); });
+}
+
+void ref_expm(float *x, float *T, float scaleOut) { expm(x, T, scaleOut); }
+
+}  // extern "C"

@@ -1,0 +1,191 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+Test infrastructure: imported only by the tests, smoke() and bench.py's CPU
+baseline leg.  Builds the oracle with its Makefile on first use.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB_PATH = os.path.join(ORACLE_DIR, "liboracle.so")
+
+GEOMETRIC, PHOTOMETRIC, BIOBJECTIVE = 0, 1, 2
+CHOLESKY, CG = 0, 1
+
+_lock = threading.Lock()
+_lib = None
+
+
+class OrcConfig(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("levels", ctypes.c_int32),
+        ("n_select", ctypes.c_int32), ("hist_bins", ctypes.c_int32), ("select_bins", ctypes.c_int32),
+        ("solver", ctypes.c_int32), ("mode", ctypes.c_int32), ("lambda_", ctypes.c_float),
+        ("iters", ctypes.c_int32 * 4), ("opt_scale_in", ctypes.c_float), ("opt_scale_out", ctypes.c_float),
+    ]
+
+
+class OrcIterTrace(ctypes.Structure):
+    _fields_ = [
+        ("level", ctypes.c_int32), ("iter", ctypes.c_int32), ("mode", ctypes.c_int32),
+        ("solved", ctypes.c_int32), ("icp_selected", ctypes.c_int32), ("status", ctypes.c_int32),
+        ("T", ctypes.c_float * 16),
+        ("A", ctypes.c_double * 36), ("b", ctypes.c_double * 6),
+        ("A_ph", ctypes.c_double * 36), ("b_ph", ctypes.c_double * 6),
+        ("A_icp", ctypes.c_double * 36), ("b_icp", ctypes.c_double * 6),
+        ("hist", ctypes.c_int32 * 256), ("median_bin", ctypes.c_int32), ("pad_", ctypes.c_int32),
+    ]
+
+
+def _build() -> None:
+    src = [os.path.join(ORACLE_DIR, f) for f in ("oracle.c", "oracle.h")]
+    src.append(os.path.join(ROOT, "recon_gb300", "csrc", "scene.h"))
+    if os.path.exists(LIB_PATH) and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in src):
+        return
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    with _lock:
+        if _lib is None:
+            _build()
+            L = ctypes.CDLL(LIB_PATH)
+            vp = ctypes.c_void_p
+            i32 = ctypes.c_int
+            f32 = ctypes.c_float
+            L.orc_create.restype = vp
+            L.orc_create.argtypes = [ctypes.POINTER(OrcConfig), vp]
+            L.orc_destroy.argtypes = [vp]
+            L.orc_set_reference.argtypes = [vp, vp, vp]
+            L.orc_set_reference_float.argtypes = [vp, vp, vp]
+            L.orc_set_current.argtypes = [vp, vp, vp]
+            L.orc_track.argtypes = [vp, vp, vp, i32]
+            L.orc_get_array.argtypes = [vp, ctypes.c_char_p, i32, vp, ctypes.c_int64]
+            L.orc_n_icp_selected.argtypes = [vp, i32]
+            L.orc_render_depth.argtypes = [vp, vp, f32, ctypes.c_uint32, ctypes.c_uint32, vp]
+            L.orc_render_gray.argtypes = [vp, vp, vp]
+            L.orc_expm_update.argtypes = [vp, vp, ctypes.c_double]
+            L.orc_expm_twist.argtypes = [vp, vp]
+            L.orc_solve_cholesky.argtypes = [vp, vp, vp]
+            L.orc_solve_cg.argtypes = [vp, vp, ctypes.c_double, i32, vp]
+            L.orc_reduce27.argtypes = [vp, vp, i32, vp, vp]
+            L.orc_reduce27_refordered.argtypes = [vp, vp, i32, vp, vp]
+            L.orc_generate_weights.argtypes = [vp, vp, i32, i32, vp, vp, vp]
+            L.orc_student_t.argtypes = [vp, i32, vp]
+            L.orc_filter_indices.argtypes = [vp, i32, vp, i32, i32, vp]
+            L.orc_grad_histogram.argtypes = [vp, i32, i32, vp]
+            L.orc_fuse_depth.argtypes = [vp, i32, i32, vp, i32, vp, vp, f32, vp, vp]
+            L.orc_zmap_to_xyz.argtypes = [vp, i32, i32, vp, vp]
+            L.orc_zmap_to_xyz6.argtypes = [vp, i32, i32, vp, vp, vp]
+            L.orc_xyz2cloud.argtypes = [vp, i32, i32, vp, vp, vp]
+            L.orc_add_vertex_attributes.argtypes = [vp, i32, vp, i32, i32, vp, vp, i32]
+            L.orc_precompute_jacobian.argtypes = [vp, i32, vp, vp, f32, i32, vp]
+            L.orc_interpolate_residual.argtypes = [i32, vp, vp, vp, vp, i32, vp, i32, i32, vp, i32, i32, vp, vp]
+            L.orc_downsample2.argtypes = [vp, i32, i32, vp]
+            L.orc_gen_cloud6.argtypes = [vp, i32, i32, vp, vp, vp]
+            L.orc_compute_normals6.argtypes = [vp, vp, i32, i32]
+            L.orc_downsample_cloud6.argtypes = [vp, vp, i32, i32, vp, vp]
+            L.orc_icp_residual_mask.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, i32, vp, vp]
+            L.orc_icp_residual_jacobian.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, i32, vp, vp, vp, f32]
+            L.orc_compact.argtypes = [vp, i32, vp]
+            L.orc_compact.restype = i32
+            L.orc_generate_weights.restype = i32
+            L.orc_filter_indices.restype = i32
+            L.orc_solve_cholesky.restype = i32
+            L.orc_linear_fuse.argtypes = [vp, vp, ctypes.c_double, i32, vp, vp, ctypes.c_double, i32]
+            L.orc_convert_gray.argtypes = [vp, i32, vp]
+            L.orc_convert_depth.argtypes = [vp, i32, vp]
+            L.orc_rgbd_float4_to_gray_z.argtypes = [vp, i32, i32, vp, vp, vp]
+            L.orc_num_threads.restype = i32
+            L.orc_set_threads.argtypes = [i32]
+            _lib = L
+    return _lib
+
+
+def ptr(a: np.ndarray) -> ctypes.c_void_p:
+    assert a.flags["C_CONTIGUOUS"]
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def ptrs(arrays) -> ctypes.Array:
+    """C array of pointers (const float *const *) to the given numpy arrays."""
+    arr = (ctypes.c_void_p * len(arrays))()
+    for i, a in enumerate(arrays):
+        assert a.flags["C_CONTIGUOUS"]
+        arr[i] = a.ctypes.data
+    return arr
+
+
+def make_config(width, height, levels, mode=PHOTOMETRIC, iters=(1, 3, 10, 5), n_select=8192, hist_bins=64,
+                select_bins=256, solver=CHOLESKY, lam=0.5) -> OrcConfig:
+    c = OrcConfig()
+    c.width, c.height, c.levels = width, height, levels
+    c.n_select, c.hist_bins, c.select_bins = n_select, hist_bins, select_bins
+    c.solver, c.mode, c.lambda_ = solver, mode, lam
+    it = list(iters) + [0] * (4 - len(iters))
+    c.iters[:] = it[:4]
+    c.opt_scale_in, c.opt_scale_out = 1e-3, 1e3
+    return c
+
+
+class OracleTracker:
+    """Operator-level oracle tracker (PhotoTracker + ShapeTracker schedule)."""
+
+    def __init__(self, cfg: OrcConfig, calib: np.ndarray):
+        self.L = lib()
+        self.cfg = cfg
+        self.calib = np.ascontiguousarray(calib, dtype=np.float32)
+        self.h = self.L.orc_create(ctypes.byref(cfg), ptr(self.calib))
+
+    def close(self):
+        if self.h:
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_reference(self, gray: np.ndarray, depth: np.ndarray):
+        g = np.ascontiguousarray(gray, np.uint8)
+        d = np.ascontiguousarray(depth, np.uint16)
+        self.L.orc_set_reference(self.h, ptr(g), ptr(d))
+
+    def set_current(self, gray: np.ndarray, depth: np.ndarray):
+        g = np.ascontiguousarray(gray, np.uint8)
+        d = np.ascontiguousarray(depth, np.uint16)
+        self.L.orc_set_current(self.h, ptr(g), ptr(d))
+
+    def track(self, T: np.ndarray | None = None, max_trace: int = 64):
+        Tin = np.eye(4, dtype=np.float32) if T is None else np.ascontiguousarray(T, np.float32).copy()
+        trace = (OrcIterTrace * max_trace)()
+        n = self.L.orc_track(self.h, ptr(Tin), ctypes.cast(trace, ctypes.c_void_p), max_trace)
+        if n < 0:
+            raise RuntimeError("oracle track failed")
+        return Tin.reshape(4, 4), list(trace)[:min(n, max_trace)]
+
+    def get(self, name: str, level: int, shape, dtype) -> np.ndarray:
+        out = np.zeros(shape, dtype=dtype)
+        n = self.L.orc_get_array(self.h, name.encode(), level, ptr(out), out.nbytes)
+        if n < 0:
+            raise KeyError(name)
+        return out.reshape(-1)[: n // out.itemsize].reshape(-1)
+
+
+def render_pair(scene, cam_ir, cam_rgb, noise_rel=0.01, noise_seed=1, frame=0):
+    L = lib()
+    d = np.zeros((cam_ir.height, cam_ir.width), np.uint16)
+    g = np.zeros((cam_rgb.height, cam_rgb.width), np.uint8)
+    L.orc_render_depth(ctypes.byref(scene), ctypes.byref(cam_ir), noise_rel, noise_seed, frame, ptr(d))
+    L.orc_render_gray(ctypes.byref(scene), ctypes.byref(cam_rgb), ptr(g))
+    return g, d
