@@ -1,0 +1,180 @@
+/*
+ * recon_track.h -- C ABI of the GB300 dense RGB-D tracking library
+ * (librecon_track.so, hand-written sm_103a CUDA behind plain C entry points).
+ *
+ * It replaces the tracking hot path of ttykkala/recon: the PhotoTracker /
+ * ShapeTracker operator classes (tracker/tracker/phototracker.h:33-154,
+ * tracker/tracker/shapetracker.h:29-137) and the extern "C" kernel launchers
+ * they call (tracker/kernels/cuda_funcs.h:36-111, histogram_common.h:31-34,
+ * expmCuda.h).  All signatures use plain pointers and sizes; every call returns
+ * a status code (the reference prints and returns, hostUtils.cpp:27-33).
+ *
+ * Pointers: "host" arguments are host memory; functions taking `on_device`
+ * accept either host (0) or device (1) image pointers.  All device work of one
+ * tracker/batch runs on the stream given at creation (NULL = the library's own
+ * stream); the reference's second GPU becomes a second stream (fusion).
+ */
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define RECON_OK 0
+#define RECON_ERR_INVALID_ARG -1
+#define RECON_ERR_NOT_ENOUGH_POINTS -2 /* shapetracker.cpp:365 "not enough points" */
+#define RECON_ERR_NON_SPD -3           /* a Cholesky pivot was not positive; pose kept */
+#define RECON_ERR_TIMEOUT -4
+#define RECON_ERR_CUDA -5
+#define RECON_ERR_STATE -6             /* reference or current frame missing */
+#define RECON_ERR_NO_DEVICE -7
+
+#define RECON_CALIB_SIZE 96 /* calibData layout of tracker/calib/calib.h:22-37 */
+#define RECON_MAX_LEVELS 4
+
+/* TrackMode, phototracker.h:30 */
+#define RECON_GEOMETRIC 0
+#define RECON_PHOTOMETRIC 1
+#define RECON_BIOBJECTIVE 2
+
+#define RECON_SOLVER_CHOLESKY 0 /* FP64 Cholesky (reference: dead choleskyKernel, warp.cu:978-1007) */
+#define RECON_SOLVER_CG 1       /* FP64 CG, 6 steps, tol 1e-8 (reference live solver, warp.cu:926-975) */
+
+#define RECON_PRECISION_FP32 0
+#define RECON_PRECISION_MIXED 1 /* FP16 image pyramids, BF16 Jacobians, FP32 math, FP64 reduction fold */
+
+typedef struct recon_config {
+    int32_t width, height, levels; /* level-0 size; 3 levels at 320 wide, 4 at 640 (phototracker.cpp:777-784) */
+    int32_t n_select;              /* photometric points, multiple of 1024 (phototracker.cpp:48: 8192) */
+    int32_t hist_bins;             /* MAD histogram bins (histogram64.cu: 64) */
+    int32_t select_bins;           /* pixel-selection histogram bins (phototracker.cpp:346: 256) */
+    int32_t solver;                /* RECON_SOLVER_* */
+    int32_t mode;                  /* RECON_GEOMETRIC / PHOTOMETRIC / BIOBJECTIVE */
+    float lambda;                  /* bi-objective weight of the ICP term (setLambda, phototracker.cpp:160-165) */
+    int32_t iters[RECON_MAX_LEVELS]; /* GN iterations, coarse -> fine (setIterationCounts, phototracker.cpp:488-490) */
+    float opt_scale_in;            /* 1e-3 (phototracker.cpp:50) */
+    float opt_scale_out;           /* 1e3  (phototracker.cpp:51) */
+    int32_t precision;             /* RECON_PRECISION_* */
+    int32_t reserved[7];
+} recon_config;
+
+typedef struct recon_track_stats {
+    int32_t status;                   /* RECON_OK or the first error of the frame */
+    int32_t iterations;               /* GN iterations executed */
+    int32_t solves;                   /* iterations that updated the pose */
+    int32_t icp_selected[RECON_MAX_LEVELS]; /* valid ICP correspondences per level (0 if unused) */
+    int32_t photo_median_bin;         /* MAD histogram median bin of the last photometric iteration */
+    int32_t non_spd;                  /* solves rejected by a non-positive pivot */
+    int32_t reserved[5];
+} recon_track_stats;
+
+/* Per-iteration record (for parity checks): pose after the update and the
+ * normal equations that produced it. */
+typedef struct recon_iter_trace {
+    int32_t level, iter, mode, solved, icp_selected, status;
+    float T[16];
+    double A[36];
+    double b[6];
+    double A_ph[36], b_ph[6], A_icp[36], b_icp[6];
+    int32_t hist[256];
+    int32_t median_bin;
+    int32_t pad_;
+} recon_iter_trace;
+
+typedef struct recon_batch recon_batch;
+
+/* ---- library ---- */
+const char *recon_last_error(void);
+int recon_device_count(void);
+
+/* calibData from raw calibration (Calibration::setupCalibDataBuffer, calib.cpp:74-93). */
+int recon_calib_setup(const double KL[9], const double KR[9], const double TLR[16], const double kcR[8],
+                      double min_dist, double max_dist, double c0, double c1, int32_t width, float *calib_out);
+
+/* ---- batch of tracker instances (one instance = one PhotoTracker + ShapeTracker) ----
+ * Every instance has its own configuration and calibration; one launch serves
+ * all instances.  The single-tracker calls below are batches of one. */
+int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs, void *stream, recon_batch **out);
+int recon_batch_destroy(recon_batch *b);
+int recon_batch_size(const recon_batch *b);
+
+/* Reference (keyframe) images for instances [0, n): uint8 gray (RGB camera) and
+ * uint16 depth in mm (IR camera, 0 = invalid).  Rebuilds the photometric
+ * selection and Jacobians and the ICP reference pyramid and resets the pose to
+ * identity (PhotoTracker::prepareReference, phototracker.cpp:360-386;
+ * ShapeTracker::setReferencePoints/prepareReference, shapetracker.cpp:205-288).
+ * gray[i] / depth[i] may be NULL to leave instance i unchanged. */
+int recon_batch_set_reference(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
+                              int32_t on_device);
+/* Reference given as the reference's float4 RGBA + normalised depth frame
+ * (rgbTex2GrayHdrZKernel, rgb2gray.cu:64-76; rows stored bottom-up). */
+int recon_batch_set_reference_rgbd_float4(recon_batch *b, int32_t inst, const float *rgbd, int32_t on_device);
+/* Current frame (setCurrentImage + prepareCurrent, phototracker.cpp:236-245, 483-485). */
+int recon_batch_set_current(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
+                            int32_t on_device);
+int recon_batch_set_current_rgbd_float4(recon_batch *b, int32_t inst, const float *rgbd, int32_t on_device);
+
+/* Runs the coarse-to-fine Gauss-Newton schedule for every instance
+ * (gpuEstimateIncrement, phototracker.cpp:666-689).  T_io: n x 16 floats,
+ * row-major, reference IR -> current IR; when non-NULL it is the initial pose
+ * and receives the result.  stats: n entries or NULL.  Synchronises. */
+int recon_batch_track(recon_batch *b, float *T_io, recon_track_stats *stats);
+/* Same, asynchronous: poses stay on the device (recon_batch_get_poses). */
+int recon_batch_track_async(recon_batch *b, const float *T_init_host);
+int recon_batch_get_poses(recon_batch *b, float *T_out, recon_track_stats *stats);
+
+int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters[RECON_MAX_LEVELS]);
+int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambda);
+
+/* Per-iteration trace of instance `inst` (enabled with max_iters > 0). */
+int recon_batch_enable_trace(recon_batch *b, int32_t max_iters);
+int recon_batch_get_trace(recon_batch *b, int32_t inst, recon_iter_trace *out, int32_t max);
+
+/* Measurement hooks (used by the benchmark).  Timing brackets every launch of
+ * the schedule with CUDA events on the batch's stream; totals per kernel kind
+ * (0 GN iteration, 1 ICP mask, 2 ICP compaction, 3 Student-t pass,
+ * 4 current-frame preparation, 5 reference preparation) accumulate in
+ * recon_batch_get_poses and are read with recon_batch_get_timing.  Work
+ * counters: per instance [photometric point-iterations, ICP point-iterations,
+ * ICP mask pixels, 0]. */
+int recon_batch_enable_timing(recon_batch *b, int32_t on);
+int recon_batch_get_timing(recon_batch *b, double *ms, int64_t *launches, int32_t reset);
+int recon_batch_get_work(recon_batch *b, uint64_t *out, int32_t reset);
+void *recon_batch_stream(recon_batch *b); /* the cudaStream_t all work of the batch runs on */
+int64_t recon_launch_count(void);         /* kernels launched by the library so far (graph replays included) */
+
+/* Copies an internal device array of instance `inst` to host memory (tests).
+ * Names: ref_gray, cur_gray, ref_z, cur_z, ref_pts, ref_nrm, cur_pts, sel_idx,
+ * sel_xyz, sel_I, sel_J, vtx, icp_select, icp_w, grad_hist.  Returns bytes. */
+int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, int32_t level, void *host_dst,
+                              int64_t nbytes);
+
+/* ---- single tracker (PhotoTracker-style handle = batch of one) ---- */
+typedef recon_batch recon_tracker;
+int recon_tracker_create(const recon_config *cfg, const float *calib, void *stream, recon_tracker **out);
+int recon_tracker_destroy(recon_tracker *t);
+int recon_set_reference(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device);
+int recon_set_current(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device);
+int recon_track(recon_tracker *t, float T_io[16], recon_track_stats *stats);
+int recon_set_iterations(recon_tracker *t, const int32_t iters[RECON_MAX_LEVELS]);
+int recon_set_mode(recon_tracker *t, int32_t mode, float lambda);
+/* getRelativePose / getGlobalPose / resetTracking (phototracker.cpp:223-262):
+ * the global pose accumulates T^-1 increments in double (applyIncrement,
+ * phototracker.cpp:514-531). */
+int recon_get_relative_pose(recon_tracker *t, float T[16]);
+int recon_get_global_pose(recon_tracker *t, double T[16]);
+int recon_reset(recon_tracker *t);
+
+/* ---- procedural RGB-D renderer (inputs for tests and benchmarks) ----
+ * scene / camera: the recon_scene / recon_camera structs of
+ * recon_gb300/csrc/scene.h.  Output pointers are device memory. */
+int recon_render_depth(const void *scene, const void *camera, float noise_rel, uint32_t noise_seed, uint32_t frame,
+                       uint16_t *depth_dev, void *stream);
+int recon_render_gray(const void *scene, const void *camera, uint8_t *gray_dev, void *stream);
+
+#ifdef __cplusplus
+}
+#endif

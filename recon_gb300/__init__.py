@@ -1,0 +1,346 @@
+"""recon_gb300: GB300-native dense RGB-D tracking (the hot path of ttykkala/recon).
+
+The compute path is librecon_track.so (hand-written sm_103a CUDA behind the C
+ABI of include/recon_track.h).  This module is a thin ctypes layer over that
+ABI mirroring the reference's operator classes (PhotoTracker / ShapeTracker,
+tracker/tracker/phototracker.h:33-154): set a reference, set a current frame,
+track.  There is no CPU fallback: when the CUDA library cannot be loaded every
+call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "librecon_track.so")
+
+GEOMETRIC, PHOTOMETRIC, BIOBJECTIVE = 0, 1, 2
+SOLVER_CHOLESKY, SOLVER_CG = 0, 1
+PRECISION_FP32, PRECISION_MIXED = 0, 1
+CALIB_SIZE = 96
+
+RECON_OK = 0
+ERRORS = {
+    -1: "invalid argument", -2: "not enough points", -3: "non-SPD normal equations",
+    -4: "timeout", -5: "CUDA error", -6: "reference or current frame missing", -7: "no CUDA device",
+}
+
+
+class ReconError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    """recon_config (include/recon_track.h)."""
+    _fields_ = [
+        ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("levels", ctypes.c_int32),
+        ("n_select", ctypes.c_int32), ("hist_bins", ctypes.c_int32), ("select_bins", ctypes.c_int32),
+        ("solver", ctypes.c_int32), ("mode", ctypes.c_int32), ("lambda_", ctypes.c_float),
+        ("iters", ctypes.c_int32 * 4), ("opt_scale_in", ctypes.c_float), ("opt_scale_out", ctypes.c_float),
+        ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
+    ]
+
+
+class TrackStats(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32), ("iterations", ctypes.c_int32), ("solves", ctypes.c_int32),
+        ("icp_selected", ctypes.c_int32 * 4), ("photo_median_bin", ctypes.c_int32), ("non_spd", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
+    ]
+
+
+class IterTrace(ctypes.Structure):
+    _fields_ = [
+        ("level", ctypes.c_int32), ("iter", ctypes.c_int32), ("mode", ctypes.c_int32),
+        ("solved", ctypes.c_int32), ("icp_selected", ctypes.c_int32), ("status", ctypes.c_int32),
+        ("T", ctypes.c_float * 16),
+        ("A", ctypes.c_double * 36), ("b", ctypes.c_double * 6),
+        ("A_ph", ctypes.c_double * 36), ("b_ph", ctypes.c_double * 6),
+        ("A_icp", ctypes.c_double * 36), ("b_icp", ctypes.c_double * 6),
+        ("hist", ctypes.c_int32 * 256), ("median_bin", ctypes.c_int32), ("pad_", ctypes.c_int32),
+    ]
+
+
+def make_config(width: int, height: int, levels: int | None = None, mode: int = PHOTOMETRIC,
+                iters=(1, 3, 10, 5), n_select: int = 8192, hist_bins: int = 64, select_bins: int = 256,
+                solver: int = SOLVER_CHOLESKY, lam: float = 0.5, precision: int = PRECISION_FP32) -> Config:
+    """Tracker configuration; defaults follow phototracker.cpp (8192 points,
+    iterations {1,3,10,5} coarse->fine, 3 levels at 320 wide and 4 at 640)."""
+    if levels is None:
+        levels = 4 if width >= 640 else 3
+    c = Config()
+    c.width, c.height, c.levels = width, height, levels
+    c.n_select, c.hist_bins, c.select_bins = n_select, hist_bins, select_bins
+    c.solver, c.mode, c.lambda_ = solver, mode, lam
+    it = list(iters)[:levels] + [0] * (4 - min(len(iters), levels))
+    c.iters[:] = it[:4]
+    c.opt_scale_in, c.opt_scale_out = 1e-3, 1e3
+    c.precision = precision
+    return c
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads librecon_track.so (built by recon_gb300.build / __graft_entry__.build)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(f"{LIB_PATH} is missing: build it with `python -m recon_gb300.build` "
+                                  "(there is no CPU fallback)")
+            L = ctypes.CDLL(LIB_PATH)
+            vp, i32, i64, f32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float
+            L.recon_last_error.restype = ctypes.c_char_p
+            L.recon_batch_create.argtypes = [i32, vp, vp, vp, ctypes.POINTER(vp)]
+            L.recon_batch_destroy.argtypes = [vp]
+            L.recon_batch_size.argtypes = [vp]
+            L.recon_batch_set_reference.argtypes = [vp, vp, vp, i32]
+            L.recon_batch_set_reference_rgbd_float4.argtypes = [vp, i32, vp, i32]
+            L.recon_batch_set_current.argtypes = [vp, vp, vp, i32]
+            L.recon_batch_set_current_rgbd_float4.argtypes = [vp, i32, vp, i32]
+            L.recon_batch_track.argtypes = [vp, vp, vp]
+            L.recon_batch_track_async.argtypes = [vp, vp]
+            L.recon_batch_get_poses.argtypes = [vp, vp, vp]
+            L.recon_batch_set_iterations.argtypes = [vp, i32, vp]
+            L.recon_batch_set_mode.argtypes = [vp, i32, i32, f32]
+            L.recon_batch_enable_trace.argtypes = [vp, i32]
+            L.recon_batch_get_trace.argtypes = [vp, i32, vp, i32]
+            L.recon_batch_get_array.argtypes = [vp, i32, ctypes.c_char_p, i32, vp, i64]
+            L.recon_batch_get_array.restype = i64
+            L.recon_calib_setup.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, i32, vp]
+            L.recon_tracker_create.argtypes = [vp, vp, vp, ctypes.POINTER(vp)]
+            L.recon_tracker_destroy.argtypes = [vp]
+            L.recon_set_reference.argtypes = [vp, vp, vp, i32]
+            L.recon_set_current.argtypes = [vp, vp, vp, i32]
+            L.recon_track.argtypes = [vp, vp, vp]
+            L.recon_set_iterations.argtypes = [vp, vp]
+            L.recon_set_mode.argtypes = [vp, i32, f32]
+            L.recon_get_relative_pose.argtypes = [vp, vp]
+            L.recon_get_global_pose.argtypes = [vp, vp]
+            L.recon_reset.argtypes = [vp]
+            L.recon_batch_enable_timing.argtypes = [vp, i32]
+            L.recon_batch_get_timing.argtypes = [vp, vp, vp, i32]
+            L.recon_batch_get_work.argtypes = [vp, vp, i32]
+            L.recon_batch_stream.argtypes = [vp]
+            L.recon_batch_stream.restype = vp
+            L.recon_launch_count.restype = i64
+            L.recon_render_depth.argtypes = [vp, vp, f32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
+            L.recon_render_gray.argtypes = [vp, vp, vp, vp]
+            _lib = L
+    return _lib
+
+
+def check(rc: int) -> int:
+    if rc < 0:
+        raise ReconError(rc, lib().recon_last_error().decode())
+    return rc
+
+
+def _ptr(a) -> ctypes.c_void_p:
+    """Address of a C-contiguous numpy array or a torch tensor."""
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return ctypes.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        assert a.is_contiguous()
+        return ctypes.c_void_p(a.data_ptr())
+    raise TypeError(type(a))
+
+
+def _on_device(a) -> int:
+    return int(hasattr(a, "is_cuda") and a.is_cuda)
+
+
+class Batch:
+    """Several tracker instances served by the same launches (recon_batch_*)."""
+
+    def __init__(self, configs, calibs, stream=None):
+        L = lib()
+        self.n = len(configs)
+        self.configs = list(configs)
+        cfg_arr = (Config * self.n)(*configs)
+        cal = np.ascontiguousarray(np.stack([np.asarray(c, np.float32).reshape(CALIB_SIZE) for c in calibs]))
+        self._calib = cal
+        h = ctypes.c_void_p()
+        st = ctypes.c_void_p(stream) if stream else None
+        check(L.recon_batch_create(self.n, ctypes.cast(cfg_arr, ctypes.c_void_p), _ptr(cal), st, ctypes.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().recon_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ptr_tables(self, grays, depths):
+        g = (ctypes.c_void_p * self.n)()
+        d = (ctypes.c_void_p * self.n)()
+        dev = None
+        keep = []
+        for i in range(self.n):
+            if grays[i] is None:
+                continue
+            gi, di = grays[i], depths[i]
+            if isinstance(gi, np.ndarray):
+                gi = np.ascontiguousarray(gi, np.uint8)
+                di = np.ascontiguousarray(di, np.uint16)
+            keep += [gi, di]
+            od = _on_device(gi)
+            if dev is None:
+                dev = od
+            elif dev != od:
+                raise ValueError("mix of host and device inputs")
+            g[i] = _ptr(gi).value
+            d[i] = _ptr(di).value
+        return g, d, int(dev or 0), keep
+
+    def set_reference(self, grays, depths):
+        g, d, dev, keep = self._ptr_tables(grays, depths)
+        check(lib().recon_batch_set_reference(self.h, ctypes.cast(g, ctypes.c_void_p),
+                                              ctypes.cast(d, ctypes.c_void_p), dev))
+
+    def set_current(self, grays, depths):
+        g, d, dev, keep = self._ptr_tables(grays, depths)
+        self._keep = keep
+        check(lib().recon_batch_set_current(self.h, ctypes.cast(g, ctypes.c_void_p),
+                                            ctypes.cast(d, ctypes.c_void_p), dev))
+
+    def set_reference_rgbd_float4(self, inst: int, rgbd):
+        a = np.ascontiguousarray(rgbd, np.float32) if isinstance(rgbd, np.ndarray) else rgbd
+        check(lib().recon_batch_set_reference_rgbd_float4(self.h, inst, _ptr(a), _on_device(a)))
+
+    def set_current_rgbd_float4(self, inst: int, rgbd):
+        a = np.ascontiguousarray(rgbd, np.float32) if isinstance(rgbd, np.ndarray) else rgbd
+        check(lib().recon_batch_set_current_rgbd_float4(self.h, inst, _ptr(a), _on_device(a)))
+
+    def track(self, T_init=None):
+        """Returns (poses [n,4,4] float32, stats list)."""
+        T = np.zeros((self.n, 16), np.float32)
+        if T_init is not None:
+            T[:] = np.asarray(T_init, np.float32).reshape(self.n, 16)
+        stats = (TrackStats * self.n)()
+        if T_init is None:
+            check(lib().recon_batch_track_async(self.h, None))
+            check(lib().recon_batch_get_poses(self.h, _ptr(T), ctypes.cast(stats, ctypes.c_void_p)))
+        else:
+            check(lib().recon_batch_track(self.h, _ptr(T), ctypes.cast(stats, ctypes.c_void_p)))
+        return T.reshape(self.n, 4, 4), list(stats)
+
+    def track_async(self, T_init=None):
+        T = None if T_init is None else np.ascontiguousarray(np.asarray(T_init, np.float32).reshape(self.n, 16))
+        check(lib().recon_batch_track_async(self.h, None if T is None else _ptr(T)))
+
+    def poses(self):
+        T = np.zeros((self.n, 16), np.float32)
+        stats = (TrackStats * self.n)()
+        check(lib().recon_batch_get_poses(self.h, _ptr(T), ctypes.cast(stats, ctypes.c_void_p)))
+        return T.reshape(self.n, 4, 4), list(stats)
+
+    def set_iterations(self, inst: int, iters):
+        it = (ctypes.c_int32 * 4)(*(list(iters) + [0] * 4)[:4])
+        check(lib().recon_batch_set_iterations(self.h, inst, ctypes.cast(it, ctypes.c_void_p)))
+
+    def set_mode(self, inst: int, mode: int, lam: float):
+        check(lib().recon_batch_set_mode(self.h, inst, mode, lam))
+
+    def enable_trace(self, max_iters: int):
+        check(lib().recon_batch_enable_trace(self.h, max_iters))
+
+    def trace(self, inst: int, max_iters: int = 256):
+        buf = (IterTrace * max_iters)()
+        n = check(lib().recon_batch_get_trace(self.h, inst, ctypes.cast(buf, ctypes.c_void_p), max_iters))
+        return list(buf)[:n]
+
+    def get_array(self, inst: int, name: str, level: int, dtype, count: int) -> np.ndarray:
+        out = np.zeros(count, dtype)
+        n = check(lib().recon_batch_get_array(self.h, inst, name.encode(), level, _ptr(out), out.nbytes))
+        return out[: n // out.itemsize]
+
+
+TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_compact", "icp_student_t", "prep_current", "prep_reference"]
+
+
+def launch_count() -> int:
+    return int(lib().recon_launch_count())
+
+
+def _batch_extras():
+    def enable_timing(self, on: bool = True):
+        check(lib().recon_batch_enable_timing(self.h, int(on)))
+
+    def timing(self, reset: bool = False):
+        ms = np.zeros(8, np.float64)
+        cnt = np.zeros(8, np.int64)
+        k = check(lib().recon_batch_get_timing(self.h, _ptr(ms), _ptr(cnt), int(reset)))
+        return {TIMING_KINDS[i]: (float(ms[i]), int(cnt[i])) for i in range(k)}
+
+    def work(self, reset: bool = False) -> np.ndarray:
+        out = np.zeros((self.n, 4), np.uint64)
+        check(lib().recon_batch_get_work(self.h, _ptr(out), int(reset)))
+        return out
+
+    def stream(self) -> int:
+        return int(lib().recon_batch_stream(self.h) or 0)
+
+    Batch.enable_timing = enable_timing
+    Batch.timing = timing
+    Batch.work = work
+    Batch.stream = stream
+
+
+_batch_extras()
+
+
+class Tracker(Batch):
+    """PhotoTracker-style single tracker (recon_tracker_* = batch of one)."""
+
+    def __init__(self, config: Config, calib, stream=None):
+        super().__init__([config], [calib], stream)
+
+    def set_reference(self, gray, depth):
+        super().set_reference([gray], [depth])
+
+    def set_current(self, gray, depth):
+        super().set_current([gray], [depth])
+
+    def track(self, T_init=None):
+        T, st = super().track(None if T_init is None else np.asarray(T_init).reshape(1, 16))
+        return T[0], st[0]
+
+    def global_pose(self) -> np.ndarray:
+        g = np.zeros(16, np.float64)
+        check(lib().recon_get_global_pose(self.h, _ptr(g)))
+        return g.reshape(4, 4)
+
+
+def render_depth(scene, camera, noise_rel: float, noise_seed: int, frame: int, out, stream=None):
+    """Ray-casts uint16 depth (mm) into the device tensor `out` (recon_render_depth)."""
+    check(lib().recon_render_depth(ctypes.byref(scene), ctypes.byref(camera), noise_rel, noise_seed, frame,
+                                   _ptr(out), ctypes.c_void_p(stream) if stream else None))
+
+
+def render_gray(scene, camera, out, stream=None):
+    check(lib().recon_render_gray(ctypes.byref(scene), ctypes.byref(camera), _ptr(out),
+                                  ctypes.c_void_p(stream) if stream else None))

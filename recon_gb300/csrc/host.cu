@@ -1,0 +1,930 @@
+// host.cu -- host side of librecon_track.so: instance memory, the per-frame
+// launch schedule (captured as a CUDA graph) and the C ABI of
+// include/recon_track.h.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <cmath>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "scene.h"
+#include "track_kernels.cuh"
+
+namespace rt {
+__global__ void k_convert_level0(const InstDesc *D, int is_ref, const uint8_t *const *in_gray,
+                                 const uint16_t *const *in_depth, const float *const *in_rgbd);
+__global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int *active);
+__global__ void k_normals(const InstDesc *D, const int *active);
+__global__ void k_xyz2cloud(const InstDesc *D, const int *active);
+__global__ void k_seg_count(const InstDesc *D, const int *active);
+__global__ void k_seg_scan(const InstDesc *D, const int *active);
+__global__ void k_seg_scatter(const InstDesc *D, const int *active);
+__global__ void k_attr_jac(const InstDesc *D, const int *active);
+__global__ void k_icp_mask(const InstDesc *D, int level);
+__global__ void k_icp_compact(const InstDesc *D, int level);
+__global__ void k_icp_student(const InstDesc *D, int level, int pass);
+__global__ void k_iter(const InstDesc *D, int level, int it);
+__global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
+                               uint16_t *out);
+__global__ void k_render_gray(recon_scene sc, recon_camera cam, uint8_t *out);
+__global__ void k_reset_pose(const InstDesc *D, const int *active);
+__global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_init);
+__global__ void k_clear_ref(const InstDesc *D, const int *active);
+}  // namespace rt
+
+using namespace rt;
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<long long> g_launches{0};  // kernels launched by this library (graph replays included)
+
+int fail(int code, const char *msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return RECON_ERR_CUDA;
+}
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);        \
+    } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Arena {
+    size_t off = 0;
+    char *base = nullptr;
+    template <class T> T *take(size_t count) {
+        size_t o = off;
+        off = align256(off + count * sizeof(T));
+        return base ? reinterpret_cast<T *>(base + o) : nullptr;
+    }
+};
+
+}  // namespace
+
+struct recon_batch {
+    int n = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::vector<recon_config> cfg;
+    std::vector<InstDesc> desc;
+    std::vector<void *> arenas;
+    InstDesc *d_desc = nullptr;
+    // input pointer tables (3 x n) and staging for host uploads
+    const void **d_inptr = nullptr;
+    std::vector<const void *> h_inptr;
+    int *d_active = nullptr;
+    uint8_t *d_stage = nullptr;
+    size_t stage_bytes = 0;
+    float *d_Tinit = nullptr;
+    int trace_max = 0;
+    recon_iter_trace *d_trace = nullptr;
+    int *d_trace_count = nullptr;
+    bool have_ref = false, have_cur = false;
+    // schedule graph
+    cudaGraphExec_t graph = nullptr;
+    bool graph_dirty = true;
+    int max_pix = 0, max_L = 0, max_P = 0;
+    long long graph_kernels = 0;
+    // optional per-launch CUDA-event timing (kinds: see TimingKind)
+    bool timing = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> graph_events, direct_events;
+    double t_ms[8] = {0};
+    long long t_cnt[8] = {0};
+    // host pose bookkeeping for the single-tracker API (applyIncrement)
+    double global_pose[16];
+    float T_prev[16];
+};
+
+namespace {
+
+void identity16(float *T) {
+    for (int i = 0; i < 16; i++) T[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+}
+void identity16d(double *T) {
+    for (int i = 0; i < 16; i++) T[i] = (i % 5 == 0) ? 1.0 : 0.0;
+}
+
+int validate(const recon_config &c) {
+    if (c.width < 32 || c.height < 16) return fail(RECON_ERR_INVALID_ARG, "image too small");
+    if (c.levels < 1 || c.levels > RECON_MAX_LEVELS) return fail(RECON_ERR_INVALID_ARG, "levels must be 1..4");
+    int m = 1 << (c.levels - 1);
+    if (c.width % m || c.height % m) return fail(RECON_ERR_INVALID_ARG, "size not divisible by 2^(levels-1)");
+    if (c.n_select <= 0 || c.n_select % kChunk) return fail(RECON_ERR_INVALID_ARG, "n_select must be a positive multiple of 1024");
+    if (c.n_select > c.width * c.height) return fail(RECON_ERR_INVALID_ARG, "n_select exceeds the pixel count");
+    if ((c.width * c.height) / kSegments > 1024) return fail(RECON_ERR_INVALID_ARG, "image too large for the 512-segment selection");
+    if (c.hist_bins < 2 || c.hist_bins > 256) return fail(RECON_ERR_INVALID_ARG, "hist_bins must be 2..256");
+    if (c.select_bins < 2 || c.select_bins > 1024) return fail(RECON_ERR_INVALID_ARG, "select_bins must be 2..1024");
+    if (c.mode < 0 || c.mode > 2) return fail(RECON_ERR_INVALID_ARG, "bad mode");
+    if (c.solver < 0 || c.solver > 1) return fail(RECON_ERR_INVALID_ARG, "bad solver");
+    for (int l = 0; l < RECON_MAX_LEVELS; l++)
+        if (c.iters[l] < 0 || c.iters[l] > 1000) return fail(RECON_ERR_INVALID_ARG, "bad iteration count");
+    if (!(c.lambda >= 0.0f && c.lambda <= 1.0f)) return fail(RECON_ERR_INVALID_ARG, "lambda must be in [0,1]");
+    return RECON_OK;
+}
+
+// lays out (base == nullptr: sizes only) the device buffers of one instance
+size_t layout(InstDesc &d, char *base) {
+    Arena a;
+    a.base = base;
+    int W = d.W, H = d.H, n = W * H, P = d.P;
+    for (int l = 0; l < kMaxLevels; l++) {
+        int nl = (l < d.L) ? (W >> l) * (H >> l) : 0;
+        d.ref_gray[l] = nl ? a.take<float>(nl) : nullptr;
+        d.cur_gray[l] = nl ? a.take<float>(nl) : nullptr;
+        d.ref_pts[l] = nl ? a.take<float4>(nl) : nullptr;
+        d.ref_nrm[l] = nl ? a.take<float4>(nl) : nullptr;
+        d.cur_pts[l] = nl ? a.take<float4>(nl) : nullptr;
+        d.sel_I[l] = (l < d.L) ? a.take<float>(P) : nullptr;
+        d.sel_J[l] = (l < d.L) ? a.take<float>(6 * (size_t)P) : nullptr;
+    }
+    d.ref_z = a.take<float>(n);
+    d.cur_z = a.take<float>(n);
+    d.vtx = a.take<float>((size_t)kVtxPlanes * n);
+    d.grad_hist = a.take<int>(1024);
+    d.seg = a.take<int>(3076);
+    d.sel_idx = a.take<int>(P);
+    d.sel_xyz = a.take<float>(3 * (size_t)P);
+    d.ph_r = a.take<float>(P);
+    d.ph_zw = a.take<float>(P);
+    d.ph_part = a.take<double>(27);
+    d.ph_hist = a.take<int>(256);
+    d.icp_res = a.take<float>(n);
+    d.icp_mask = a.take<uint8_t>(n);
+    int nblk = (n + kChunk - 1) / kChunk;
+    d.icp_blkcnt = a.take<int>(nblk);
+    d.icp_select = a.take<int>(n);
+    d.icp_r2 = a.take<float>(n);
+    d.icp_w = a.take<float>(n);
+    d.icp_var = a.take<unsigned long long>(4);
+    d.icp_nsel = a.take<int>(kMaxLevels);
+    d.icp_part = a.take<double>((size_t)nblk * 27);
+    d.work = a.take<unsigned long long>(4);
+    d.counter = a.take<unsigned int>(4);
+    d.T = a.take<float>(16);
+    d.stats = a.take<int>(ST_COUNT);
+    return a.off;
+}
+
+int ensure_stage(recon_batch *b, size_t bytes) {
+    if (bytes <= b->stage_bytes) return RECON_OK;
+    if (b->d_stage) cudaFree(b->d_stage);
+    b->d_stage = nullptr;
+    b->stage_bytes = 0;
+    CK(cudaMalloc(&b->d_stage, bytes));
+    b->stage_bytes = bytes;
+    return RECON_OK;
+}
+
+// uploads host images to staging (if needed) and fills the device pointer table
+int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth, const float *const *rgbd,
+                 int on_device) {
+    int n = b->n;
+    b->h_inptr.assign(3 * (size_t)n, nullptr);
+    std::vector<int> active(n, 0);
+    size_t need = 0;
+    if (!on_device) {
+        for (int i = 0; i < n; i++) {
+            size_t px = (size_t)b->cfg[i].width * b->cfg[i].height;
+            if (rgbd && rgbd[i]) need += align256(px * 16);
+            else if (gray && depth && gray[i] && depth[i]) need += align256(px) + align256(px * 2);
+        }
+        int rc = ensure_stage(b, need ? need : 256);
+        if (rc) return rc;
+    }
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+        size_t px = (size_t)b->cfg[i].width * b->cfg[i].height;
+        if (rgbd && rgbd[i]) {
+            const void *p = rgbd[i];
+            if (!on_device) {
+                CK(cudaMemcpyAsync(b->d_stage + off, rgbd[i], px * 16, cudaMemcpyHostToDevice, b->stream));
+                p = b->d_stage + off;
+                off += align256(px * 16);
+            }
+            b->h_inptr[2 * (size_t)n + i] = p;
+            active[i] = 1;
+        } else if (gray && depth && gray[i] && depth[i]) {
+            const void *pg = gray[i], *pd = depth[i];
+            if (!on_device) {
+                CK(cudaMemcpyAsync(b->d_stage + off, gray[i], px, cudaMemcpyHostToDevice, b->stream));
+                pg = b->d_stage + off;
+                off += align256(px);
+                CK(cudaMemcpyAsync(b->d_stage + off, depth[i], px * 2, cudaMemcpyHostToDevice, b->stream));
+                pd = b->d_stage + off;
+                off += align256(px * 2);
+            }
+            b->h_inptr[i] = pg;
+            b->h_inptr[(size_t)n + i] = pd;
+            active[i] = 1;
+        }
+    }
+    CK(cudaMemcpyAsync(b->d_inptr, b->h_inptr.data(), 3 * (size_t)n * sizeof(void *), cudaMemcpyHostToDevice,
+                       b->stream));
+    CK(cudaMemcpyAsync(b->d_active, active.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    // the pageable source vectors must stay valid until the copies complete
+    CK(cudaStreamSynchronize(b->stream));
+    return RECON_OK;
+}
+
+dim3 grid_pix(int pix, int n, int block = 256) { return dim3((pix + block - 1) / block, n, 1); }
+
+enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_COMPACT, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_COUNT };
+
+// brackets one launch with a pair of events when timing is enabled; events
+// recorded during stream capture become graph nodes and are re-recorded by
+// every replay
+struct TimedScope {
+    recon_batch *b;
+    cudaStream_t s;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *list;
+    cudaEvent_t e1 = nullptr, e2 = nullptr;
+    int kind;
+    TimedScope(recon_batch *b_, cudaStream_t s_, int kind_, bool in_graph) : b(b_), s(s_), kind(kind_) {
+        list = in_graph ? &b->graph_events : &b->direct_events;
+        if (!b->timing) return;
+        cudaEventCreate(&e1);
+        cudaEventCreate(&e2);
+        cudaEventRecord(e1, s);
+    }
+    ~TimedScope() {
+        if (!b->timing) return;
+        cudaEventRecord(e2, s);
+        list->push_back({kind, {e1, e2}});
+    }
+};
+
+void collect_events(recon_batch *b, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> &list,
+                    bool destroy) {
+    for (auto &ev : list) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev.second.first, ev.second.second) == cudaSuccess) {
+            b->t_ms[ev.first] += ms;
+            b->t_cnt[ev.first] += 1;
+        }
+        if (destroy) {
+            cudaEventDestroy(ev.second.first);
+            cudaEventDestroy(ev.second.second);
+        }
+    }
+    if (destroy) list.clear();
+}
+
+int prepare_reference(recon_batch *b) {
+    TimedScope ts(b, b->stream, TK_PREP_REF, false);
+    int n = b->n;
+    auto D = b->d_desc;
+    auto in = b->d_inptr;
+    k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(
+        D, 1, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
+    k_normals<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(D, b->d_active);
+    for (int l = 1; l < b->max_L; l++)
+        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, b->stream>>>(D, l, 1, b->d_active);
+    k_clear_ref<<<dim3(1, n), 256, 0, b->stream>>>(D, b->d_active);
+    k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(D, b->d_active);
+    k_seg_count<<<dim3(kSegments / 8, n), 256, 0, b->stream>>>(D, b->d_active);
+    k_seg_scan<<<dim3(1, n), 32, 0, b->stream>>>(D, b->d_active);
+    k_seg_scatter<<<dim3(kSegments / 8, n), 256, 0, b->stream>>>(D, b->d_active);
+    k_attr_jac<<<grid_pix(b->max_P, n), 256, 0, b->stream>>>(D, b->d_active);
+    k_reset_pose<<<dim3(1, n), 32, 0, b->stream>>>(D, b->d_active);
+    g_launches += 10 + (b->max_L - 1);
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int prepare_current(recon_batch *b) {
+    TimedScope ts(b, b->stream, TK_PREP_CUR, false);
+    int n = b->n;
+    auto D = b->d_desc;
+    auto in = b->d_inptr;
+    k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(
+        D, 0, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
+    for (int l = 1; l < b->max_L; l++)
+        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, b->stream>>>(D, l, 0, b->d_active);
+    g_launches += 1 + (b->max_L - 1);
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
+// the per-frame Gauss-Newton schedule (gpuEstimateIncrement, phototracker.cpp:666-689)
+int launch_schedule(recon_batch *b, cudaStream_t s) {
+    int n = b->n;
+    auto D = b->d_desc;
+    bool any_icp = false;
+    for (auto &c : b->cfg) any_icp |= (c.mode != RECON_PHOTOMETRIC);
+    for (int level = b->max_L - 1; level >= 0; level--) {
+        int maxit = 0, maxpix = 0;
+        for (int i = 0; i < n; i++) {
+            const recon_config &c = b->cfg[i];
+            if (level >= c.levels) continue;
+            int it = c.iters[c.levels - 1 - level];
+            if (it > maxit) maxit = it;
+            int px = (c.width >> level) * (c.height >> level);
+            if (px > maxpix) maxpix = px;
+        }
+        if (maxit == 0) continue;
+        int nchunk = (maxpix + kChunk - 1) / kChunk;
+        if (any_icp) {
+            {
+                TimedScope ts(b, s, TK_ICP_MASK, true);
+                k_icp_mask<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
+            }
+            {
+                TimedScope ts(b, s, TK_ICP_COMPACT, true);
+                k_icp_compact<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
+            }
+            for (int pass = 1; pass <= 3; pass++) {
+                TimedScope ts(b, s, TK_ICP_STUDENT, true);
+                k_icp_student<<<grid_pix(maxpix, n), 256, 0, s>>>(D, level, pass);
+            }
+            b->graph_kernels += 5;
+        }
+        for (int it = 0; it < maxit; it++) {
+            TimedScope ts(b, s, TK_ITER, true);
+            k_iter<<<dim3(1 + (any_icp ? nchunk : 0), n), kLanes, 0, s>>>(D, level, it);
+            b->graph_kernels++;
+        }
+    }
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int run_schedule(recon_batch *b) {
+    if (b->graph_dirty) {
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        for (auto &ev : b->graph_events) {
+            cudaEventDestroy(ev.second.first);
+            cudaEventDestroy(ev.second.second);
+        }
+        b->graph_events.clear();
+        cudaStream_t cs;
+        CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t g;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(cs);
+            return cuda_fail(e, "cudaStreamBeginCapture");
+        }
+        b->graph_kernels = 0;
+        int rc = launch_schedule(b, cs);
+        e = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        b->graph_dirty = false;
+    }
+    CK(cudaGraphLaunch(b->graph, b->stream));
+    g_launches += b->graph_kernels;
+    return RECON_OK;
+}
+
+int upload_desc(recon_batch *b) {
+    CK(cudaMemcpyAsync(b->d_desc, b->desc.data(), b->n * sizeof(InstDesc), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return RECON_OK;
+}
+
+}  // namespace
+
+namespace rt {
+
+__global__ void k_reset_pose(const InstDesc *D, const int *active) {
+    const InstDesc &d = D[blockIdx.y];
+    if (!active[blockIdx.y]) return;
+    if (threadIdx.x < 16) d.T[threadIdx.x] = (threadIdx.x % 5 == 0) ? 1.0f : 0.0f;
+}
+
+__global__ void k_clear_ref(const InstDesc *D, const int *active) {
+    const InstDesc &d = D[blockIdx.y];
+    if (!active[blockIdx.y]) return;
+    for (int k = threadIdx.x; k < 1024; k += blockDim.x) d.grad_hist[k] = 0;
+    for (int k = threadIdx.x; k < d.P; k += blockDim.x) d.sel_idx[k] = 0;
+}
+
+__global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_init) {
+    const InstDesc &d = D[blockIdx.y];
+    int t = threadIdx.x;
+    if (have_init && t < 16) d.T[t] = T_init[16 * blockIdx.y + t];
+    if (t < ST_COUNT) d.stats[t] = 0;
+    if (t == 0) {
+        *d.counter = 0u;
+        if (d.trace_count) *d.trace_count = 0;
+    }
+}
+
+}  // namespace rt
+
+// ====================================================================
+// C ABI
+// ====================================================================
+extern "C" {
+
+const char *recon_last_error(void) { return g_last_error.c_str(); }
+
+int recon_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+int recon_calib_setup(const double KL[9], const double KR[9], const double TLR[16], const double kcR[8],
+                      double min_dist, double max_dist, double c0, double c1, int32_t width, float *calib) {
+    if (!KL || !KR || !TLR || !kcR || !calib || width <= 0) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    memset(calib, 0, RECON_CALIB_SIZE * sizeof(float));
+    auto putK = [&](int off, const double *K) {
+        for (int i = 0; i < 9; i++) calib[off + i] = (i % 4 == 0) ? 1.0f : 0.0f;
+        for (int i = 0; i < 6; i++) calib[off + i] = (float)(width * K[i]);
+        const float *m = calib + off;
+        double det = (double)m[0] * ((double)m[4] * m[8] - (double)m[5] * m[7]) -
+                     (double)m[1] * ((double)m[3] * m[8] - (double)m[5] * m[6]) +
+                     (double)m[2] * ((double)m[3] * m[7] - (double)m[4] * m[6]);
+        float *r = calib + off + 9;
+        if (std::fabs(det) < 1e-5) {
+            for (int i = 0; i < 9; i++) r[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+            return;
+        }
+        r[0] = (float)(((double)m[4] * m[8] - (double)m[5] * m[7]) / det);
+        r[1] = (float)(-((double)m[1] * m[8] - (double)m[7] * m[2]) / det);
+        r[2] = (float)(((double)m[1] * m[5] - (double)m[4] * m[2]) / det);
+        r[3] = (float)(-((double)m[3] * m[8] - (double)m[5] * m[6]) / det);
+        r[4] = (float)(((double)m[0] * m[8] - (double)m[6] * m[2]) / det);
+        r[5] = (float)(-((double)m[0] * m[5] - (double)m[3] * m[2]) / det);
+        r[6] = (float)(((double)m[3] * m[7] - (double)m[6] * m[4]) / det);
+        r[7] = (float)(-((double)m[0] * m[7] - (double)m[6] * m[1]) / det);
+        r[8] = (float)(((double)m[0] * m[4] - (double)m[3] * m[1]) / det);
+    };
+    putK(0, KR);
+    for (int i = 0; i < 8; i++) calib[18 + i] = (float)kcR[i];
+    double TRL[16] = {TLR[0], TLR[4], TLR[8],  -(TLR[0] * TLR[3] + TLR[4] * TLR[7] + TLR[8] * TLR[11]),
+                      TLR[1], TLR[5], TLR[9],  -(TLR[1] * TLR[3] + TLR[5] * TLR[7] + TLR[9] * TLR[11]),
+                      TLR[2], TLR[6], TLR[10], -(TLR[2] * TLR[3] + TLR[6] * TLR[7] + TLR[10] * TLR[11]),
+                      0,      0,      0,       1};
+    for (int i = 0; i < 16; i++) {
+        calib[26 + i] = (float)TLR[i];
+        calib[64 + i] = (float)TRL[i];
+    }
+    putK(43, KL);
+    calib[61] = (float)c0;
+    calib[42] = (float)c1;
+    calib[62] = (float)min_dist;
+    calib[63] = (float)max_dist;
+    return RECON_OK;
+}
+
+int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs, void *stream, recon_batch **out) {
+    if (!out || !cfgs || !calibs || n <= 0) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(RECON_ERR_NO_DEVICE, "no CUDA device");
+    for (int i = 0; i < n; i++) {
+        int rc = validate(cfgs[i]);
+        if (rc) return rc;
+    }
+    recon_batch *b = new recon_batch();
+    b->n = n;
+    b->cfg.assign(cfgs, cfgs + n);
+    b->desc.resize(n);
+    identity16d(b->global_pose);
+    identity16(b->T_prev);
+    if (stream) {
+        b->stream = (cudaStream_t)stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete b;
+            return cuda_fail(e, "cudaStreamCreate");
+        }
+        b->own_stream = true;
+    }
+    for (int i = 0; i < n; i++) {
+        const recon_config &c = cfgs[i];
+        InstDesc &d = b->desc[i];
+        memset(&d, 0, sizeof(d));
+        d.W = c.width;
+        d.H = c.height;
+        d.L = c.levels;
+        d.P = c.n_select;
+        d.hist_bins = c.hist_bins;
+        d.select_bins = c.select_bins;
+        d.mode = c.mode;
+        d.solver = c.solver;
+        d.lambda = c.lambda;
+        d.opt_in = c.opt_scale_in;
+        d.opt_out = c.opt_scale_out;
+        d.precision = c.precision;
+        for (int l = 0; l < kMaxLevels; l++) d.iters[l] = c.iters[l];
+        memcpy(d.calib, calibs + (size_t)RECON_CALIB_SIZE * i, sizeof(d.calib));
+        size_t bytes = layout(d, nullptr);
+        void *mem = nullptr;
+        cudaError_t e = cudaMalloc(&mem, bytes);
+        if (e != cudaSuccess) {
+            recon_batch_destroy(b);
+            return cuda_fail(e, "cudaMalloc(instance)");
+        }
+        b->arenas.push_back(mem);
+        cudaMemsetAsync(mem, 0, bytes, b->stream);
+        layout(d, (char *)mem);
+        b->max_pix = std::max(b->max_pix, c.width * c.height);
+        b->max_L = std::max(b->max_L, c.levels);
+        b->max_P = std::max(b->max_P, c.n_select);
+    }
+    cudaError_t e = cudaMalloc(&b->d_desc, n * sizeof(InstDesc));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_inptr, 3 * (size_t)n * sizeof(void *));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_active, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_Tinit, 16 * (size_t)n * sizeof(float));
+    if (e != cudaSuccess) {
+        recon_batch_destroy(b);
+        return cuda_fail(e, "cudaMalloc(batch)");
+    }
+    for (int i = 0; i < n; i++) {
+        float I[16];
+        identity16(I);
+        cudaMemcpyAsync(b->desc[i].T, I, sizeof(I), cudaMemcpyHostToDevice, b->stream);
+        cudaStreamSynchronize(b->stream);
+    }
+    int rc = upload_desc(b);
+    if (rc) {
+        recon_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return RECON_OK;
+}
+
+int recon_batch_destroy(recon_batch *b) {
+    if (!b) return RECON_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (void *p : b->arenas) cudaFree(p);
+    if (b->d_desc) cudaFree(b->d_desc);
+    if (b->d_inptr) cudaFree(b->d_inptr);
+    if (b->d_active) cudaFree(b->d_active);
+    if (b->d_stage) cudaFree(b->d_stage);
+    if (b->d_Tinit) cudaFree(b->d_Tinit);
+    if (b->d_trace) cudaFree(b->d_trace);
+    if (b->d_trace_count) cudaFree(b->d_trace_count);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return RECON_OK;
+}
+
+int recon_batch_size(const recon_batch *b) { return b ? b->n : 0; }
+
+int recon_batch_set_reference(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
+                              int32_t on_device) {
+    if (!b || !gray || !depth) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    int rc = stage_inputs(b, gray, depth, nullptr, on_device);
+    if (rc) return rc;
+    rc = prepare_reference(b);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    b->have_ref = true;
+    return RECON_OK;
+}
+
+int recon_batch_set_reference_rgbd_float4(recon_batch *b, int32_t inst, const float *rgbd, int32_t on_device) {
+    if (!b || !rgbd || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    std::vector<const float *> p(b->n, nullptr);
+    p[inst] = rgbd;
+    int rc = stage_inputs(b, nullptr, nullptr, p.data(), on_device);
+    if (rc) return rc;
+    rc = prepare_reference(b);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    b->have_ref = true;
+    return RECON_OK;
+}
+
+int recon_batch_set_current(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
+                            int32_t on_device) {
+    if (!b || !gray || !depth) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    int rc = stage_inputs(b, gray, depth, nullptr, on_device);
+    if (rc) return rc;
+    rc = prepare_current(b);
+    if (rc) return rc;
+    b->have_cur = true;
+    return RECON_OK;
+}
+
+int recon_batch_set_current_rgbd_float4(recon_batch *b, int32_t inst, const float *rgbd, int32_t on_device) {
+    if (!b || !rgbd || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    std::vector<const float *> p(b->n, nullptr);
+    p[inst] = rgbd;
+    int rc = stage_inputs(b, nullptr, nullptr, p.data(), on_device);
+    if (rc) return rc;
+    rc = prepare_current(b);
+    if (rc) return rc;
+    b->have_cur = true;
+    return RECON_OK;
+}
+
+int recon_batch_track_async(recon_batch *b, const float *T_init_host) {
+    if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
+    if (!b->have_ref || !b->have_cur) return fail(RECON_ERR_STATE, "reference or current frame missing");
+    if (T_init_host)
+        CK(cudaMemcpyAsync(b->d_Tinit, T_init_host, 16 * (size_t)b->n * sizeof(float), cudaMemcpyHostToDevice,
+                           b->stream));
+    k_begin_track<<<dim3(1, b->n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, T_init_host ? 1 : 0);
+    g_launches += 1;
+    CK(cudaGetLastError());
+    return run_schedule(b);
+}
+
+int recon_batch_get_poses(recon_batch *b, float *T_out, recon_track_stats *stats) {
+    if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
+    std::vector<int> st((size_t)b->n * ST_COUNT);
+    for (int i = 0; i < b->n; i++) {
+        if (T_out) CK(cudaMemcpyAsync(T_out + 16 * (size_t)i, b->desc[i].T, 64, cudaMemcpyDeviceToHost, b->stream));
+        if (stats)
+            CK(cudaMemcpyAsync(st.data() + (size_t)i * ST_COUNT, b->desc[i].stats, ST_COUNT * sizeof(int),
+                               cudaMemcpyDeviceToHost, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->timing) {
+        collect_events(b, b->graph_events, false);
+        collect_events(b, b->direct_events, true);
+    }
+    if (stats) {
+        for (int i = 0; i < b->n; i++) {
+            const int *s = st.data() + (size_t)i * ST_COUNT;
+            recon_track_stats &o = stats[i];
+            memset(&o, 0, sizeof(o));
+            o.iterations = s[ST_ITERS];
+            o.solves = s[ST_SOLVES];
+            o.non_spd = s[ST_NONSPD];
+            o.photo_median_bin = s[ST_MEDIAN];
+            for (int l = 0; l < RECON_MAX_LEVELS; l++) o.icp_selected[l] = s[ST_ICPSEL0 + l];
+            o.status = o.non_spd ? RECON_ERR_NON_SPD : RECON_OK;
+            if (b->cfg[i].mode == RECON_GEOMETRIC && o.solves == 0 && o.iterations == 0)
+                o.status = RECON_ERR_NOT_ENOUGH_POINTS;
+        }
+    }
+    return RECON_OK;
+}
+
+int recon_batch_track(recon_batch *b, float *T_io, recon_track_stats *stats) {
+    int rc = recon_batch_track_async(b, T_io);
+    if (rc) return rc;
+    return recon_batch_get_poses(b, T_io, stats);
+}
+
+int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters[RECON_MAX_LEVELS]) {
+    if (!b || !iters || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    recon_config c = b->cfg[inst];
+    for (int l = 0; l < RECON_MAX_LEVELS; l++) c.iters[l] = iters[l];
+    int rc = validate(c);
+    if (rc) return rc;
+    b->cfg[inst] = c;
+    for (int l = 0; l < kMaxLevels; l++) b->desc[inst].iters[l] = iters[l];
+    b->graph_dirty = true;
+    return upload_desc(b);
+}
+
+int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambda) {
+    if (!b || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    recon_config c = b->cfg[inst];
+    c.mode = mode;
+    c.lambda = lambda < 0.0f ? 0.0f : (lambda > 1.0f ? 1.0f : lambda);  // setLambda clamps, phototracker.cpp:160-165
+    int rc = validate(c);
+    if (rc) return rc;
+    b->cfg[inst] = c;
+    b->desc[inst].mode = c.mode;
+    b->desc[inst].lambda = c.lambda;
+    b->graph_dirty = true;
+    return upload_desc(b);
+}
+
+int recon_batch_enable_trace(recon_batch *b, int32_t max_iters) {
+    if (!b || max_iters < 0) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    if (b->d_trace) cudaFree(b->d_trace);
+    if (b->d_trace_count) cudaFree(b->d_trace_count);
+    b->d_trace = nullptr;
+    b->d_trace_count = nullptr;
+    b->trace_max = max_iters;
+    if (max_iters > 0) {
+        CK(cudaMalloc(&b->d_trace, (size_t)b->n * max_iters * sizeof(recon_iter_trace)));
+        CK(cudaMalloc(&b->d_trace_count, (size_t)b->n * sizeof(int)));
+        CK(cudaMemset(b->d_trace, 0, (size_t)b->n * max_iters * sizeof(recon_iter_trace)));
+        CK(cudaMemset(b->d_trace_count, 0, (size_t)b->n * sizeof(int)));
+    }
+    for (int i = 0; i < b->n; i++) {
+        b->desc[i].trace = max_iters > 0 ? b->d_trace + (size_t)i * max_iters : nullptr;
+        b->desc[i].trace_max = max_iters;
+        b->desc[i].trace_count = max_iters > 0 ? b->d_trace_count + i : nullptr;
+    }
+    return upload_desc(b);
+}
+
+int recon_batch_get_trace(recon_batch *b, int32_t inst, recon_iter_trace *out, int32_t max) {
+    if (!b || inst < 0 || inst >= b->n || !out) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    if (!b->d_trace) return 0;
+    int cnt = 0;
+    CK(cudaMemcpy(&cnt, b->d_trace_count + inst, sizeof(int), cudaMemcpyDeviceToHost));
+    if (cnt > b->trace_max) cnt = b->trace_max;
+    if (cnt > max) cnt = max;
+    if (cnt > 0)
+        CK(cudaMemcpy(out, b->d_trace + (size_t)inst * b->trace_max, cnt * sizeof(recon_iter_trace),
+                      cudaMemcpyDeviceToHost));
+    return cnt;
+}
+
+int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, int32_t level, void *host_dst,
+                              int64_t nbytes) {
+    if (!b || inst < 0 || inst >= b->n || !name || !host_dst) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    const InstDesc &d = b->desc[inst];
+    if (level < 0 || level >= d.L) return fail(RECON_ERR_INVALID_ARG, "bad level");
+    int W = d.W >> level, H = d.H >> level, P = d.P, n0 = d.W * d.H;
+    const void *src = nullptr;
+    int64_t sz = 0;
+    std::string nm(name);
+    if (nm == "ref_gray") { src = d.ref_gray[level]; sz = (int64_t)W * H * 4; }
+    else if (nm == "cur_gray") { src = d.cur_gray[level]; sz = (int64_t)W * H * 4; }
+    else if (nm == "ref_z") { src = d.ref_z; sz = (int64_t)n0 * 4; }
+    else if (nm == "cur_z") { src = d.cur_z; sz = (int64_t)n0 * 4; }
+    else if (nm == "ref_pts") { src = d.ref_pts[level]; sz = (int64_t)W * H * 16; }
+    else if (nm == "ref_nrm") { src = d.ref_nrm[level]; sz = (int64_t)W * H * 16; }
+    else if (nm == "cur_pts") { src = d.cur_pts[level]; sz = (int64_t)W * H * 16; }
+    else if (nm == "sel_idx") { src = d.sel_idx; sz = (int64_t)P * 4; }
+    else if (nm == "sel_xyz") { src = d.sel_xyz; sz = (int64_t)P * 12; }
+    else if (nm == "sel_I") { src = d.sel_I[level]; sz = (int64_t)P * 4; }
+    else if (nm == "sel_J") { src = d.sel_J[level]; sz = (int64_t)P * 24; }
+    else if (nm == "vtx") { src = d.vtx; sz = (int64_t)n0 * 4 * kVtxPlanes; }
+    else if (nm == "grad_hist") { src = d.grad_hist; sz = (int64_t)d.select_bins * 4; }
+    else if (nm == "T") { src = d.T; sz = 64; }
+    else if (nm == "icp_nsel") { src = d.icp_nsel; sz = 16; }
+    else if (nm == "icp_select" || nm == "icp_w") {
+        int nsel = 0;
+        CK(cudaMemcpy(&nsel, d.icp_nsel + level, 4, cudaMemcpyDeviceToHost));
+        src = (nm == "icp_select") ? (const void *)d.icp_select : (const void *)d.icp_w;
+        sz = (int64_t)nsel * 4;
+    } else return fail(RECON_ERR_INVALID_ARG, "unknown array");
+    if (sz > nbytes) return fail(RECON_ERR_INVALID_ARG, "destination too small");
+    CK(cudaStreamSynchronize(b->stream));
+    CK(cudaMemcpy(host_dst, src, sz, cudaMemcpyDeviceToHost));
+    return sz;
+}
+
+int recon_batch_enable_timing(recon_batch *b, int32_t on) {
+    if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
+    CK(cudaStreamSynchronize(b->stream));
+    if ((bool)on != b->timing) b->graph_dirty = true;
+    b->timing = on != 0;
+    for (int k = 0; k < 8; k++) { b->t_ms[k] = 0.0; b->t_cnt[k] = 0; }
+    return RECON_OK;
+}
+
+int recon_batch_get_timing(recon_batch *b, double *ms, int64_t *launches, int32_t reset) {
+    if (!b || !ms || !launches) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    CK(cudaStreamSynchronize(b->stream));
+    collect_events(b, b->direct_events, true);
+    for (int k = 0; k < TK_COUNT; k++) {
+        ms[k] = b->t_ms[k];
+        launches[k] = b->t_cnt[k];
+        if (reset) { b->t_ms[k] = 0.0; b->t_cnt[k] = 0; }
+    }
+    return TK_COUNT;
+}
+
+int recon_batch_get_work(recon_batch *b, uint64_t *out, int32_t reset) {
+    if (!b || !out) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    CK(cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < b->n; i++) {
+        CK(cudaMemcpy(out + 4 * (size_t)i, b->desc[i].work, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        if (reset) CK(cudaMemset(b->desc[i].work, 0, 4 * sizeof(uint64_t)));
+    }
+    return RECON_OK;
+}
+
+void *recon_batch_stream(recon_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+int64_t recon_launch_count(void) { return g_launches.load(); }
+
+// ---- single tracker ----
+int recon_tracker_create(const recon_config *cfg, const float *calib, void *stream, recon_tracker **out) {
+    return recon_batch_create(1, cfg, calib, stream, out);
+}
+int recon_tracker_destroy(recon_tracker *t) { return recon_batch_destroy(t); }
+int recon_set_reference(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device) {
+    if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
+    int rc = recon_batch_set_reference(t, &gray, &depth, on_device);
+    if (rc == RECON_OK) identity16(t->T_prev);
+    return rc;
+}
+int recon_set_current(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device) {
+    return recon_batch_set_current(t, &gray, &depth, on_device);
+}
+
+// applyIncrement, phototracker.cpp:514-531: Tinc = inv(T_prev)^-1 ... in double
+static void apply_increment(recon_tracker *t, const float *Tnew) {
+    // the tracker pose maps reference -> current; the camera motion since the
+    // previous frame is inv(Tprev) composed with Tnew's inverse direction
+    double Tp[16], iTp[16], Tn[16], iTn[16], inc[16], g[16];
+    for (int i = 0; i < 16; i++) { Tp[i] = t->T_prev[i]; Tn[i] = Tnew[i]; }
+    auto inv = [](const double *M, double *Mi) {
+        Mi[0] = M[0]; Mi[1] = M[4]; Mi[2] = M[8];   Mi[3] = -(M[0] * M[3] + M[4] * M[7] + M[8] * M[11]);
+        Mi[4] = M[1]; Mi[5] = M[5]; Mi[6] = M[9];   Mi[7] = -(M[1] * M[3] + M[5] * M[7] + M[9] * M[11]);
+        Mi[8] = M[2]; Mi[9] = M[6]; Mi[10] = M[10]; Mi[11] = -(M[2] * M[3] + M[6] * M[7] + M[10] * M[11]);
+        Mi[12] = 0;   Mi[13] = 0;   Mi[14] = 0;     Mi[15] = 1;
+    };
+    auto mul = [](const double *A, const double *B, double *C) {
+        double t2[16];
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++) {
+                double s = 0;
+                for (int k = 0; k < 4; k++) s += A[r * 4 + k] * B[k * 4 + c];
+                t2[r * 4 + c] = s;
+            }
+        memcpy(C, t2, sizeof(t2));
+    };
+    inv(Tp, iTp);
+    inv(Tn, iTn);
+    (void)iTp;
+    mul(Tp, iTn, inc);  // previous -> new camera motion
+    mul(t->global_pose, inc, g);
+    memcpy(t->global_pose, g, sizeof(g));
+    memcpy(t->T_prev, Tnew, 16 * sizeof(float));
+}
+
+int recon_track(recon_tracker *t, float T_io[16], recon_track_stats *stats) {
+    if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
+    float T[16];
+    if (T_io) memcpy(T, T_io, sizeof(T));
+    int rc = recon_batch_track_async(t, T_io ? T : nullptr);
+    if (rc) return rc;
+    rc = recon_batch_get_poses(t, T, stats);
+    if (rc) return rc;
+    apply_increment(t, T);
+    if (T_io) memcpy(T_io, T, sizeof(T));
+    return stats ? stats[0].status : RECON_OK;
+}
+int recon_set_iterations(recon_tracker *t, const int32_t iters[RECON_MAX_LEVELS]) {
+    return recon_batch_set_iterations(t, 0, iters);
+}
+int recon_set_mode(recon_tracker *t, int32_t mode, float lambda) { return recon_batch_set_mode(t, 0, mode, lambda); }
+int recon_get_relative_pose(recon_tracker *t, float T[16]) {
+    if (!t || !T) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    return recon_batch_get_poses(t, T, nullptr);
+}
+int recon_get_global_pose(recon_tracker *t, double T[16]) {
+    if (!t || !T) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    memcpy(T, t->global_pose, sizeof(t->global_pose));
+    return RECON_OK;
+}
+int recon_reset(recon_tracker *t) {
+    if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
+    identity16d(t->global_pose);
+    identity16(t->T_prev);
+    float I[16];
+    identity16(I);
+    CK(cudaMemcpyAsync(t->desc[0].T, I, sizeof(I), cudaMemcpyHostToDevice, t->stream));
+    CK(cudaStreamSynchronize(t->stream));
+    t->have_ref = false;
+    t->have_cur = false;
+    return RECON_OK;
+}
+
+// ---- renderer ----
+int recon_render_depth(const void *scene, const void *camera, float noise_rel, uint32_t noise_seed, uint32_t frame,
+                       uint16_t *depth_dev, void *stream) {
+    if (!scene || !camera || !depth_dev) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    recon_scene sc;
+    recon_camera cam;
+    memcpy(&sc, scene, sizeof(sc));
+    memcpy(&cam, camera, sizeof(cam));
+    int n = cam.width * cam.height;
+    k_render_depth<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(sc, cam, noise_rel, noise_seed, frame, depth_dev);
+    g_launches += 1;
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int recon_render_gray(const void *scene, const void *camera, uint8_t *gray_dev, void *stream) {
+    if (!scene || !camera || !gray_dev) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    recon_scene sc;
+    recon_camera cam;
+    memcpy(&sc, scene, sizeof(sc));
+    memcpy(&cam, camera, sizeof(cam));
+    int n = cam.width * cam.height;
+    k_render_gray<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(sc, cam, gray_dev);
+    g_launches += 1;
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,914 @@
+// kernels.cu -- sm_103a kernels of the dense RGB-D tracking hot path.
+//
+// Compiled with -fmad=false: every FP32/FP64 expression is rounded operation by
+// operation in the reference's source order, so the results reproduce the
+// reference semantics (and the CPU oracle) bit for bit.  One launch serves all
+// tracker instances of a batch (blockIdx.y = instance).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "scene.h"
+#include "solve.cuh"
+#include "track_kernels.cuh"
+#include "track_math.cuh"
+
+namespace rt {
+
+#define INST_DESC const InstDesc &d = D[blockIdx.y]
+
+// ------------------------------------------------------------------
+// input conversion and pyramids
+// ------------------------------------------------------------------
+
+// uint8 gray -> [0,1], uint16 mm -> z = -mm (rgb2gray.cu:64-76 for the u8/u16
+// form); the current frame also gets its ICP cloud (genPointsCloud6Kernel,
+// d2z.cu:436-469) and the reference its xyz + mask (convertZMapToXYZ6Kernel,
+// rgb2gray.cu:595-624; the same formula as convertZMapToXYZKernel, 570-593).
+__global__ void k_convert_level0(const InstDesc *D, int is_ref, const uint8_t *const *in_gray,
+                                 const uint16_t *const *in_depth, const float *const *in_rgbd) {
+    INST_DESC;
+    const uint8_t *gp = in_gray[blockIdx.y];
+    const uint16_t *dp = in_depth[blockIdx.y];
+    const float *fp = in_rgbd[blockIdx.y];
+    if (!fp && (!gp || !dp)) return;  // instance not updated by this call
+    int n = d.W * d.H;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float g, z;
+    if (fp) {
+        // rgbTex2GrayHdrZKernel: texture read at (x, H-1-y)
+        int xi = i % d.W, yi = i / d.W;
+        float4 p = __ldg((const float4 *)fp + xi + (d.H - 1 - yi) * d.W);
+        g = 0.3f * p.x + 0.59f * p.y + 0.11f * p.z;
+        float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
+        z = -(p.w * (maxDist - minDist) + minDist);
+    } else {
+        g = (float)__ldg(gp + i) / 255.0f;
+        uint16_t dm = __ldg(dp + i);
+        z = dm ? -(float)dm : 0.0f;
+    }
+    int xi = i % d.W, yi = i / d.W;
+    float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
+    float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
+    if (is_ref) {
+        d.ref_gray[0][i] = g;
+        d.ref_z[i] = z;
+        float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (z < -minDist && z > -maxDist) {
+            o.x = ((float)xi - cx) * z / fx;
+            o.y = ((float)yi - cy) * z / fy;
+            o.z = z;
+            o.w = 1.0f;
+        }
+        d.ref_pts[0][i] = o;
+    } else {
+        d.cur_gray[0][i] = g;
+        d.cur_z[i] = z;
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (z < 0) {
+            o.x = ((float)xi - cx) * z / fx;
+            o.y = ((float)yi - cy) * z / fy;
+            o.z = z;
+            o.w = 1.0f;
+        }
+        d.cur_pts[0][i] = o;
+    }
+}
+
+// fastDownSampleHdrKernel (downSample2Cuda.cu:35-42) for the gray pyramid and
+// downSampleCloud6Kernel (d2z.cu:557-588) for the point pyramid.
+__global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    if (level >= d.L) return;
+    int wlo = d.W >> level, hlo = d.H >> level;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= wlo * hlo) return;
+    int x = i % wlo, y = i / wlo;
+    int w2 = 2 * wlo;
+    int h0 = 2 * x + 2 * y * w2;
+    const float *hi = is_ref ? d.ref_gray[level - 1] : d.cur_gray[level - 1];
+    float *lo = is_ref ? d.ref_gray[level] : d.cur_gray[level];
+    lo[i] = (hi[h0] + hi[h0 + 1] + hi[h0 + w2] + hi[h0 + w2 + 1]) / 4.0f;
+
+    const float4 *src = is_ref ? d.ref_pts[level - 1] : d.cur_pts[level - 1];
+    int offs[4] = {h0, h0 + 1, h0 + w2, h0 + w2 + 1};
+    float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+    float ns = 0.0f;
+    for (int k = 0; k < 4; k++) {
+        float4 s = src[offs[k]];
+        if (s.w != 0.0f) {
+            ns++;
+            p0 += s.x;
+            p1 += s.y;
+            p2 += s.z;
+            if (is_ref) {
+                float4 nn = d.ref_nrm[level - 1][offs[k]];
+                n0 += nn.x;
+                n1 += nn.y;
+                n2 += nn.z;
+            }
+        }
+    }
+    if (ns > 0.0f) {
+        p0 /= ns;
+        p1 /= ns;
+        p2 /= ns;
+        if (is_ref) {
+            n0 /= ns;
+            n1 /= ns;
+            n2 /= ns;
+            normalize3(n0, n1, n2);
+            d.ref_nrm[level][i] = make_float4(n0, n1, n2, 0.0f);
+        }
+        float4 o = make_float4(p0, p1, p2, 1.0f);
+        if (is_ref) d.ref_pts[level][i] = o;
+        else d.cur_pts[level][i] = o;
+    } else {
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (is_ref) {
+            d.ref_pts[level][i] = o;
+            d.ref_nrm[level][i] = o;
+        } else {
+            d.cur_pts[level][i] = o;
+        }
+    }
+}
+
+// computeNormalsCudaKernel, d2z.cu:503-537 (reference level 0)
+__global__ void k_normals(const InstDesc *D, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    int W = d.W, H = d.H;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * H) return;
+    int xi = i % W, yi = i / W;
+    float4 me = d.ref_pts[0][i];
+    float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+    float mask = me.w;
+    if (xi < 1 || yi < 1 || xi > W - 2 || yi > H - 2) {
+        mask = 0.0f;
+    } else {
+        float4 x1 = d.ref_pts[0][i - 1], x2 = d.ref_pts[0][i + 1];
+        float4 y1 = d.ref_pts[0][i - W], y2 = d.ref_pts[0][i + W];
+        if (x1.z < 0 && x2.z < 0 && y1.z < 0 && y2.z < 0) {
+            float ux = x2.x - x1.x, uy = x2.y - x1.y, uz = x2.z - x1.z;
+            float vx = y2.x - y1.x, vy = y2.y - y1.y, vz = y2.z - y1.z;
+            float nx = uy * vz - uz * vy;
+            float ny = -(ux * vz - uz * vx);
+            float nz = ux * vy - uy * vx;
+            normalize3(nx, ny, nz);
+            nrm = make_float4(nx, ny, nz, 0.0f);
+        } else {
+            mask = 0.0f;
+        }
+    }
+    d.ref_nrm[0][i] = nrm;
+    // only .w changes; neighbours read x/y/z of this element, which stay the same
+    d.ref_pts[0][i].w = mask;
+}
+
+// ------------------------------------------------------------------
+// photometric reference: vertex records, gradient histogram, selection
+// ------------------------------------------------------------------
+
+// xyz2CloudKernel, d2z.cu:235-331, plus the 256-bin gradient-magnitude
+// histogram (gpu_hist.cu:136, cuda_hist.cu:100-152) with privatised
+// shared-memory integer atomics.
+__global__ void k_xyz2cloud(const InstDesc *D, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    __shared__ int sh[1024];
+    int nb = d.select_bins;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) sh[k] = 0;
+    __syncthreads();
+    int W = d.W, H = d.H, n = W * H;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float4 pt = d.ref_pts[0][i];
+        float *vp = d.vtx;
+        float v[kVtxPlanes];
+        for (int k = 0; k < kVtxPlanes; k++) v[k] = 0.0f;
+        v[2] = -d.calib[RC_MAXD];
+        // convertZMapToXYZKernel zeroes out-of-range pixels, so xyz alone carries
+        // the validity (ref_pts.w is later narrowed by the normal test)
+        float p3x = pt.x, p3y = pt.y, p3z = pt.z;
+        if (p3z < 0) {
+            const float *T = d.calib + RC_TLR;
+            float rx, ry, rz;
+            mul4(T, p3x, p3y, p3z, rx, ry, rz);
+            float pux = rx / rz, puy = ry / rz;
+            float px, py;
+            distort(pux, puy, d.calib + RC_KCR, d.calib + RC_KR, px, py);
+            if (in_bounds10(px, py, W, H)) {
+                const float *img = d.ref_gray[0];
+                int xdi = ftoi(px), ydi = ftoi(py);
+                float fx = px - xdi, fy = py - ydi;
+                float color1 = bilin(xdi, ydi, fx, fy, W, img);
+                float colorN = bilin(ftoi(px), ftoi(py - 1.0f), fx, fy, W, img);
+                float colorE = bilin(ftoi(px + 1.0f), ftoi(py), fx, fy, W, img);
+                float colorW = bilin(ftoi(px - 1.0f), ftoi(py), fx, fy, W, img);
+                float colorS = bilin(ftoi(px), ftoi(py + 1.0f), fx, fy, W, img);
+                float gradX1 = (colorE - colorW) / 2.0f;
+                float gradY1 = (colorS - colorN) / 2.0f;
+                float gm = fabsf(gradY1) + fabsf(gradX1);
+                v[0] = p3x; v[1] = p3y; v[2] = p3z;
+                v[3] = px; v[4] = py;
+                v[5] = gradX1; v[6] = gradY1;
+                v[7] = gm < 1.0f ? gm : 1.0f;
+                v[8] = color1;
+            }
+        }
+        for (int k = 0; k < kVtxPlanes; k++) vp[(size_t)k * n + i] = v[k];
+        unsigned int bin = (unsigned int)(v[7] * (nb - 1) + 0.5f);
+        if (bin < (unsigned)nb) atomicAdd(&sh[bin], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nb; k += blockDim.x)
+        if (sh[k]) atomicAdd(&d.grad_hist[k], sh[k]);
+}
+
+// seekThreshold256Kernel2 (filterIndex256.cu:26-46) + per-segment counts of
+// filterIndexKernel4 (filterIndex256.cu:110-133).  seg layout:
+// [0,512) cnt, [512,1024) mcnt, [1024,1536) start, [1536,2048) mstart,
+// [2048,2560) kept, [3072] thr, [3073] excess, [3074] written.
+__global__ void k_seg_count(const InstDesc *D, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    int nb = d.select_bins, P = d.P;
+    __shared__ unsigned int s_thr;
+    __shared__ int s_excess;
+    if (threadIdx.x == 0) {
+        unsigned int thr = 0;
+        int sel = 0;
+        for (int k = nb - 1; k >= 0; k--) {
+            sel += d.grad_hist[k];
+            if (sel > P) { thr = (unsigned)k; break; }
+        }
+        s_thr = thr;
+        s_excess = sel - P;
+        if (blockIdx.x == 0) {
+            d.seg[3072] = (int)thr;
+            d.seg[3073] = sel - P;
+        }
+    }
+    __syncthreads();
+    int n = d.W * d.H;
+    int ppt = n / kSegments;
+    int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int lane = threadIdx.x & 31;
+    if (warp >= kSegments) return;
+    const float *grad = d.vtx + (size_t)7 * n;
+    unsigned int thr = s_thr;
+    int cnt = 0, mcnt = 0;
+    for (int base = warp * ppt; base < warp * ppt + ppt; base += 32) {
+        int i = base + lane;
+        bool in = i < warp * ppt + ppt;
+        unsigned int q = in ? (unsigned int)(grad[i] * (nb - 1) + 0.5f) : 0u;
+        unsigned int ab = __ballot_sync(0xffffffffu, in && q > thr);
+        unsigned int me = __ballot_sync(0xffffffffu, in && q == thr);
+        cnt += __popc(ab);
+        mcnt += __popc(me);
+    }
+    if (lane == 0) {
+        d.seg[warp] = cnt;
+        d.seg[512 + warp] = mcnt;
+    }
+}
+
+// segment start offsets and the reference's sequential trimming of surplus
+// threshold-bin points (filterIndex256.cu:136-157), one CTA per instance
+__global__ void k_seg_scan(const InstDesc *D, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    if (threadIdx.x != 0) return;
+    int *cnt = d.seg, *mcnt = d.seg + 512, *start = d.seg + 1024, *mstart = d.seg + 1536, *kept = d.seg + 2048;
+    int tooMuch = d.seg[3073];
+    start[0] = 0;
+    for (int i = 1; i < kSegments; i++) start[i] = start[i - 1] + cnt[i - 1];
+    for (int i = 0; i < kSegments; i++) kept[i] = mcnt[i];
+    mstart[0] = start[kSegments - 1] + cnt[kSegments - 1];
+    for (int i = 1; i < kSegments; i++) {
+        if (tooMuch > 0 && kept[i - 1] > 0) {
+            kept[i - 1] -= tooMuch;
+            if (kept[i - 1] < 0) {
+                tooMuch += kept[i - 1];
+                kept[i - 1] = 0;
+            } else {
+                tooMuch = 0;
+            }
+        }
+        mstart[i] = mstart[i - 1] + kept[i - 1];
+    }
+    d.seg[3074] = mstart[kSegments - 1] + kept[kSegments - 1];
+}
+
+// filterIndexKernel4's scatter (filterIndex256.cu:159-168): one warp per segment
+__global__ void k_seg_scatter(const InstDesc *D, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    int nb = d.select_bins, P = d.P;
+    int n = d.W * d.H;
+    int ppt = n / kSegments;
+    int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int lane = threadIdx.x & 31;
+    if (warp >= kSegments) return;
+    const float *grad = d.vtx + (size_t)7 * n;
+    unsigned int thr = (unsigned int)d.seg[3072];
+    int pos_a = d.seg[1024 + warp];
+    int pos_m = d.seg[1536 + warp];
+    int kept = d.seg[2048 + warp];
+    int m = 0;
+    unsigned int lower = (1u << lane) - 1u;
+    for (int base = warp * ppt; base < warp * ppt + ppt; base += 32) {
+        int i = base + lane;
+        bool in = i < warp * ppt + ppt;
+        unsigned int q = in ? (unsigned int)(grad[i] * (nb - 1) + 0.5f) : 0u;
+        bool ia = in && q > thr, im = in && q == thr;
+        unsigned int ab = __ballot_sync(0xffffffffu, ia);
+        unsigned int me = __ballot_sync(0xffffffffu, im);
+        if (ia) {
+            int pos = pos_a + __popc(ab & lower);
+            if (pos < P) d.sel_idx[pos] = i;
+        }
+        if (im) {
+            int r = m + __popc(me & lower);
+            if (r < kept) {
+                int pos = pos_m + r;
+                if (pos < P) d.sel_idx[pos] = i;
+            }
+        }
+        pos_a += __popc(ab);
+        m += __popc(me);
+    }
+}
+
+// addVertexAttributesWithoutNormalsKernel3/4 (d2z.cu:700-936) and
+// precomputeJacobian4Kernel (warp.cu:502-645), fused per selected point.
+__global__ void k_attr_jac(const InstDesc *D, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    int P = d.P, L = d.L, W = d.W, H = d.H, n = W * H;
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P) return;
+    int pix = d.sel_idx[k];
+    const float *v = d.vtx;
+    float p3x = v[pix], p3y = v[(size_t)n + pix], p3z = v[(size_t)2 * n + pix];
+    float gx[kMaxLevels] = {0, 0, 0, 0}, gy[kMaxLevels] = {0, 0, 0, 0}, col[kMaxLevels] = {0, 0, 0, 0};
+    gx[0] = v[(size_t)5 * n + pix];
+    gy[0] = v[(size_t)6 * n + pix];
+    col[0] = v[(size_t)8 * n + pix];
+    const float *T = d.calib + RC_TLR;
+    const float *kc = d.calib + RC_KCR;
+    const float *KR = d.calib + RC_KR;
+    float rx, ry, rz;
+    mul4(T, p3x, p3y, p3z, rx, ry, rz);
+    {
+        float pux = rx / rz, puy = ry / rz;
+        float px, py;
+        distort(pux, puy, kc, KR, px, py);
+        if (in_bounds10(px, py, W, H)) {
+            float a = 0.5f, b = -0.25f;
+            float lx = px, ly = py;
+            for (int l = 1; l < L; l++) {
+                lx = a * lx + b;
+                ly = a * ly + b;
+                int wl = W >> l, hl = H >> l;
+                int xdi = ftoi(lx), ydi = ftoi(ly);
+                float fracX = lx - xdi, fracY = ly - ydi;
+                const float *g = d.ref_gray[l];
+                col[l] = bilin_clamped(xdi, ydi, fracX, fracY, wl, hl, g);
+                float cN = bilin_clamped(xdi, ydi - 1, fracX, fracY, wl, hl, g);
+                float cW = bilin_clamped(xdi - 1, ydi, fracX, fracY, wl, hl, g);
+                float cE = bilin_clamped(xdi + 1, ydi, fracX, fracY, wl, hl, g);
+                float cS = bilin_clamped(xdi, ydi + 1, fracX, fracY, wl, hl, g);
+                gx[l] = (cE - cW) / 2.0f;
+                gy[l] = (cS - cN) / 2.0f;
+            }
+        }
+    }
+    d.sel_xyz[k] = p3x;
+    d.sel_xyz[P + k] = p3y;
+    d.sel_xyz[2 * P + k] = p3z;
+    for (int l = 0; l < L; l++) d.sel_I[l][k] = col[l];
+
+    // precomputeJacobian4Kernel
+    float optScaleIn = d.opt_in;
+    rx *= optScaleIn;
+    ry *= optScaleIn;
+    rz *= optScaleIn;
+    float dN0 = 1.0f / rz, dN1 = 0, dN2 = -rx / (rz * rz);
+    float dN3 = 0, dN4 = 1.0f / rz, dN5 = -ry / (rz * rz);
+    float x = rx / rz;
+    float y = ry / rz;
+    float x2 = x * x, y2 = y * y;
+    float x4 = x2 * x2, y4 = y2 * y2;
+    float r2 = x2 + y2, r4 = r2 * r2;
+    float dD0 = 1 + kc[0] * (3 * x2 + y2) + kc[1] * (5 * x4 + 6 * x2 * y2 + y4) + kc[4] * r4 * (7 * x2 + y2);
+    float dD1 = kc[0] * 2 * x * y + kc[1] * 4 * x * y * r2 + kc[4] * 6 * x * y * r4;
+    float dD2 = kc[0] * 2 * y * x + kc[1] * 4 * x * y * r2 + kc[4] * 6 * x * y * r4;
+    float dD3 = 1 + kc[0] * (3 * x2 + y2) + kc[1] * (5 * x4 + 6 * x2 * y2 + y4) + kc[4] * r4 * (7 * y2 + x2);
+    const float dps[6][3] = {{0.0f, -rz, ry}, {rz, 0.0f, -rx}, {-ry, rx, 0.0f},
+                             {1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+        float drx, dry, drz;
+        rot4(T, dps[c][0], dps[c][1], dps[c][2], drx, dry, drz);
+        float dpnx = dN0 * drx + dN1 * dry + dN2 * drz;
+        float dpny = dN3 * drx + dN4 * dry + dN5 * drz;
+        float ddx = dD0 * dpnx + dD1 * dpny;
+        float ddy = dD2 * dpnx + dD3 * dpny;
+        float ddz = 0;
+        float dp2x, dp2y, dp2z;
+        mul3(KR, ddx, ddy, ddz, dp2x, dp2y, dp2z);
+        for (int l = 0; l < L; l++) {
+            float val;
+            if (l == 0) val = dp2x * gx[0] + dp2y * gy[0];
+            else {
+                float s = (l == 1) ? 2.0f : (l == 2 ? 4.0f : 8.0f);
+                val = (dp2x / s) * gx[l] + (dp2y / s) * gy[l];
+            }
+            d.sel_J[l][c * P + k] = val;
+        }
+    }
+}
+
+// ------------------------------------------------------------------
+// ICP: correspondence mask, compaction, Student-t weights
+// ------------------------------------------------------------------
+
+// icpResidualKernel2, rgb2gray.cu:223-260: full-grid residual and mask at a
+// level; per-block (1024 pixels) valid counts for the stable compaction.
+__global__ void k_icp_mask(const InstDesc *D, int level) {
+    INST_DESC;
+    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
+    if (d.iters[d.L - 1 - level] <= 0) return;
+    int w = d.W >> level, h = d.H >> level, n = w * h;
+    __shared__ int s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 4) d.icp_var[threadIdx.x] = 0ull;
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.work[2] += (unsigned long long)n;
+    __syncthreads();
+    const float *T = d.T;
+    const float *K = d.calib + RC_KL;
+    float a = 1.0f / (float)(1 << level);
+    float b = 0.5f * (a - 1.0f);
+    int cnt = 0;
+    for (int m = 0; m < 4; m++) {
+        int i = blockIdx.x * kChunk + threadIdx.x + kLanes * m;
+        if (i >= n) break;
+        uint8_t ok = 0;
+        float res = 0.0f;
+        float4 p = d.ref_pts[level][i];
+        if (p.w != 0.0f) {
+            float4 rn = d.ref_nrm[level][i];
+            float qx, qy, qz, cnx, cny, cnz;
+            mul4(T, p.x, p.y, p.z, qx, qy, qz);
+            rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
+            float q2x = qx / qz, q2y = qy / qz;
+            float p2x = a * (K[0] * q2x + K[2]) + b;
+            float p2y = a * (K[4] * q2y + K[5]) + b;
+            if (p2x >= 0 && p2x < (w - 1) && p2y >= 0 && p2y < (h - 1)) {
+                int xdi = ftoi(p2x), ydi = ftoi(p2y);
+                int off2 = xdi + ydi * w;
+                float fx = p2x - xdi, fy = p2y - ydi;
+                float cx, cy, cz, m0, m1, m2, m3;
+                bilin_pts(d.cur_pts[level], off2, w, fx, fy, cx, cy, cz, m0, m1, m2, m3);
+                if (m0 != 0.0f && m1 != 0.0f && m2 != 0.0f && m3 != 0.0f) {
+                    float dx = cx - qx, dy = cy - qy, dz = cz - qz;
+                    res = dx * cnx + dy * cny + dz * cnz;
+                    ok = 1;
+                }
+            }
+        }
+        d.icp_res[i] = res;
+        d.icp_mask[i] = ok;
+        cnt += ok;
+    }
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&s_cnt, cnt);
+    __syncthreads();
+    if (threadIdx.x == 0) d.icp_blkcnt[blockIdx.x] = s_cnt;
+}
+
+__device__ __forceinline__ long long trunc_prod(float r2, float w) {
+    float prod = r2 * w;
+    return (prod >= 0.0f && prod < 9.0e18f) ? (long long)prod : (prod >= 9.0e18f ? 9000000000000000000LL : 0);
+}
+
+__device__ __forceinline__ void block_add_ll(unsigned long long *dst, long long v) {
+    __shared__ long long s_acc;
+    if (threadIdx.x == 0) s_acc = 0;
+    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long *)&s_acc, (unsigned long long)v);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_acc != 0) atomicAdd(dst, (unsigned long long)s_acc);
+}
+
+// selectValidIndex + packIndex + initWeightsKernel (rgb2gray.cu:395-475,
+// 827-850): stable compaction in pixel order, r^2, first Student-t weight and
+// the first variance sum (exact int64 sum of truncated products).
+__global__ void k_icp_compact(const InstDesc *D, int level) {
+    INST_DESC;
+    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
+    if (d.iters[d.L - 1 - level] <= 0) return;
+    int w = d.W >> level, h = d.H >> level, n = w * h;
+    int nblk = (n + kChunk - 1) / kChunk;
+    if ((int)blockIdx.x >= nblk) return;
+    __shared__ int s_base, s_tot;
+    __shared__ int s_warp[8];
+    if (threadIdx.x < 32) {
+        int pre = 0, tot = 0;
+        for (int k = threadIdx.x; k < nblk; k += 32) {
+            int c = d.icp_blkcnt[k];
+            tot += c;
+            if (k < (int)blockIdx.x) pre += c;
+        }
+        pre = __reduce_add_sync(0xffffffffu, pre);
+        tot = __reduce_add_sync(0xffffffffu, tot);
+        if (threadIdx.x == 0) { s_base = pre; s_tot = tot; }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.icp_nsel[level] = s_tot;
+    int base = s_base;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    long long vsum = 0;
+    for (int m = 0; m < 4; m++) {
+        int i = blockIdx.x * kChunk + threadIdx.x + kLanes * m;
+        int f = (i < n) ? d.icp_mask[i] : 0;
+        unsigned int bal = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_warp[wid] = __popc(bal);
+        __syncthreads();
+        int wbase = 0;
+        for (int k = 0; k < wid; k++) wbase += s_warp[k];
+        int tot = 0;
+        for (int k = 0; k < 8; k++) tot += s_warp[k];
+        if (f) {
+            int pos = base + wbase + __popc(bal & ((1u << lane) - 1u));
+            float r = d.icp_res[i];
+            float r2 = r * r;
+            float w0 = 6 / (5 + r2 / 100.0f);
+            d.icp_select[pos] = i;
+            d.icp_r2[pos] = r2;
+            d.icp_w[pos] = w0;
+            vsum += trunc_prod(r2, w0);
+        }
+        base += tot;
+        __syncthreads();
+    }
+    block_add_ll(&d.icp_var[0], vsum);
+}
+
+// updateWeightsKernel / clampWeightsKernel (rgb2gray.cu:549-569) with the
+// variance of the previous pass; the final pass clamps at 1.
+__global__ void k_icp_student(const InstDesc *D, int level, int pass) {
+    INST_DESC;
+    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
+    if (d.iters[d.L - 1 - level] <= 0) return;
+    int nsel = d.icp_nsel[level];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    long long vsum = 0;
+    if (i < nsel) {
+        float Sf = (float)(long long)d.icp_var[pass - 1];
+        float minVal = (float)nsel;
+        float var = (nsel <= 1024) ? Sf : (Sf < minVal ? minVal : Sf);
+        float sigma2 = var / (float)nsel;
+        float r2 = d.icp_r2[i];
+        float wv = 6 / (5 + r2 / sigma2);
+        if (pass == 3) wv = fminf(wv, 1.0f);
+        else vsum = trunc_prod(r2, wv);
+        d.icp_w[i] = wv;
+    }
+    if (pass < 3) block_add_ll(&d.icp_var[pass], vsum);
+}
+
+// ------------------------------------------------------------------
+// one Gauss-Newton iteration for every instance
+// ------------------------------------------------------------------
+
+struct IterShared {
+    float T[16];
+    double wpart[8][27];
+    double tot[27];
+    double A_ph[27], A_icp[27];
+    int hist[256];
+    int median;
+    int last;
+    SolveScratch S;
+};
+
+// canonical per-lane accumulation of the 27 normal-equation terms
+__device__ __forceinline__ void acc27(float *s, const float *j, float r) {
+    int q = 0;
+#pragma unroll
+    for (int a = 0; a < 6; a++)
+#pragma unroll
+        for (int c = a; c < 6; c++) s[q++] += j[a] * j[c];
+#pragma unroll
+    for (int c = 0; c < 6; c++) s[q++] += j[c] * r;
+}
+
+// warp butterfly (xor 16..1) in FP32, then the chunk value in FP64 summed
+// over the CTA's 8 warps in warp order; accumulated into sh.tot.
+__device__ __forceinline__ void chunk_fold(IterShared &sh, float *s) {
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+        float v = s[q];
+        for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh.wpart[wid][q] = (double)v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        int q = threadIdx.x;
+        double c = 0.0;
+        for (int w = 0; w < 8; w++) c = c + sh.wpart[w][q];
+        sh.tot[q] = sh.tot[q] + c;
+    }
+    __syncthreads();
+}
+
+__device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
+    int P = d.P;
+    int w = d.W >> level, h = d.H >> level;
+    float a = 1.0f / (float)(1 << level);
+    float b = 0.5f * (a - 1.0f);
+    const float *img = d.cur_gray[level];
+    const float *I = d.sel_I[level];
+    int nb = d.hist_bins;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) sh.hist[k] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        float r, zw;
+        photo_residual(d.calib, sh.T, a, b, d.sel_xyz[i], d.sel_xyz[P + i], d.sel_xyz[2 * P + i], I[i], img, w, h,
+                       d.cur_z, d.W, d.H, r, zw);
+        d.ph_r[i] = r;
+        d.ph_zw[i] = zw;
+        atomicAdd(&sh.hist[mad_bin(r, nb)], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // first bin whose cumulative count exceeds P/2 (seekThreshold64Kernel, histogram64.cu:48-61)
+        int lane = threadIdx.x;
+        int per = (nb + 31) / 32;
+        int loc = 0;
+        for (int k = 0; k < per; k++) {
+            int bin = lane * per + k;
+            if (bin < nb) loc += sh.hist[bin];
+        }
+        int incl = loc;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        int half = P / 2;
+        unsigned int over = __ballot_sync(0xffffffffu, incl > half);
+        int med = 0;
+        if (over) {
+            int l0 = __ffs(over) - 1;
+            if (lane == l0) {
+                int acc = incl - loc;
+                for (int k = 0; k < per; k++) {
+                    int bin = lane * per + k;
+                    if (bin < nb) {
+                        acc += sh.hist[bin];
+                        if (acc > half) { med = bin; break; }
+                    }
+                }
+                sh.median = med;
+            }
+        } else if (lane == 0) {
+            sh.median = 0;
+        }
+    }
+    for (int q = threadIdx.x; q < 27; q += blockDim.x) sh.tot[q] = 0.0;
+    __syncthreads();
+    float s = mad_scale(sh.median, nb);
+    const float *J = d.sel_J[level];
+    int t = threadIdx.x;
+    for (int c = 0; c < P / kChunk; c++) {
+        float acc[27];
+#pragma unroll
+        for (int q = 0; q < 27; q++) acc[q] = 0.0f;
+        for (int m = 0; m < 4; m++) {
+            int i = c * kChunk + t + kLanes * m;
+            float r = d.ph_r[i];
+            float wv = tukey_weight(r, d.ph_zw[i], s);
+            float jw[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) jw[k] = J[k * P + i] * wv;
+            acc27(acc, jw, r * wv);
+        }
+        chunk_fold(sh, acc);
+    }
+    if (threadIdx.x < 27) {
+        sh.A_ph[threadIdx.x] = sh.tot[threadIdx.x];
+        d.ph_part[threadIdx.x] = sh.tot[threadIdx.x];
+    }
+}
+
+// icpResidualIndexKernel2, rgb2gray.cu:323-390, for one point
+__device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int level, int idx, int nsel, float *j,
+                                          float &res) {
+    res = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 6; c++) j[c] = 0.0f;
+    if (idx >= nsel) return;
+    int w = d.W >> level, h = d.H >> level;
+    const float *K = d.calib + RC_KL;
+    float a = 1.0f / (float)(1 << level);
+    float b = 0.5f * (a - 1.0f);
+    int sel = d.icp_select[idx];
+    float4 p = d.ref_pts[level][sel];
+    float4 rn = d.ref_nrm[level][sel];
+    float qx, qy, qz, cnx, cny, cnz;
+    mul4(T, p.x, p.y, p.z, qx, qy, qz);
+    rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
+    float q2x = qx / qz, q2y = qy / qz;
+    float p2x = a * (K[0] * q2x + K[2]) + b;
+    float p2y = a * (K[4] * q2y + K[5]) + b;
+    if (!(p2x >= 0 && p2x < (w - 1) && p2y >= 0 && p2y < (h - 1))) return;
+    float weight = d.icp_w[idx];
+    int xdi = ftoi(p2x), ydi = ftoi(p2y);
+    float fx = p2x - xdi, fy = p2y - ydi;
+    int off2 = xdi + ydi * w;
+    float cx, cy, cz, m0, m1, m2, m3;
+    bilin_pts(d.cur_pts[level], off2, w, fx, fy, cx, cy, cz, m0, m1, m2, m3);
+    if (!(m0 != 0.0f && weight > 0.0f && fabsf(cz - qz) < 300.0f)) return;
+    float optScaleIn = d.opt_in;
+    float rvx = cx - qx, rvy = cy - qy, rvz = cz - qz;
+    res = optScaleIn * weight * (rvx * cnx + rvy * cny + rvz * cnz);
+    const float dP[3][3] = {{0, -p.z, p.y}, {p.z, 0, -p.x}, {-p.y, p.x, 0}};
+    const float dNv[3][3] = {{0, -rn.z, rn.y}, {rn.z, 0, -rn.x}, {-rn.y, rn.x, 0}};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float bx, by, bz, nx, ny, nz;
+        rot4(T, dP[c][0], dP[c][1], dP[c][2], bx, by, bz);
+        rot4(T, dNv[c][0], dNv[c][1], dNv[c][2], nx, ny, nz);
+        j[c] = -optScaleIn * weight * (-cnx * bx - cny * by - cnz * bz + rvx * nx + rvy * ny + rvz * nz);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float e0 = c == 0 ? 1.0f : 0.0f, e1 = c == 1 ? 1.0f : 0.0f, e2 = c == 2 ? 1.0f : 0.0f;
+        float bx, by, bz;
+        rot4(T, e0, e1, e2, bx, by, bz);
+        j[3 + c] = -weight * (-cnx * bx - cny * by - cnz * bz);
+    }
+}
+
+__device__ void icp_chunk(const InstDesc &d, IterShared &sh, int level, int chunk, int nsel) {
+    for (int q = threadIdx.x; q < 27; q += blockDim.x) sh.tot[q] = 0.0;
+    __syncthreads();
+    float acc[27];
+#pragma unroll
+    for (int q = 0; q < 27; q++) acc[q] = 0.0f;
+    for (int m = 0; m < 4; m++) {
+        int idx = chunk * kChunk + threadIdx.x + kLanes * m;
+        float j[6], r;
+        icp_point(d, sh.T, level, idx, nsel, j, r);
+        acc27(acc, j, r);
+    }
+    chunk_fold(sh, acc);
+    if (threadIdx.x < 27) d.icp_part[(size_t)chunk * 27 + threadIdx.x] = sh.tot[threadIdx.x];
+}
+
+__device__ __forceinline__ void unpack27(const double *t, double *A, double *b) {
+    int q = 0;
+    for (int j = 0; j < 6; j++)
+        for (int i = j; i < 6; i++) {
+            A[i + j * 6] = t[q];
+            A[i * 6 + j] = t[q];
+            q++;
+        }
+    for (int c = 0; c < 6; c++) b[c] = t[q++];
+}
+
+// One GN iteration at `level`, iteration `it`.  blockIdx.x == 0 is the
+// photometric CTA (updateLinearSystem, phototracker.cpp:505-511); blockIdx.x
+// >= 1 are ICP chunks (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).
+// The last CTA of an instance to finish fuses (linearFuse, shapetracker.cpp:392-394),
+// solves and applies the SE(3) update (estimateIncrement, phototracker.cpp:646-664).
+__global__ void __launch_bounds__(256) k_iter(const InstDesc *D, int level, int it) {
+    INST_DESC;
+    if (level >= d.L) return;
+    if (it >= d.iters[d.L - 1 - level]) return;
+    bool use_ph = d.mode != RECON_GEOMETRIC;
+    bool use_icp = d.mode != RECON_PHOTOMETRIC;
+    int nsel = use_icp ? d.icp_nsel[level] : 0;
+    int nchunks = (nsel + kChunk - 1) / kChunk;
+    // CTA 0 always takes part (it carries the photometric term when the mode
+    // has one), so every iteration is finalised exactly once
+    int expected = 1 + nchunks;
+    int role = blockIdx.x;
+    if (role >= 1 && role - 1 >= nchunks) return;
+    __shared__ IterShared sh;
+    if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
+    __syncthreads();
+    if (role == 0) {
+        if (use_ph) photo_iteration(d, sh, level);
+    } else {
+        icp_chunk(d, sh, level, role - 1, nsel);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int ticket = atomicAdd(d.counter, 1u);
+        sh.last = (ticket == (unsigned)(expected - 1));
+    }
+    __syncthreads();
+    if (!sh.last) return;
+    __threadfence();
+    // ---- finalize: ICP totals in chunk order, fuse, solve, update ----
+    if (threadIdx.x < 27) {
+        int q = threadIdx.x;
+        double tot = 0.0;
+        for (int c = 0; c < nchunks; c++) tot = tot + __ldcg(d.icp_part + (size_t)c * 27 + q);
+        sh.A_icp[q] = tot;
+        if (use_ph) sh.A_ph[q] = __ldcg(d.ph_part + q);
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    int lane = threadIdx.x;
+    SolveScratch &S = sh.S;
+    bool ok = true;
+    if (lane == 0) {
+        double Aph[36], bph[6], Aic[36], bic[6];
+        for (int i = 0; i < 36; i++) { Aph[i] = 0.0; Aic[i] = 0.0; }
+        for (int i = 0; i < 6; i++) { bph[i] = 0.0; bic[i] = 0.0; }
+        if (use_ph) unpack27(sh.A_ph, Aph, bph);
+        if (use_icp && nsel > 0) unpack27(sh.A_icp, Aic, bic);
+        if (d.mode == RECON_PHOTOMETRIC) {
+            for (int i = 0; i < 36; i++) S.A[i] = Aph[i];
+            for (int i = 0; i < 6; i++) S.b[i] = bph[i];
+        } else if (d.mode == RECON_GEOMETRIC) {
+            for (int i = 0; i < 36; i++) S.A[i] = Aic[i];
+            for (int i = 0; i < 6; i++) S.b[i] = bic[i];
+        } else {
+            // linearFuseKernel (warp.cu:918-924) in FP64: (1-lambda)/N1 * photo + lambda/N2 * icp
+            double c1 = (double)(1.0f - d.lambda) / (double)d.P;
+            double c2 = (double)d.lambda / (double)nsel;
+            for (int i = 0; i < 36; i++) S.A[i] = c1 * Aph[i] + c2 * Aic[i];
+            for (int i = 0; i < 6; i++) S.b[i] = c1 * bph[i] + c2 * bic[i];
+        }
+        if (d.trace && it >= 0) {
+            int slot = *d.trace_count;
+            if (slot < d.trace_max) {
+                recon_iter_trace *tr = d.trace + slot;
+                for (int i = 0; i < 36; i++) { tr->A[i] = S.A[i]; tr->A_ph[i] = Aph[i]; tr->A_icp[i] = Aic[i]; }
+                for (int i = 0; i < 6; i++) { tr->b[i] = S.b[i]; tr->b_ph[i] = bph[i]; tr->b_icp[i] = bic[i]; }
+            }
+        }
+    }
+    if (use_icp && nsel <= 0) ok = false;  // ShapeTracker "not enough points": no solve
+    __syncwarp();
+    int st = 0;
+    if (ok) st = wsolve_update(S, d.solver, sh.T, (double)d.opt_out, lane);
+    if (lane < 16) d.T[lane] = sh.T[lane];
+    if (lane == 0) {
+        d.stats[ST_ITERS] += 1;
+        if (ok) d.stats[ST_SOLVES] += 1;
+        if (st != 0) d.stats[ST_NONSPD] += 1;
+        if (use_ph) d.stats[ST_MEDIAN] = sh.median;
+        if (use_ph) d.work[0] += (unsigned long long)d.P;
+        if (use_icp) d.work[1] += (unsigned long long)nsel;
+        if (use_icp) d.stats[ST_ICPSEL0 + level] = nsel;
+        if (d.trace) {
+            int slot = *d.trace_count;
+            if (slot < d.trace_max) {
+                recon_iter_trace *tr = d.trace + slot;
+                tr->level = level;
+                tr->iter = it;
+                tr->mode = d.mode;
+                tr->solved = ok ? 1 : 0;
+                tr->status = st;
+                tr->icp_selected = use_icp ? nsel : 0;
+                for (int i = 0; i < 16; i++) tr->T[i] = sh.T[i];
+                tr->median_bin = use_ph ? sh.median : -1;
+                for (int k = 0; k < 256; k++) tr->hist[k] = (use_ph && k < d.hist_bins) ? sh.hist[k] : 0;
+            }
+            *d.trace_count = slot + 1;
+        }
+        *d.counter = 0u;
+    }
+}
+
+// ------------------------------------------------------------------
+// procedural renderer
+// ------------------------------------------------------------------
+
+__global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
+                               uint16_t *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cam.width * cam.height) return;
+    out[i] = scene_depth_pixel(&sc, &cam, i % cam.width, i / cam.width, noise_rel, seed, frame);
+}
+
+__global__ void k_render_gray(recon_scene sc, recon_camera cam, uint8_t *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cam.width * cam.height) return;
+    out[i] = scene_gray_pixel(&sc, &cam, i % cam.width, i / cam.width);
+}
+
+}  // namespace rt

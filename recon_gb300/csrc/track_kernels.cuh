@@ -1,0 +1,64 @@
+// track_kernels.cuh -- device-side instance descriptor shared by the kernels
+// and the host code of librecon_track.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/recon_track.h"
+
+namespace rt {
+
+constexpr int kMaxLevels = 4;
+constexpr int kChunk = 1024;     // canonical reduction chunk (points)
+constexpr int kLanes = 256;      // lanes per chunk, 4 points each
+constexpr int kSegments = 512;   // pixel-selection segments (filterIndex256.cu:183)
+constexpr int kVtxPlanes = 9;    // x y z px py gx gy gmag gray
+
+enum StatSlot { ST_ITERS = 0, ST_SOLVES, ST_NONSPD, ST_STATUS, ST_MEDIAN, ST_ICPSEL0, ST_COUNT = 16 };
+
+struct InstDesc {
+    int W, H, L, P;
+    int hist_bins, select_bins, mode, solver;
+    float lambda, opt_in, opt_out;
+    int precision;
+    int iters[kMaxLevels];
+    float calib[RECON_CALIB_SIZE];
+    // reference (keyframe)
+    float *ref_gray[kMaxLevels];
+    float *ref_z;
+    float4 *ref_pts[kMaxLevels];  // x y z mask
+    float4 *ref_nrm[kMaxLevels];  // nx ny nz 0
+    float *vtx;                   // kVtxPlanes planes of W*H
+    int *grad_hist;               // select_bins
+    int *seg;                     // segment tables, 6 * kSegments + 4
+    int *sel_idx;                 // P
+    float *sel_xyz;               // 3 * P (SoA)
+    float *sel_I[kMaxLevels];     // P
+    float *sel_J[kMaxLevels];     // 6 * P (SoA)
+    // current frame
+    float *cur_gray[kMaxLevels];
+    float *cur_z;
+    float4 *cur_pts[kMaxLevels];  // x y z mask
+    // photometric scratch
+    float *ph_r, *ph_zw;
+    double *ph_part;  // 27
+    int *ph_hist;     // 256
+    // ICP scratch
+    float *icp_res;          // W*H full-grid residual
+    uint8_t *icp_mask;       // W*H
+    int *icp_blkcnt;         // blocks of 1024 pixels
+    int *icp_select;         // W*H
+    float *icp_r2, *icp_w;   // W*H
+    unsigned long long *icp_var;  // 4
+    int *icp_nsel;           // kMaxLevels
+    double *icp_part;        // chunks * 27
+    unsigned long long *work; // [0] photometric point-iterations, [1] ICP point-iterations, [2] ICP mask pixels
+    unsigned int *counter;
+    float *T;                // 16, device pose (reference IR -> current IR)
+    int *stats;              // ST_COUNT
+    recon_iter_trace *trace;
+    int trace_max;
+    int *trace_count;
+};
+
+}  // namespace rt

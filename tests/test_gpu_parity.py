@@ -1,0 +1,207 @@
+"""GPU parity: librecon_track.so against the CPU oracle on the same inputs.
+
+Integer outputs (masks, histograms, selected indices, ICP correspondence counts)
+must be identical; the FP32/FP64 values are also required to be bit-identical,
+because the kernels evaluate the reference's expressions in the same order
+without FMA contraction and reduce the normal equations in the same canonical
+order as the oracle.  The tolerance the tracking contract states (residuals
+1e-5 relative, poses 1e-6 rad / 1e-6 m) is therefore met with zero error.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+import recon_gb300 as rg
+from scenes import frame_pair, n_select_for
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32) if a.dtype == np.float32 else (a.view(np.uint64) if a.dtype == np.float64 else a)
+
+
+def assert_bitexact(a, b, what):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, what
+    if not np.array_equal(bits(a), bits(b)):
+        diff = np.flatnonzero(bits(a).reshape(-1) != bits(b).reshape(-1))
+        i = diff[0]
+        raise AssertionError(f"{what}: {diff.size} of {a.size} differ; first at {i}: "
+                             f"{a.reshape(-1)[i]!r} vs {b.reshape(-1)[i]!r}")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda_lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    rg.lib()
+
+
+def run_pair(pair, mode, solver=rg.SOLVER_CHOLESKY, iters=None, n_select=None, lam=0.5, hist_bins=64):
+    W, H, L = pair.W, pair.H, pair.L
+    P = n_select or n_select_for(W, H)
+    it = iters or (1, 3, 10, 5)
+    cfg = rg.make_config(W, H, L, mode=mode, iters=it, n_select=P, solver=solver, lam=lam, hist_bins=hist_bins)
+    trk = rg.Tracker(cfg, pair.cal.calib)
+    trk.enable_trace(64)
+    trk.set_reference(pair.g0, pair.d0)
+    trk.set_current(pair.g1, pair.d1)
+    T, st = trk.track()
+    ocfg = O.make_config(W, H, L, mode=mode, iters=it, n_select=P, solver=solver, lam=lam, hist_bins=hist_bins)
+    orc = O.OracleTracker(ocfg, pair.cal.calib)
+    orc.set_reference(pair.g0, pair.d0)
+    orc.set_current(pair.g1, pair.d1)
+    To, tro = orc.track()
+    return trk, orc, T, st, To, tro
+
+
+CASES = [
+    ("320x240", dict(W=320, H=240)),
+    ("640x480_kc", dict(W=640, H=480, distortion=True)),
+    ("160x120", dict(W=160, H=120)),
+    ("80x60", dict(W=80, H=60)),
+]
+
+
+@pytest.fixture(scope="module", params=CASES, ids=[c[0] for c in CASES])
+def pair(request):
+    return frame_pair(**request.param[1])
+
+
+def test_render_matches_cpu_twin():
+    from recon_gb300 import synth
+    cal = synth.make_calibration(640, 480, distortion=True)
+    sc = synth.make_scene(3)
+    T = synth.offset_pose(1, 5.0, 40.0)
+    cam_ir = synth.camera_struct(cal, "L", T)
+    cam_rgb = synth.camera_struct(cal, "R", T)
+    g_cpu, d_cpu = O.render_pair(sc, cam_ir, cam_rgb, noise_rel=0.01, noise_seed=9, frame=4)
+    d = torch.zeros((480, 640), dtype=torch.int16, device="cuda")
+    g = torch.zeros((480, 640), dtype=torch.uint8, device="cuda")
+    rg.render_depth(sc, cam_ir, 0.01, 9, 4, d)
+    rg.render_gray(sc, cam_rgb, g)
+    torch.cuda.synchronize()
+    assert_bitexact(d.cpu().numpy().view(np.uint16), d_cpu, "depth")
+    assert_bitexact(g.cpu().numpy(), g_cpu, "gray")
+
+
+def test_reference_and_current_preparation(pair):
+    W, H, L = pair.W, pair.H, pair.L
+    P = n_select_for(W, H)
+    trk, orc, *_ = run_pair(pair, rg.BIOBJECTIVE)
+    for l in range(L):
+        n = (W >> l) * (H >> l)
+        assert_bitexact(trk.get_array(0, "ref_gray", l, np.float32, n), orc.get("ref_gray", l, n, np.float32),
+                        f"ref gray L{l}")
+        assert_bitexact(trk.get_array(0, "cur_gray", l, np.float32, n), orc.get("cur_gray", l, n, np.float32),
+                        f"cur gray L{l}")
+        rp = trk.get_array(0, "ref_pts", l, np.float32, 4 * n).reshape(n, 4)
+        rn = trk.get_array(0, "ref_nrm", l, np.float32, 4 * n).reshape(n, 4)
+        o6 = orc.get("ref6", l, 6 * n, np.float32).reshape(n, 6)
+        om = orc.get("refmask", l, n, np.int32)
+        assert_bitexact((rp[:, 3] != 0).astype(np.int32), om, f"ref mask L{l}")
+        assert_bitexact(rp[:, :3], o6[:, :3], f"ref xyz L{l}")
+        valid = om != 0
+        assert_bitexact(rn[valid, :3], o6[valid, 3:6], f"ref normals L{l}")
+        cp = trk.get_array(0, "cur_pts", l, np.float32, 4 * n).reshape(n, 4)
+        c6 = orc.get("cur6", l, 6 * n, np.float32).reshape(n, 6)
+        cm = orc.get("curmask", l, n, np.int32)
+        assert_bitexact((cp[:, 3] != 0).astype(np.int32), cm, f"cur mask L{l}")
+        assert_bitexact(cp[:, :3], c6[:, :3], f"cur xyz L{l}")
+    assert_bitexact(trk.get_array(0, "sel_idx", 0, np.int32, P), orc.get("sel_idx", 0, P, np.int32), "selection")
+    assert_bitexact(trk.get_array(0, "sel_xyz", 0, np.float32, 3 * P), orc.get("sel_xyz", 0, 3 * P, np.float32),
+                    "selected xyz")
+    for l in range(L):
+        assert_bitexact(trk.get_array(0, "sel_I", l, np.float32, P), orc.get("sel_I", l, P, np.float32),
+                        f"I_ref L{l}")
+        assert_bitexact(trk.get_array(0, "sel_J", l, np.float32, 6 * P), orc.get("sel_J", l, 6 * P, np.float32),
+                        f"J L{l}")
+
+
+def compare_traces(tr_gpu, tr_orc):
+    assert len(tr_gpu) == len(tr_orc)
+    for k, (g, o) in enumerate(zip(tr_gpu, tr_orc)):
+        where = f"iteration {k} (level {o.level}, iter {o.iter})"
+        assert (g.level, g.iter, g.solved, g.icp_selected) == (o.level, o.iter, o.solved, o.icp_selected), where
+        if o.median_bin >= 0:
+            assert g.median_bin == o.median_bin, where
+            assert_bitexact(np.array(g.hist), np.array(o.hist), "histogram " + where)
+        assert_bitexact(np.array(g.A_ph), np.array(o.A_ph), "A_photo " + where)
+        assert_bitexact(np.array(g.b_ph), np.array(o.b_ph), "b_photo " + where)
+        assert_bitexact(np.array(g.A_icp), np.array(o.A_icp), "A_icp " + where)
+        assert_bitexact(np.array(g.b_icp), np.array(o.b_icp), "b_icp " + where)
+        assert_bitexact(np.array(g.T), np.array(o.T), "pose " + where)
+
+
+@pytest.mark.parametrize("mode", [rg.PHOTOMETRIC, rg.GEOMETRIC, rg.BIOBJECTIVE], ids=["photo", "icp", "biobj"])
+def test_tracking_trace_matches_oracle(pair, mode):
+    trk, orc, T, st, To, tro = run_pair(pair, mode)
+    compare_traces(trk.trace(0), tro)
+    assert_bitexact(T, To, "final pose")
+    assert st.iterations == len(tro)
+
+
+def test_cg_solver_matches_oracle():
+    p = frame_pair(320, 240, seed=21)
+    trk, orc, T, st, To, tro = run_pair(p, rg.BIOBJECTIVE, solver=rg.SOLVER_CG, iters=(10, 10, 10))
+    compare_traces(trk.trace(0), tro)
+
+
+def test_256_bin_mad_histogram():
+    p = frame_pair(320, 240, seed=5)
+    trk, orc, T, st, To, tro = run_pair(p, rg.PHOTOMETRIC, iters=(10, 10, 10), hist_bins=256)
+    compare_traces(trk.trace(0), tro)
+
+
+def test_batch_of_mixed_instances_matches_single_runs():
+    pairs = [frame_pair(320, 240, seed=31), frame_pair(160, 120, seed=32), frame_pair(640, 480, seed=33),
+             frame_pair(80, 60, seed=34)]
+    modes = [rg.BIOBJECTIVE, rg.PHOTOMETRIC, rg.BIOBJECTIVE, rg.GEOMETRIC]
+    iters = [(4, 6, 8), (3, 5, 7), (1, 3, 10, 5), (12, 4, 9)]
+    cfgs = [rg.make_config(p.W, p.H, p.L, mode=m, iters=it, n_select=n_select_for(p.W, p.H))
+            for p, m, it in zip(pairs, modes, iters)]
+    b = rg.Batch(cfgs, [p.cal.calib for p in pairs])
+    b.set_reference([p.g0 for p in pairs], [p.d0 for p in pairs])
+    b.set_current([p.g1 for p in pairs], [p.d1 for p in pairs])
+    T, st = b.track()
+    for i, (p, m, it) in enumerate(zip(pairs, modes, iters)):
+        ocfg = O.make_config(p.W, p.H, p.L, mode=m, iters=it, n_select=n_select_for(p.W, p.H))
+        orc = O.OracleTracker(ocfg, p.cal.calib)
+        orc.set_reference(p.g0, p.d0)
+        orc.set_current(p.g1, p.d1)
+        To, _ = orc.track()
+        assert_bitexact(T[i], To, f"instance {i}")
+
+
+def test_device_inputs_and_initial_pose():
+    p = frame_pair(320, 240, seed=41)
+    cfg = rg.make_config(320, 240, 3, mode=rg.BIOBJECTIVE, iters=(2, 3, 4))
+    trk = rg.Tracker(cfg, p.cal.calib)
+    g0 = torch.from_numpy(p.g0).cuda()
+    d0 = torch.from_numpy(p.d0.view(np.int16)).cuda()
+    g1 = torch.from_numpy(p.g1).cuda()
+    d1 = torch.from_numpy(p.d1.view(np.int16)).cuda()
+    trk.set_reference(g0, d0)
+    trk.set_current(g1, d1)
+    T0 = np.eye(4, dtype=np.float32)
+    T0[:3, 3] = [3.0, -2.0, 5.0]
+    T, st = trk.track(T0)
+    ocfg = O.make_config(320, 240, 3, mode=rg.BIOBJECTIVE, iters=(2, 3, 4))
+    orc = O.OracleTracker(ocfg, p.cal.calib)
+    orc.set_reference(p.g0, p.d0)
+    orc.set_current(p.g1, p.d1)
+    To, _ = orc.track(T0)
+    assert_bitexact(T, To, "pose from an initial guess")
+
+
+def test_pose_accuracy_against_ground_truth():
+    from recon_gb300 import synth
+    p = frame_pair(640, 480, seed=51, noise=0.0)
+    trk, orc, T, st, To, tro = run_pair(p, rg.BIOBJECTIVE)
+    dt, dr = synth.pose_error(p.T_gt, T.astype(np.float64))
+    assert dt < 1.0 and dr < 0.05, (dt, dr)
