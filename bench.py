@@ -1,0 +1,412 @@
+#!/usr/bin/env python
+"""Benchmark: tracked frames/s of bi-objective (photometric + point-to-plane ICP,
+lambda = 0.5) tracking at 640x480 with a 4-level pyramid over a 300-frame
+seeded smooth trajectory, a keyframe every 10 frames.
+
+One step tracks the whole trajectory: the 30 keyframe segments (keyframe 10j,
+frames 10j+1 .. 10j+10 tracked against it, each frame starting from the
+previous frame's pose as the reference tracker does between reference updates)
+run as one batch of 30 tracker instances, so every launch serves all segments.
+
+  value  inputs already in HBM (frames pre-rendered on the GPU), poses read back
+  e2e    the same through the C ABI from pinned host buffers: every step copies
+         the frames host->device and the poses device->host inside the timed region
+
+`--impl reference` times the reference algorithm's CPU implementation instead
+(the oracle port, all host threads) on a bounded sample of the same workload.
+Under torchrun each rank tracks its own trajectory (weak scaling, no collective
+on the data path); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, LEVELS = 640, 480, 4
+N_FRAMES = 300
+KEYFRAME_EVERY = 10
+ITERS = (1, 3, 10, 5)
+LAMBDA = 0.5
+N_SELECT = 8192
+# algorithmic bytes per point and GN iteration (photometric: xyz 12 + I_ref 4 +
+# J 24 + 4 bilinear taps 16 + depth tap 4 + r/zweight written and re-read 16;
+# ICP: point+normal 24 + 4 taps x 12 + mask 4 + weight 4 + index 4)
+B_PHOTO = 76
+B_ICP = 84
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--frames", type=int, default=N_FRAMES)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- workload
+def make_workload(seed: int, n_frames: int):
+    from recon_gb300 import synth
+    cal = synth.make_calibration(W, H)
+    scene = synth.make_scene(seed)
+    poses = synth.smooth_trajectory(n_frames + 1, seed + 2)
+    return cal, scene, poses
+
+
+def render_frames_gpu(cal, scene, poses, seed, torch):
+    import recon_gb300 as rg
+    from recon_gb300 import synth
+    n = len(poses)
+    gray = torch.empty((n, H, W), dtype=torch.uint8, device="cuda")
+    depth = torch.empty((n, H, W), dtype=torch.int16, device="cuda")
+    for f in range(n):
+        rg.render_depth(scene, synth.camera_struct(cal, "L", poses[f]), 0.01, seed + 1, f, depth[f])
+        rg.render_gray(scene, synth.camera_struct(cal, "R", poses[f]), gray[f])
+    torch.cuda.synchronize()
+    return gray, depth
+
+
+def segments(n_frames):
+    """(keyframe index, [tracked frame indices]) per keyframe segment."""
+    segs = []
+    for k in range(0, n_frames, KEYFRAME_EVERY):
+        segs.append((k, list(range(k + 1, min(k + KEYFRAME_EVERY, n_frames) + 1))))
+    return segs
+
+
+def make_batch(cal, n_inst, stream):
+    import recon_gb300 as rg
+    cfg = rg.make_config(W, H, LEVELS, mode=rg.BIOBJECTIVE, iters=ITERS, n_select=N_SELECT, lam=LAMBDA)
+    return rg.Batch([cfg] * n_inst, [cal.calib] * n_inst, stream=stream)
+
+
+def run_step(batch, segs, gray_src, depth_src, poses_out):
+    """Tracks every segment of the trajectory once (inputs: device tensors or pinned host arrays)."""
+    n = len(segs)
+    batch.set_reference([gray_src[k] for k, _ in segs], [depth_src[k] for k, _ in segs])
+    steps = max(len(fr) for _, fr in segs)
+    for s in range(steps):
+        idx = [fr[min(s, len(fr) - 1)] for _, fr in segs]
+        batch.set_current([gray_src[i] for i in idx], [depth_src[i] for i in idx])
+        batch.track_async(None)
+        T, st = batch.poses()
+        for j, (_, fr) in enumerate(segs):
+            if s < len(fr):
+                poses_out[fr[s]] = T[j]
+    return poses_out
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_track(cal, gray_np, depth_np, frames_per_seg, segs_sel, threads):
+    """Oracle (CPU port of the reference algorithm) on a sample of segments."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    O.lib().orc_set_threads(threads)
+    cfg = O.make_config(W, H, LEVELS, mode=O.BIOBJECTIVE, iters=ITERS, n_select=N_SELECT, lam=LAMBDA)
+    out = {}
+    n = 0
+    t0 = time.perf_counter()
+    for k, fr in segs_sel:
+        orc = O.OracleTracker(cfg, cal.calib)
+        orc.set_reference(gray_np[k], depth_np[k])
+        T = None
+        for f in fr[:frames_per_seg]:
+            orc.set_current(gray_np[f], depth_np[f])
+            T, _ = orc.track(T)
+            out[f] = T.copy()
+            n += 1
+        orc.close()
+    dt = time.perf_counter() - t0
+    return n / dt, out, n, dt
+
+
+def host_frames(cal, scene, poses, seed, frames):
+    """Renders the given frames on the CPU twin (identical to the GPU renderer)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    from recon_gb300 import synth
+    g, d = {}, {}
+    for f in frames:
+        g[f], d[f] = O.render_pair(scene, synth.camera_struct(cal, "L", poses[f]),
+                                   synth.camera_struct(cal, "R", poses[f]), noise_rel=0.01,
+                                   noise_seed=seed + 1, frame=f)
+    return g, d
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    seed = 1000
+    cal, scene, poses = make_workload(seed, args.frames)
+    segs = segments(args.frames)
+    threads = os.cpu_count() or 1
+    sample_segs = segs[:1]
+    frames_per = 10
+    need = sorted({k for k, _ in sample_segs} | {f for _, fr in sample_segs for f in fr[:frames_per]})
+    g, d = host_frames(cal, scene, poses, seed, need)
+    times = []
+    for i in range(args.warmup + args.steps):
+        fps, _, n, dt = cpu_track(cal, g, d, frames_per, sample_segs, threads)
+        if i >= args.warmup:
+            times.append(dt / n)
+    fps = 1.0 / float(np.mean(times))
+    line = {
+        "impl": "reference", "metric": "tracked frames/s (bi-objective 640x480, 300-frame trajectory)",
+        "value": fps, "unit": "frames/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * float(np.mean(times)) * frames_per, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": "bi-objective lambda=0.5, 640x480, 4 levels, iterations 1/3/10/5, keyframe every 10",
+                   "sample_per_step": f"{frames_per} frames of one keyframe segment"},
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"{frames_per} frames of one keyframe segment per step, all {threads} threads"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- main
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        return reference_arm(args, rank, world)
+    import torch
+    import recon_gb300 as rg
+    from recon_gb300 import synth
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    seed = 1000 + 17 * rank
+    cal, scene, poses = make_workload(seed, args.frames)
+    segs = segments(args.frames)
+    gray, depth = render_frames_gpu(cal, scene, poses, seed, torch)
+    stream = torch.cuda.Stream()
+    batch = make_batch(cal, len(segs), stream.cuda_stream)
+    poses_out = np.zeros((args.frames + 1, 4, 4), np.float32)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # -------- device-resident timed region
+    for _ in range(args.warmup):
+        run_step(batch, segs, gray, depth, poses_out)
+    batch.enable_timing(True)
+    batch.work(reset=True)
+    launches0 = rg.launch_count()
+    barrier()
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            run_step(batch, segs, gray, depth, poses_out)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    launches = rg.launch_count() - launches0
+    timing = batch.timing(reset=True)
+    work = batch.work(reset=True).astype(np.float64)
+    batch.enable_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    frames_per_step = args.frames
+    value = world * frames_per_step * args.steps / (ms / 1000.0)
+
+    # -------- roofline of the dominant kernel (the GN iteration kernel)
+    it_ms, it_launches = timing["gn_iteration"]
+    bytes_iter = float(work[:, 0].sum() * B_PHOTO + work[:, 1].sum() * B_ICP)
+    per_launch_bytes = bytes_iter / max(it_launches, 1)
+    per_launch_s = it_ms / 1000.0 / max(it_launches, 1)
+    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    peak, peak_kind = load_peaks()
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_iter_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_launch_scaled")
+        except Exception:
+            traffic = None
+
+    # -------- pose error against ground truth (all tracked frames)
+    errs = []
+    for k, fr in segs:
+        for f in fr:
+            gt = synth.relative_pose(poses[k], poses[f])
+            errs.append(synth.pose_error(gt, poses_out[f].astype(np.float64)))
+    errs = np.array(errs)
+
+    # -------- e2e through the C ABI from pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        g_host = torch.empty(gray.shape, dtype=torch.uint8, pin_memory=True)
+        d_host = torch.empty(depth.shape, dtype=torch.int16, pin_memory=True)
+        g_host.copy_(gray)
+        d_host.copy_(depth)
+        g_np = g_host.numpy()
+        d_np = d_host.numpy().view(np.uint16)
+        for _ in range(max(1, args.warmup)):
+            run_step(batch, segs, g_np, d_np, poses_out)
+        barrier()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            run_step(batch, segs, g_np, d_np, poses_out)
+        e1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+        ms_e2e = max(e0.elapsed_time(e1), 1000.0 * wall)
+        if world > 1:
+            t = torch.tensor([ms_e2e], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_e2e = float(t.item())
+        n_ref = len(segs)
+        n_cur = sum(1 for _ in range(max(len(fr) for _, fr in segs))) * len(segs)
+        h2d = (n_ref + n_cur) * W * H * 3
+        d2h = max(len(fr) for _, fr in segs) * len(segs) * (64 + 64)
+        e2e = {"value": world * frames_per_step * args.steps / (ms_e2e / 1000.0), "unit": "frames/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    # -------- CPU baseline: the oracle on a bounded sample, and its pose agreement
+    cpu = None
+    oracle_err = None
+    if rank == 0 and not args.no_cpu:
+        sample_segs = segs[:1]
+        frames_per = 10
+        need = sorted({k for k, _ in sample_segs} | {f for _, fr in sample_segs for f in fr[:frames_per]})
+        gh = {f: gray[f].cpu().numpy() for f in need}
+        dh = {f: depth[f].cpu().numpy().view(np.uint16) for f in need}
+        threads = os.cpu_count() or 1
+        fps_cpu, oposes, n, dt = cpu_track(cal, gh, dh, frames_per, sample_segs, threads)
+        cpu = {"value": fps_cpu, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": f"{n} frames ({frames_per} of keyframe segment 0), oracle with {threads} OpenMP threads, "
+                         f"{dt:.1f} s"}
+        d_t, d_r = [], []
+        for f, To in oposes.items():
+            et, er = synth.pose_error(To.astype(np.float64), poses_out[f].astype(np.float64))
+            d_t.append(et)
+            d_r.append(er)
+        oracle_err = {"frames": len(d_t), "max_mm": float(max(d_t)), "max_deg": float(max(d_r)),
+                      "bit_identical": bool(all(np.array_equal(oposes[f].view(np.uint32),
+                                                               poses_out[f].view(np.uint32)) for f in oposes))}
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": "tracked frames/s (bi-objective 640x480, 300-frame trajectory)",
+            "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32", "data": "synthetic (seeded procedural scene ray-cast on the GPU)",
+            "config": {"workload": "bi-objective lambda=0.5, 640x480, 4 levels, iterations 1/3/10/5, 8192 "
+                                   "photometric points, 300-frame smooth trajectory, keyframe every 10 frames, "
+                                   "30 keyframe segments batched",
+                       "l2": "inputs larger than L2 (301 frames, 277 MB; ~1.2 GB working set)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "kernel": "k_iter",
+                         "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": per_launch_bytes,
+                         "avg_launch_ms": per_launch_s * 1000.0},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "pose_error_vs_ground_truth": {"median_mm": float(np.median(errs[:, 0])),
+                                           "max_mm": float(errs[:, 0].max()),
+                                           "median_deg": float(np.median(errs[:, 1])),
+                                           "max_deg": float(errs[:, 1].max())},
+            "pose_error_vs_oracle": oracle_err,
+            "kernel_ms": {k: v[0] for k, v in timing.items()},
+            "kernel_launches": {k: v[1] for k, v in timing.items()},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -62,6 +62,11 @@ int cuda_fail(cudaError_t e, const char *where) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// The runtime's last-error slot is per host thread and shared with every other
+// CUDA user in the process; an error left there by unrelated code must not be
+// reported as a failure of this library's launches.
+void clear_stale_error() { (void)cudaGetLastError(); }
+
 struct Arena {
     size_t off = 0;
     char *base = nullptr;
@@ -488,6 +493,7 @@ int recon_calib_setup(const double KL[9], const double KR[9], const double TLR[1
 }
 
 int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs, void *stream, recon_batch **out) {
+    clear_stale_error();
     if (!out || !cfgs || !calibs || n <= 0) return fail(RECON_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
     int ndev = 0;
@@ -588,6 +594,7 @@ int recon_batch_size(const recon_batch *b) { return b ? b->n : 0; }
 
 int recon_batch_set_reference(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
                               int32_t on_device) {
+    clear_stale_error();
     if (!b || !gray || !depth) return fail(RECON_ERR_INVALID_ARG, "null argument");
     int rc = stage_inputs(b, gray, depth, nullptr, on_device);
     if (rc) return rc;
@@ -599,6 +606,7 @@ int recon_batch_set_reference(recon_batch *b, const uint8_t *const *gray, const 
 }
 
 int recon_batch_set_reference_rgbd_float4(recon_batch *b, int32_t inst, const float *rgbd, int32_t on_device) {
+    clear_stale_error();
     if (!b || !rgbd || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
     std::vector<const float *> p(b->n, nullptr);
     p[inst] = rgbd;
@@ -613,6 +621,7 @@ int recon_batch_set_reference_rgbd_float4(recon_batch *b, int32_t inst, const fl
 
 int recon_batch_set_current(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
                             int32_t on_device) {
+    clear_stale_error();
     if (!b || !gray || !depth) return fail(RECON_ERR_INVALID_ARG, "null argument");
     int rc = stage_inputs(b, gray, depth, nullptr, on_device);
     if (rc) return rc;
@@ -623,6 +632,7 @@ int recon_batch_set_current(recon_batch *b, const uint8_t *const *gray, const ui
 }
 
 int recon_batch_set_current_rgbd_float4(recon_batch *b, int32_t inst, const float *rgbd, int32_t on_device) {
+    clear_stale_error();
     if (!b || !rgbd || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
     std::vector<const float *> p(b->n, nullptr);
     p[inst] = rgbd;
@@ -635,6 +645,7 @@ int recon_batch_set_current_rgbd_float4(recon_batch *b, int32_t inst, const floa
 }
 
 int recon_batch_track_async(recon_batch *b, const float *T_init_host) {
+    clear_stale_error();
     if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
     if (!b->have_ref || !b->have_cur) return fail(RECON_ERR_STATE, "reference or current frame missing");
     if (T_init_host)
@@ -647,6 +658,7 @@ int recon_batch_track_async(recon_batch *b, const float *T_init_host) {
 }
 
 int recon_batch_get_poses(recon_batch *b, float *T_out, recon_track_stats *stats) {
+    clear_stale_error();
     if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
     std::vector<int> st((size_t)b->n * ST_COUNT);
     for (int i = 0; i < b->n; i++) {
@@ -685,6 +697,7 @@ int recon_batch_track(recon_batch *b, float *T_io, recon_track_stats *stats) {
 }
 
 int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters[RECON_MAX_LEVELS]) {
+    clear_stale_error();
     if (!b || !iters || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
     recon_config c = b->cfg[inst];
     for (int l = 0; l < RECON_MAX_LEVELS; l++) c.iters[l] = iters[l];
@@ -697,6 +710,7 @@ int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters
 }
 
 int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambda) {
+    clear_stale_error();
     if (!b || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
     recon_config c = b->cfg[inst];
     c.mode = mode;
@@ -711,6 +725,7 @@ int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambd
 }
 
 int recon_batch_enable_trace(recon_batch *b, int32_t max_iters) {
+    clear_stale_error();
     if (!b || max_iters < 0) return fail(RECON_ERR_INVALID_ARG, "bad argument");
     if (b->d_trace) cudaFree(b->d_trace);
     if (b->d_trace_count) cudaFree(b->d_trace_count);
@@ -732,6 +747,7 @@ int recon_batch_enable_trace(recon_batch *b, int32_t max_iters) {
 }
 
 int recon_batch_get_trace(recon_batch *b, int32_t inst, recon_iter_trace *out, int32_t max) {
+    clear_stale_error();
     if (!b || inst < 0 || inst >= b->n || !out) return fail(RECON_ERR_INVALID_ARG, "bad argument");
     if (!b->d_trace) return 0;
     int cnt = 0;
@@ -746,6 +762,7 @@ int recon_batch_get_trace(recon_batch *b, int32_t inst, recon_iter_trace *out, i
 
 int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, int32_t level, void *host_dst,
                               int64_t nbytes) {
+    clear_stale_error();
     if (!b || inst < 0 || inst >= b->n || !name || !host_dst) return fail(RECON_ERR_INVALID_ARG, "bad argument");
     const InstDesc &d = b->desc[inst];
     if (level < 0 || level >= d.L) return fail(RECON_ERR_INVALID_ARG, "bad level");
@@ -781,6 +798,7 @@ int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, in
 }
 
 int recon_batch_enable_timing(recon_batch *b, int32_t on) {
+    clear_stale_error();
     if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
     CK(cudaStreamSynchronize(b->stream));
     if ((bool)on != b->timing) b->graph_dirty = true;
@@ -790,6 +808,7 @@ int recon_batch_enable_timing(recon_batch *b, int32_t on) {
 }
 
 int recon_batch_get_timing(recon_batch *b, double *ms, int64_t *launches, int32_t reset) {
+    clear_stale_error();
     if (!b || !ms || !launches) return fail(RECON_ERR_INVALID_ARG, "null argument");
     CK(cudaStreamSynchronize(b->stream));
     collect_events(b, b->direct_events, true);
@@ -802,6 +821,7 @@ int recon_batch_get_timing(recon_batch *b, double *ms, int64_t *launches, int32_
 }
 
 int recon_batch_get_work(recon_batch *b, uint64_t *out, int32_t reset) {
+    clear_stale_error();
     if (!b || !out) return fail(RECON_ERR_INVALID_ARG, "null argument");
     CK(cudaStreamSynchronize(b->stream));
     for (int i = 0; i < b->n; i++) {
@@ -887,6 +907,7 @@ int recon_get_global_pose(recon_tracker *t, double T[16]) {
     return RECON_OK;
 }
 int recon_reset(recon_tracker *t) {
+    clear_stale_error();
     if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
     identity16d(t->global_pose);
     identity16(t->T_prev);
@@ -902,6 +923,7 @@ int recon_reset(recon_tracker *t) {
 // ---- renderer ----
 int recon_render_depth(const void *scene, const void *camera, float noise_rel, uint32_t noise_seed, uint32_t frame,
                        uint16_t *depth_dev, void *stream) {
+    clear_stale_error();
     if (!scene || !camera || !depth_dev) return fail(RECON_ERR_INVALID_ARG, "null argument");
     recon_scene sc;
     recon_camera cam;
@@ -915,6 +937,7 @@ int recon_render_depth(const void *scene, const void *camera, float noise_rel, u
 }
 
 int recon_render_gray(const void *scene, const void *camera, uint8_t *gray_dev, void *stream) {
+    clear_stale_error();
     if (!scene || !camera || !gray_dev) return fail(RECON_ERR_INVALID_ARG, "null argument");
     recon_scene sc;
     recon_camera cam;
