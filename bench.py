@@ -63,6 +63,27 @@ def dist_info():
     return rank, world, local
 
 
+def rank_seed(rank: int) -> int:
+    """Scene/trajectory seed of a rank: every rank tracks its own trajectory (weak scaling)."""
+    return 1000 + 17 * rank
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    """Slowest rank's time (the job finishes when the last rank does)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, frames_per_rank_step: int, steps: int, max_ms: float) -> float:
+    """Frames/s of the whole job: all ranks' frames over the slowest rank's time."""
+    return world * frames_per_rank_step * steps / (max_ms / 1000.0)
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -159,18 +180,20 @@ def make_batch(cal, n_inst, stream):
 
 
 def run_step(batch, segs, gray_src, depth_src, poses_out):
-    """Tracks every segment of the trajectory once (inputs: device tensors or pinned host arrays)."""
-    n = len(segs)
+    """Tracks every segment of the trajectory once (inputs: device tensors or pinned host arrays).
+
+    The keyframes of all segments are set in one call; the segments' frames are
+    then tracked as one sequence (recon_batch_track_sequence): frame s of every
+    segment per launch, each starting from the previous frame's pose."""
     batch.set_reference([gray_src[k] for k, _ in segs], [depth_src[k] for k, _ in segs])
     steps = max(len(fr) for _, fr in segs)
+    idx = [[fr[min(s, len(fr) - 1)] for _, fr in segs] for s in range(steps)]
+    T, st = batch.track_sequence([[gray_src[i] for i in row] for row in idx],
+                                 [[depth_src[i] for i in row] for row in idx])
     for s in range(steps):
-        idx = [fr[min(s, len(fr) - 1)] for _, fr in segs]
-        batch.set_current([gray_src[i] for i in idx], [depth_src[i] for i in idx])
-        batch.track_async(None)
-        T, st = batch.poses()
         for j, (_, fr) in enumerate(segs):
             if s < len(fr):
-                poses_out[fr[s]] = T[j]
+                poses_out[fr[s]] = T[s, j]
     return poses_out
 
 
@@ -256,7 +279,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    seed = 1000 + 17 * rank
+    seed = rank_seed(rank)
     cal, scene, poses = make_workload(seed, args.frames)
     segs = segments(args.frames)
     gray, depth = render_frames_gpu(cal, scene, poses, seed, torch)
@@ -289,12 +312,9 @@ def main():
     timing = batch.timing(reset=True)
     work = batch.work(reset=True).astype(np.float64)
     batch.enable_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, "cuda")
     frames_per_step = args.frames
-    value = world * frames_per_step * args.steps / (ms / 1000.0)
+    value = job_throughput(world, frames_per_step, args.steps, ms)
 
     # -------- roofline of the dominant kernel (the GN iteration kernel)
     it_ms, it_launches = timing["gn_iteration"]
@@ -339,15 +359,12 @@ def main():
         barrier()
         wall = time.perf_counter() - t0
         ms_e2e = max(e0.elapsed_time(e1), 1000.0 * wall)
-        if world > 1:
-            t = torch.tensor([ms_e2e], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_e2e = float(t.item())
+        ms_e2e = max_over_ranks(ms_e2e, world, "cuda")
         n_ref = len(segs)
         n_cur = sum(1 for _ in range(max(len(fr) for _, fr in segs))) * len(segs)
         h2d = (n_ref + n_cur) * W * H * 3
         d2h = max(len(fr) for _, fr in segs) * len(segs) * (64 + 64)
-        e2e = {"value": world * frames_per_step * args.steps / (ms_e2e / 1000.0), "unit": "frames/s",
+        e2e = {"value": job_throughput(world, frames_per_step, args.steps, ms_e2e), "unit": "frames/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     # -------- CPU baseline: the oracle on a bounded sample, and its pose agreement

@@ -126,6 +126,30 @@ int recon_batch_track(recon_batch *b, float *T_io, recon_track_stats *stats);
 int recon_batch_track_async(recon_batch *b, const float *T_init_host);
 int recon_batch_get_poses(recon_batch *b, float *T_out, recon_track_stats *stats);
 
+/* Tracks nf consecutive current frames for every instance against its present
+ * reference, each frame starting from the previous frame's pose (the
+ * reference tracker's behaviour between reference updates,
+ * phototracker.cpp:691-728).  gray/depth: nf x n pointers, row f = frame f of
+ * every instance.  Host inputs are copied on a second stream into two staging
+ * slots, overlapping frame f+1's upload with frame f's tracking (pinned host
+ * memory makes the copies asynchronous).  T_out: nf x n x 16 floats (host) or
+ * NULL; stats: statistics of the last frame.  Synchronises once at the end. */
+int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const *gray, const uint16_t *const *depth,
+                               int32_t on_device, float *T_out, recon_track_stats *stats);
+
+/* Keyframe depth fusion: fuses nframes (1..8) tracked frames' depth maps into
+ * every instance's keyframe depth (T_host: nframes x n x 16, keyframe -> frame
+ * poses as returned by tracking; depth: nframes x n uint16 mm maps), gating on
+ * |dz| < gate_mm, then rebuilds the photometric selection/Jacobians and the ICP
+ * reference pyramid from the fused depth with the keyframe's gray image.  The
+ * current pose is kept.  Runs on the batch's second (reconstruction) stream;
+ * later tracking on the pose stream waits for it.  Reference analogues:
+ * filterDepthIIRKernel (warp.cu:398-467, disabled), updateVoxelsKernel's
+ * running mean (VoxelGrid_cuda.cu:1005-1013), KeyFrameModel::integrateDepthMaps
+ * (KeyFrameModel.cpp:537-583, not compiled). */
+int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *const *depth, const float *T_host,
+                              int32_t on_device, float gate_mm);
+
 int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters[RECON_MAX_LEVELS]);
 int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambda);
 

@@ -1297,9 +1297,9 @@ void orc_destroy(orc_tracker *t) {
 
 /* PhotoTracker::prepareReference + selectPixels (phototracker.cpp:338-386) and
  * ShapeTracker::setReferencePoints + prepareReference (shapetracker.cpp:205-288) */
-int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0) {
+static int prepare_reference(orc_tracker *t, const float *gray0, const float *z0, int reset_pose) {
     int W = t->W, H = t->H, L = t->L, P = t->P;
-    memcpy(t->ref_gray[0], gray0, W * H * sizeof(float));
+    if (gray0) memcpy(t->ref_gray[0], gray0, W * H * sizeof(float));
     memcpy(t->ref_z, z0, W * H * sizeof(float));
     for (int l = 1; l < L; l++) orc_downsample2(t->ref_gray[l - 1], W >> l, H >> l, t->ref_gray[l]);
     /* photometric */
@@ -1329,9 +1329,35 @@ int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0)
     orc_compute_normals6(t->ref6[0], t->refmask[0], W, H);
     for (int l = 1; l < L; l++)
         orc_downsample_cloud6(t->ref6[l - 1], t->refmask[l - 1], W >> l, H >> l, t->ref6[l], t->refmask[l]);
-    for (int i = 0; i < 16; i++) t->T[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    if (reset_pose)
+        for (int i = 0; i < 16; i++) t->T[i] = (i % 5 == 0) ? 1.0f : 0.0f;
     t->has_ref = 1;
     return 0;
+}
+
+int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0) {
+    return prepare_reference(t, gray0, z0, 1);
+}
+
+/* Keyframe fusion of nframes depth maps (uint16 mm) with their tracked poses
+ * (keyframe -> frame), then the reference is rebuilt from the fused depth
+ * with the keyframe's gray image; the current pose is kept. */
+int orc_fuse_keyframe(orc_tracker *t, int nframes, const uint16_t *const *depth, const float *Tframes, float gate) {
+    if (!t->has_ref || nframes < 0 || nframes > 8) return -1;
+    int n = t->W * t->H;
+    float *zf[8];
+    for (int f = 0; f < nframes; f++) {
+        zf[f] = (float *)xmalloc(n * sizeof(float));
+        orc_convert_depth(depth[f], n, zf[f]);
+    }
+    float *zout = (float *)xmalloc(n * sizeof(float));
+    float *wout = (float *)xmalloc(n * sizeof(float));
+    orc_fuse_depth(t->ref_z, t->W, t->H, t->calib, nframes, (const float *const *)zf, Tframes, gate, zout, wout);
+    int rc = prepare_reference(t, NULL, zout, 0);
+    for (int f = 0; f < nframes; f++) free(zf[f]);
+    free(zout);
+    free(wout);
+    return rc;
 }
 
 int orc_set_reference(orc_tracker *t, const uint8_t *gray, const uint16_t *depth) {

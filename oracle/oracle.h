@@ -129,6 +129,7 @@ void orc_destroy(orc_tracker *t);
 int orc_set_reference(orc_tracker *t, const uint8_t *gray, const uint16_t *depth);
 int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0);
 int orc_set_current(orc_tracker *t, const uint8_t *gray, const uint16_t *depth);
+int orc_fuse_keyframe(orc_tracker *t, int nframes, const uint16_t *const *depth, const float *Tframes, float gate);
 int orc_track(orc_tracker *t, float *T, orc_iter_trace *trace, int max_trace);
 int orc_get_array(orc_tracker *t, const char *name, int level, void *dst, int64_t nbytes);
 int orc_n_icp_selected(orc_tracker *t, int level);

@@ -128,6 +128,8 @@ def lib() -> ctypes.CDLL:
             L.recon_get_relative_pose.argtypes = [vp, vp]
             L.recon_get_global_pose.argtypes = [vp, vp]
             L.recon_reset.argtypes = [vp]
+            L.recon_batch_track_sequence.argtypes = [vp, i32, vp, vp, i32, vp, vp]
+            L.recon_batch_fuse_keyframe.argtypes = [vp, i32, vp, vp, i32, f32]
             L.recon_batch_enable_timing.argtypes = [vp, i32]
             L.recon_batch_get_timing.argtypes = [vp, vp, vp, i32]
             L.recon_batch_get_work.argtypes = [vp, vp, i32]
@@ -247,6 +249,54 @@ class Batch:
         else:
             check(lib().recon_batch_track(self.h, _ptr(T), ctypes.cast(stats, ctypes.c_void_p)))
         return T.reshape(self.n, 4, 4), list(stats)
+
+    def track_sequence(self, grays, depths):
+        """grays/depths: nf lists of n images (host arrays or CUDA tensors).
+        Returns poses [nf, n, 4, 4] and the last frame's stats."""
+        nf = len(grays)
+        g = (ctypes.c_void_p * (nf * self.n))()
+        d = (ctypes.c_void_p * (nf * self.n))()
+        dev = None
+        keep = []
+        for f in range(nf):
+            for i in range(self.n):
+                gi, di = grays[f][i], depths[f][i]
+                if isinstance(gi, np.ndarray):
+                    gi = np.ascontiguousarray(gi, np.uint8)
+                    di = np.ascontiguousarray(di, np.uint16)
+                keep += [gi, di]
+                od = _on_device(gi)
+                if dev is None:
+                    dev = od
+                elif dev != od:
+                    raise ValueError("mix of host and device inputs")
+                g[f * self.n + i] = _ptr(gi).value
+                d[f * self.n + i] = _ptr(di).value
+        T = np.zeros((nf, self.n, 16), np.float32)
+        stats = (TrackStats * self.n)()
+        check(lib().recon_batch_track_sequence(self.h, nf, ctypes.cast(g, ctypes.c_void_p),
+                                               ctypes.cast(d, ctypes.c_void_p), int(dev or 0), _ptr(T),
+                                               ctypes.cast(stats, ctypes.c_void_p)))
+        return T.reshape(nf, self.n, 4, 4), list(stats)
+
+    def fuse_keyframe(self, depths, T, gate_mm: float = 30.0):
+        """depths: nframes lists of n depth maps; T: [nframes, n, 4, 4] keyframe -> frame poses."""
+        nf = len(depths)
+        d = (ctypes.c_void_p * (nf * self.n))()
+        dev = None
+        keep = []
+        for f in range(nf):
+            for i in range(self.n):
+                di = depths[f][i]
+                if isinstance(di, np.ndarray):
+                    di = np.ascontiguousarray(di, np.uint16)
+                keep.append(di)
+                od = _on_device(di)
+                dev = od if dev is None else dev
+                d[f * self.n + i] = _ptr(di).value
+        Tn = np.ascontiguousarray(np.asarray(T, np.float32).reshape(nf * self.n, 16))
+        check(lib().recon_batch_fuse_keyframe(self.h, nf, ctypes.cast(d, ctypes.c_void_p), _ptr(Tn), int(dev or 0),
+                                              gate_mm))
 
     def track_async(self, T_init=None):
         T = None if T_init is None else np.ascontiguousarray(np.asarray(T_init, np.float32).reshape(self.n, 16))

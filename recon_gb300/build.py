@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librecon_track.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-UNITS = ["kernels.cu", "host.cu"]
+UNITS = ["kernels.cu", "host.cu", "refshim.cu"]
 HEADERS = ["scene.h", "solve.cuh", "track_kernels.cuh", "track_math.cuh"]
 
 
@@ -33,6 +33,7 @@ def nvcc() -> str:
 def _sources():
     srcs = [os.path.join(CSRC, u) for u in UNITS] + [os.path.join(CSRC, h) for h in HEADERS]
     srcs.append(os.path.join(ROOT, "include", "recon_track.h"))
+    srcs.append(os.path.join(ROOT, "include", "recon_ref_shim.h"))
     srcs.append(os.path.abspath(__file__))
     return srcs
 

@@ -28,13 +28,17 @@ __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
 __global__ void k_icp_compact(const InstDesc *D, int level);
 __global__ void k_icp_student(const InstDesc *D, int level, int pass);
-__global__ void k_iter(const InstDesc *D, int level, int it);
+__global__ void k_iter(const InstDesc *D, int level, int it, int nph_grid);
 __global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
                                uint16_t *out);
 __global__ void k_render_gray(recon_scene sc, recon_camera cam, uint8_t *out);
 __global__ void k_reset_pose(const InstDesc *D, const int *active);
 __global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_init);
 __global__ void k_clear_ref(const InstDesc *D, const int *active);
+__global__ void k_store_pose(const InstDesc *D, float *dst);
+__global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const uint16_t *const *depth,
+                             const float *Tf, float gate, const int *active);
+__global__ void k_ref_from_z(const InstDesc *D, const int *active);
 }  // namespace rt
 
 using namespace rt;
@@ -66,6 +70,7 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // CUDA user in the process; an error left there by unrelated code must not be
 // reported as a failure of this library's launches.
 void clear_stale_error() { (void)cudaGetLastError(); }
+
 
 struct Arena {
     size_t off = 0;
@@ -108,6 +113,25 @@ struct recon_batch {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> graph_events, direct_events;
     double t_ms[8] = {0};
     long long t_cnt[8] = {0};
+    // sequence tracking: pointer tables, pose history, host-input double buffer
+    const void **d_seqptr = nullptr;
+    size_t seqptr_cap = 0;
+    const void **h_seqptr = nullptr;  // pinned
+    float *d_Tseq = nullptr;
+    size_t Tseq_cap = 0;
+    int *d_ones = nullptr;
+    uint8_t *d_slot[2] = {nullptr, nullptr};
+    size_t slot_bytes = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+    // keyframe fusion runs on a second stream (the reference's reconstruction GPU)
+    cudaStream_t recon_stream = nullptr;
+    cudaEvent_t ev_pose = nullptr, ev_fused = nullptr;
+    uint16_t *d_fuse = nullptr;
+    size_t fuse_bytes = 0;
+    const void **d_fuse_ptr = nullptr;
+    float *d_fuse_T = nullptr;
+    size_t fuse_cap = 0;
     // host pose bookkeeping for the single-tracker API (applyIncrement)
     double global_pose[16];
     float T_prev[16];
@@ -165,7 +189,8 @@ size_t layout(InstDesc &d, char *base) {
     d.ph_r = a.take<float>(P);
     d.ph_zw = a.take<float>(P);
     d.ph_part = a.take<double>(27);
-    d.ph_hist = a.take<int>(256);
+    d.ph_hist = a.take<int>(1024);
+    d.ph_counter = a.take<unsigned int>(4);
     d.icp_res = a.take<float>(n);
     d.icp_mask = a.take<uint8_t>(n);
     int nblk = (n + kChunk - 1) / kChunk;
@@ -173,6 +198,8 @@ size_t layout(InstDesc &d, char *base) {
     d.icp_select = a.take<int>(n);
     d.icp_r2 = a.take<float>(n);
     d.icp_w = a.take<float>(n);
+    d.icp_pk_pts = a.take<float4>(n);
+    d.icp_pk_nrm = a.take<float4>(n);
     d.icp_var = a.take<unsigned long long>(4);
     d.icp_nsel = a.take<int>(kMaxLevels);
     d.icp_part = a.take<double>((size_t)nblk * 27);
@@ -257,16 +284,19 @@ struct TimedScope {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> *list;
     cudaEvent_t e1 = nullptr, e2 = nullptr;
     int kind;
+    unsigned int flags;
     TimedScope(recon_batch *b_, cudaStream_t s_, int kind_, bool in_graph) : b(b_), s(s_), kind(kind_) {
         list = in_graph ? &b->graph_events : &b->direct_events;
+        // inside a capture an event record must be external to become a graph node
+        flags = in_graph ? cudaEventRecordExternal : cudaEventRecordDefault;
         if (!b->timing) return;
         cudaEventCreate(&e1);
         cudaEventCreate(&e2);
-        cudaEventRecord(e1, s);
+        cudaEventRecordWithFlags(e1, s, flags);
     }
     ~TimedScope() {
         if (!b->timing) return;
-        cudaEventRecord(e2, s);
+        cudaEventRecordWithFlags(e2, s, flags);
         list->push_back({kind, {e1, e2}});
     }
 };
@@ -287,44 +317,52 @@ void collect_events(recon_batch *b, std::vector<std::pair<int, std::pair<cudaEve
     if (destroy) list.clear();
 }
 
-int prepare_reference(recon_batch *b) {
-    TimedScope ts(b, b->stream, TK_PREP_REF, false);
+// reference preparation; from_inputs: convert the staged images (else rebuild
+// from the current ref_z, keeping the keyframe gray); reset_pose: T <- I
+int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose = true,
+                      cudaStream_t st = nullptr) {
+    cudaStream_t s = st ? st : b->stream;
+    TimedScope ts(b, s, TK_PREP_REF, false);
     int n = b->n;
     auto D = b->d_desc;
     auto in = b->d_inptr;
-    k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(
-        D, 1, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
-    k_normals<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(D, b->d_active);
+    if (from_inputs)
+        k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, s>>>(
+            D, 1, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
+    else
+        k_ref_from_z<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
+    k_normals<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
     for (int l = 1; l < b->max_L; l++)
-        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, b->stream>>>(D, l, 1, b->d_active);
-    k_clear_ref<<<dim3(1, n), 256, 0, b->stream>>>(D, b->d_active);
-    k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(D, b->d_active);
-    k_seg_count<<<dim3(kSegments / 8, n), 256, 0, b->stream>>>(D, b->d_active);
-    k_seg_scan<<<dim3(1, n), 32, 0, b->stream>>>(D, b->d_active);
-    k_seg_scatter<<<dim3(kSegments / 8, n), 256, 0, b->stream>>>(D, b->d_active);
-    k_attr_jac<<<grid_pix(b->max_P, n), 256, 0, b->stream>>>(D, b->d_active);
-    k_reset_pose<<<dim3(1, n), 32, 0, b->stream>>>(D, b->d_active);
-    g_launches += 10 + (b->max_L - 1);
+        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, 1, b->d_active);
+    k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, b->d_active);
+    k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
+    k_seg_count<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, b->d_active);
+    k_seg_scan<<<dim3(1, n), 32, 0, s>>>(D, b->d_active);
+    k_seg_scatter<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, b->d_active);
+    k_attr_jac<<<grid_pix(b->max_P, n), 256, 0, s>>>(D, b->d_active);
+    if (reset_pose) k_reset_pose<<<dim3(1, n), 32, 0, s>>>(D, b->d_active);
+    g_launches += 9 + (b->max_L - 1) + (reset_pose ? 1 : 0);
     CK(cudaGetLastError());
     return RECON_OK;
 }
 
-int prepare_current(recon_batch *b) {
+int prepare_current(recon_batch *b, const void **in = nullptr, const int *active = nullptr) {
     TimedScope ts(b, b->stream, TK_PREP_CUR, false);
     int n = b->n;
     auto D = b->d_desc;
-    auto in = b->d_inptr;
+    if (!in) in = b->d_inptr;
+    if (!active) active = b->d_active;
     k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(
         D, 0, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
     for (int l = 1; l < b->max_L; l++)
-        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, b->stream>>>(D, l, 0, b->d_active);
+        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, b->stream>>>(D, l, 0, active);
     g_launches += 1 + (b->max_L - 1);
     CK(cudaGetLastError());
     return RECON_OK;
 }
 
 // the per-frame Gauss-Newton schedule (gpuEstimateIncrement, phototracker.cpp:666-689)
-int launch_schedule(recon_batch *b, cudaStream_t s) {
+int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
     int n = b->n;
     auto D = b->d_desc;
     bool any_icp = false;
@@ -343,22 +381,23 @@ int launch_schedule(recon_batch *b, cudaStream_t s) {
         int nchunk = (maxpix + kChunk - 1) / kChunk;
         if (any_icp) {
             {
-                TimedScope ts(b, s, TK_ICP_MASK, true);
+                TimedScope ts(b, s, TK_ICP_MASK, in_graph);
                 k_icp_mask<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
             }
             {
-                TimedScope ts(b, s, TK_ICP_COMPACT, true);
+                TimedScope ts(b, s, TK_ICP_COMPACT, in_graph);
                 k_icp_compact<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
             }
             for (int pass = 1; pass <= 3; pass++) {
-                TimedScope ts(b, s, TK_ICP_STUDENT, true);
+                TimedScope ts(b, s, TK_ICP_STUDENT, in_graph);
                 k_icp_student<<<grid_pix(maxpix, n), 256, 0, s>>>(D, level, pass);
             }
             b->graph_kernels += 5;
         }
+        int nph = b->max_P / kChunk;
         for (int it = 0; it < maxit; it++) {
-            TimedScope ts(b, s, TK_ITER, true);
-            k_iter<<<dim3(1 + (any_icp ? nchunk : 0), n), kLanes, 0, s>>>(D, level, it);
+            TimedScope ts(b, s, TK_ITER, in_graph);
+            k_iter<<<dim3(nph + (any_icp ? nchunk : 0), n), kLanes, 0, s>>>(D, level, it, nph);
             b->graph_kernels++;
         }
     }
@@ -367,6 +406,14 @@ int launch_schedule(recon_batch *b, cudaStream_t s) {
 }
 
 int run_schedule(recon_batch *b) {
+    if (b->timing) {
+        // timed runs launch directly so that every launch keeps its own events
+        b->graph_kernels = 0;
+        int rc = launch_schedule(b, b->stream, false);
+        g_launches += b->graph_kernels;
+        b->graph_dirty = true;
+        return rc;
+    }
     if (b->graph_dirty) {
         if (b->graph) cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -384,7 +431,7 @@ int run_schedule(recon_batch *b) {
             return cuda_fail(e, "cudaStreamBeginCapture");
         }
         b->graph_kernels = 0;
-        int rc = launch_schedule(b, cs);
+        int rc = launch_schedule(b, cs, true);
         e = cudaStreamEndCapture(cs, &g);
         cudaStreamDestroy(cs);
         if (rc) return rc;
@@ -422,6 +469,11 @@ __global__ void k_clear_ref(const InstDesc *D, const int *active) {
     for (int k = threadIdx.x; k < d.P; k += blockDim.x) d.sel_idx[k] = 0;
 }
 
+__global__ void k_store_pose(const InstDesc *D, float *dst) {
+    const InstDesc &d = D[blockIdx.y];
+    if (threadIdx.x < 16) dst[16 * blockIdx.y + threadIdx.x] = d.T[threadIdx.x];
+}
+
 __global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_init) {
     const InstDesc &d = D[blockIdx.y];
     int t = threadIdx.x;
@@ -429,8 +481,10 @@ __global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_i
     if (t < ST_COUNT) d.stats[t] = 0;
     if (t == 0) {
         *d.counter = 0u;
+        *d.ph_counter = 0u;
         if (d.trace_count) *d.trace_count = 0;
     }
+    for (int k = t; k < 256; k += blockDim.x) d.ph_hist[k] = 0;
 }
 
 }  // namespace rt
@@ -585,6 +639,30 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->d_Tinit) cudaFree(b->d_Tinit);
     if (b->d_trace) cudaFree(b->d_trace);
     if (b->d_trace_count) cudaFree(b->d_trace_count);
+    if (b->d_seqptr) cudaFree(b->d_seqptr);
+    if (b->h_seqptr) cudaFreeHost(b->h_seqptr);
+    if (b->d_Tseq) cudaFree(b->d_Tseq);
+    if (b->d_ones) cudaFree(b->d_ones);
+    for (int k = 0; k < 2; k++) {
+        if (b->d_slot[k]) cudaFree(b->d_slot[k]);
+        if (b->ev_copied[k]) cudaEventDestroy(b->ev_copied[k]);
+        if (b->ev_free[k]) cudaEventDestroy(b->ev_free[k]);
+    }
+    if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
+    if (b->recon_stream) cudaStreamDestroy(b->recon_stream);
+    if (b->ev_pose) cudaEventDestroy(b->ev_pose);
+    if (b->ev_fused) cudaEventDestroy(b->ev_fused);
+    if (b->d_fuse) cudaFree(b->d_fuse);
+    if (b->d_fuse_ptr) cudaFree(b->d_fuse_ptr);
+    if (b->d_fuse_T) cudaFree(b->d_fuse_T);
+    for (auto &ev : b->graph_events) {
+        cudaEventDestroy(ev.second.first);
+        cudaEventDestroy(ev.second.second);
+    }
+    for (auto &ev : b->direct_events) {
+        cudaEventDestroy(ev.second.first);
+        cudaEventDestroy(ev.second.second);
+    }
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RECON_OK;
@@ -834,6 +912,191 @@ int recon_batch_get_work(recon_batch *b, uint64_t *out, int32_t reset) {
 void *recon_batch_stream(recon_batch *b) { return b ? (void *)b->stream : nullptr; }
 
 int64_t recon_launch_count(void) { return g_launches.load(); }
+
+int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const *gray, const uint16_t *const *depth,
+                               int32_t on_device, float *T_out, recon_track_stats *stats) {
+    clear_stale_error();
+    if (!b || nf <= 0 || !gray || !depth) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    if (!b->have_ref) return fail(RECON_ERR_STATE, "reference frame missing");
+    int n = b->n;
+    for (size_t k = 0; k < (size_t)nf * n; k++)
+        if (!gray[k] || !depth[k]) return fail(RECON_ERR_INVALID_ARG, "null frame pointer");
+    if (!b->d_ones) {
+        std::vector<int> ones(n, 1);
+        CK(cudaMalloc(&b->d_ones, n * sizeof(int)));
+        CK(cudaMemcpy(b->d_ones, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    size_t rows = on_device ? (size_t)nf : 2;
+    size_t need_ptr = rows * 3 * n;
+    if (need_ptr > b->seqptr_cap) {
+        if (b->d_seqptr) cudaFree(b->d_seqptr);
+        if (b->h_seqptr) cudaFreeHost(b->h_seqptr);
+        b->d_seqptr = nullptr;
+        b->h_seqptr = nullptr;
+        b->seqptr_cap = 0;
+        CK(cudaMalloc(&b->d_seqptr, need_ptr * sizeof(void *)));
+        CK(cudaMallocHost(&b->h_seqptr, need_ptr * sizeof(void *)));
+        b->seqptr_cap = need_ptr;
+    }
+    size_t need_T = (size_t)nf * n * 16;
+    if (need_T > b->Tseq_cap) {
+        if (b->d_Tseq) cudaFree(b->d_Tseq);
+        b->d_Tseq = nullptr;
+        b->Tseq_cap = 0;
+        CK(cudaMalloc(&b->d_Tseq, need_T * sizeof(float)));
+        b->Tseq_cap = need_T;
+    }
+    std::vector<size_t> px(n);
+    size_t frame_bytes = 0;
+    for (int i = 0; i < n; i++) {
+        px[i] = (size_t)b->cfg[i].width * b->cfg[i].height;
+        frame_bytes += align256(px[i]) + align256(2 * px[i]);
+    }
+    if (!on_device) {
+        if (frame_bytes > b->slot_bytes) {
+            for (int k = 0; k < 2; k++) {
+                if (b->d_slot[k]) cudaFree(b->d_slot[k]);
+                b->d_slot[k] = nullptr;
+            }
+            b->slot_bytes = 0;
+            for (int k = 0; k < 2; k++) CK(cudaMalloc(&b->d_slot[k], frame_bytes));
+            b->slot_bytes = frame_bytes;
+        }
+        if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) {
+            if (!b->ev_copied[k]) CK(cudaEventCreateWithFlags(&b->ev_copied[k], cudaEventDisableTiming));
+            if (!b->ev_free[k]) CK(cudaEventCreateWithFlags(&b->ev_free[k], cudaEventDisableTiming));
+        }
+        // the two staging slots are the only two rows of the pointer table
+        for (int k = 0; k < 2; k++) {
+            size_t off = 0;
+            for (int i = 0; i < n; i++) {
+                b->h_seqptr[(size_t)k * 3 * n + i] = b->d_slot[k] + off;
+                off += align256(px[i]);
+                b->h_seqptr[(size_t)k * 3 * n + n + i] = b->d_slot[k] + off;
+                off += align256(2 * px[i]);
+                b->h_seqptr[(size_t)k * 3 * n + 2 * n + i] = nullptr;
+            }
+        }
+    } else {
+        for (int f = 0; f < nf; f++)
+            for (int i = 0; i < n; i++) {
+                b->h_seqptr[(size_t)f * 3 * n + i] = gray[(size_t)f * n + i];
+                b->h_seqptr[(size_t)f * 3 * n + n + i] = depth[(size_t)f * n + i];
+                b->h_seqptr[(size_t)f * 3 * n + 2 * n + i] = nullptr;
+            }
+    }
+    CK(cudaMemcpyAsync(b->d_seqptr, b->h_seqptr, need_ptr * sizeof(void *), cudaMemcpyHostToDevice, b->stream));
+    if (!on_device) {
+        // the previous call's last kernels may still read the slots
+        CK(cudaEventRecord(b->ev_free[0], b->stream));
+        CK(cudaEventRecord(b->ev_free[1], b->stream));
+    }
+    for (int f = 0; f < nf; f++) {
+        const void **row;
+        if (on_device) {
+            row = b->d_seqptr + (size_t)f * 3 * n;
+        } else {
+            int k = f & 1;
+            row = b->d_seqptr + (size_t)k * 3 * n;
+            // copy frame f into slot k once the frame that used it (f-2) is done
+            CK(cudaStreamWaitEvent(b->copy_stream, b->ev_free[k], 0));
+            for (int i = 0; i < n; i++) {
+                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + i], gray[(size_t)f * n + i], px[i],
+                                   cudaMemcpyHostToDevice, b->copy_stream));
+                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + n + i], depth[(size_t)f * n + i],
+                                   2 * px[i], cudaMemcpyHostToDevice, b->copy_stream));
+            }
+            CK(cudaEventRecord(b->ev_copied[k], b->copy_stream));
+            CK(cudaStreamWaitEvent(b->stream, b->ev_copied[k], 0));
+        }
+        int rc = prepare_current(b, row, b->d_ones);
+        if (rc) return rc;
+        if (!on_device) CK(cudaEventRecord(b->ev_free[f & 1], b->stream));
+        k_begin_track<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, 0);
+        g_launches += 1;
+        rc = run_schedule(b);
+        if (rc) return rc;
+        k_store_pose<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tseq + (size_t)f * n * 16);
+        g_launches += 1;
+        CK(cudaGetLastError());
+    }
+    b->have_cur = true;
+    if (T_out) CK(cudaMemcpyAsync(T_out, b->d_Tseq, need_T * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+    return recon_batch_get_poses(b, nullptr, stats);
+}
+
+int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *const *depth, const float *T_host,
+                              int32_t on_device, float gate_mm) {
+    clear_stale_error();
+    if (!b || nframes < 1 || nframes > 8 || !depth || !T_host || !(gate_mm > 0.0f))
+        return fail(RECON_ERR_INVALID_ARG, "bad argument (1..8 frames, positive gate)");
+    if (!b->have_ref) return fail(RECON_ERR_STATE, "reference frame missing");
+    int n = b->n;
+    size_t cnt = (size_t)nframes * n;
+    for (size_t k = 0; k < cnt; k++)
+        if (!depth[k]) return fail(RECON_ERR_INVALID_ARG, "null depth pointer");
+    if (!b->recon_stream) {
+        CK(cudaStreamCreateWithFlags(&b->recon_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&b->ev_pose, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b->ev_fused, cudaEventDisableTiming));
+    }
+    if (cnt > b->fuse_cap) {
+        if (b->d_fuse_ptr) cudaFree(b->d_fuse_ptr);
+        if (b->d_fuse_T) cudaFree(b->d_fuse_T);
+        b->d_fuse_ptr = nullptr;
+        b->d_fuse_T = nullptr;
+        b->fuse_cap = 0;
+        CK(cudaMalloc(&b->d_fuse_ptr, cnt * sizeof(void *)));
+        CK(cudaMalloc(&b->d_fuse_T, cnt * 16 * sizeof(float)));
+        b->fuse_cap = cnt;
+    }
+    std::vector<const void *> ptrs(cnt);
+    std::vector<size_t> px(n);
+    size_t bytes = 0;
+    for (int i = 0; i < n; i++) {
+        px[i] = (size_t)b->cfg[i].width * b->cfg[i].height;
+        bytes += (size_t)nframes * align256(2 * px[i]);
+    }
+    // the fusion waits for the pose stream's pending work (tracked frames)
+    CK(cudaEventRecord(b->ev_pose, b->stream));
+    CK(cudaStreamWaitEvent(b->recon_stream, b->ev_pose, 0));
+    if (!on_device) {
+        if (bytes > b->fuse_bytes) {
+            if (b->d_fuse) cudaFree(b->d_fuse);
+            b->d_fuse = nullptr;
+            b->fuse_bytes = 0;
+            CK(cudaMalloc(&b->d_fuse, bytes));
+            b->fuse_bytes = bytes;
+        }
+        size_t off = 0;
+        for (int f = 0; f < nframes; f++)
+            for (int i = 0; i < n; i++) {
+                uint8_t *dst = (uint8_t *)b->d_fuse + off;
+                CK(cudaMemcpyAsync(dst, depth[(size_t)f * n + i], 2 * px[i], cudaMemcpyHostToDevice,
+                                   b->recon_stream));
+                ptrs[(size_t)f * n + i] = dst;
+                off += align256(2 * px[i]);
+            }
+    } else {
+        for (size_t k = 0; k < cnt; k++) ptrs[k] = depth[k];
+    }
+    std::vector<int> ones(n, 1);
+    CK(cudaMemcpyAsync(b->d_fuse_ptr, ptrs.data(), cnt * sizeof(void *), cudaMemcpyHostToDevice, b->recon_stream));
+    CK(cudaMemcpyAsync(b->d_fuse_T, T_host, cnt * 16 * sizeof(float), cudaMemcpyHostToDevice, b->recon_stream));
+    CK(cudaMemcpyAsync(b->d_active, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->recon_stream));
+    k_fuse_depth<<<grid_pix(b->max_pix, n), 256, 0, b->recon_stream>>>(
+        b->d_desc, nframes, n, (const uint16_t *const *)b->d_fuse_ptr, b->d_fuse_T, gate_mm, b->d_active);
+    g_launches += 1;
+    int rc = prepare_reference(b, false, false, b->recon_stream);
+    if (rc) return rc;
+    // the pose stream continues with the fused reference
+    CK(cudaEventRecord(b->ev_fused, b->recon_stream));
+    CK(cudaStreamWaitEvent(b->stream, b->ev_fused, 0));
+    // pageable sources (ptrs, ones, T_host) must outlive the copies
+    CK(cudaStreamSynchronize(b->recon_stream));
+    return RECON_OK;
+}
 
 // ---- single tracker ----
 int recon_tracker_create(const recon_config *cfg, const float *calib, void *stream, recon_tracker **out) {

@@ -136,6 +136,85 @@ __global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int
     }
 }
 
+// Keyframe depth fusion (the oracle's orc_fuse_depth restates the same steps):
+// every valid keyframe pixel is back-projected with KL (rgb2gray.cu:570-593),
+// mapped into frame f by its tracked pose, looked up at the nearest IR pixel
+// (the zWeight tap of warp.cu:306-327), mapped back with the inverse pose (as
+// filterDepthIIRKernel does, warp.cu:398-467), gated on |dz| < gate and averaged
+// with unit weights (the running mean of updateVoxelsKernel,
+// VoxelGrid_cuda.cu:1005-1013).  Writes the fused depth in place into ref_z.
+// depth: nframes x n_inst frame pointers; Tf: nframes x n_inst x 16 poses.
+__global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const uint16_t *const *depth,
+                             const float *Tf, float gate, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    __shared__ float sT[8][16], sTi[8][16];
+    if (threadIdx.x < nframes && threadIdx.x < 8) {
+        const float *M = Tf + ((size_t)threadIdx.x * n_inst + blockIdx.y) * 16;
+        float *Mi = sTi[threadIdx.x];
+        for (int k = 0; k < 16; k++) sT[threadIdx.x][k] = M[k];
+        // invertRT4Cuda, kernelUtils.h:100-107
+        Mi[0] = M[0]; Mi[1] = M[4]; Mi[2] = M[8];   Mi[3] = -(M[0] * M[3] + M[4] * M[7] + M[8] * M[11]);
+        Mi[4] = M[1]; Mi[5] = M[5]; Mi[6] = M[9];   Mi[7] = -(M[1] * M[3] + M[5] * M[7] + M[9] * M[11]);
+        Mi[8] = M[2]; Mi[9] = M[6]; Mi[10] = M[10]; Mi[11] = -(M[2] * M[3] + M[6] * M[7] + M[10] * M[11]);
+        Mi[12] = 0;   Mi[13] = 0;   Mi[14] = 0;     Mi[15] = 1;
+    }
+    __syncthreads();
+    int W = d.W, H = d.H;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W * H) return;
+    float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
+    const float *KL = d.calib + RC_KL;
+    float fx = KL[0], fy = KL[4], cx = KL[2], cy = KL[5];
+    int xi = idx % W, yi = idx / W;
+    float z = d.ref_z[idx];
+    if (!(z < -minDist && z > -maxDist)) return;
+    float px3 = ((float)xi - cx) * z / fx, py3 = ((float)yi - cy) * z / fy, pz3 = z;
+    float zsum = z, wsum = 1.0f;
+    for (int f = 0; f < nframes && f < 8; f++) {
+        float qx, qy, qz;
+        mul4(sT[f], px3, py3, pz3, qx, qy, qz);
+        float q2x = qx / qz, q2y = qy / qz;
+        float pxl = KL[0] * q2x + KL[1] * q2y + KL[2];
+        float pyl = KL[3] * q2x + KL[4] * q2y + KL[5];
+        int xd = ftoi(pxl + 0.5f), yd = ftoi(pyl + 0.5f);
+        if (xd < 0 || yd < 0 || xd >= W || yd >= H) continue;
+        uint16_t dm = depth[(size_t)f * n_inst + blockIdx.y][xd + yd * W];
+        float zf = dm ? -(float)dm : 0.0f;
+        if (!(zf < -minDist && zf > -maxDist)) continue;
+        float mx = ((float)xd - cx) * zf / fx, my = ((float)yd - cy) * zf / fy, mz = zf;
+        float kx, ky, kz;
+        mul4(sTi[f], mx, my, mz, kx, ky, kz);
+        float dz = kz - z;
+        if (fabsf(dz) < gate) {
+            zsum += kz;
+            wsum += 1.0f;
+        }
+    }
+    d.ref_z[idx] = zsum / wsum;
+}
+
+// reference level-0 points from ref_z (convertZMapToXYZ6Kernel, rgb2gray.cu:595-624)
+__global__ void k_ref_from_z(const InstDesc *D, const int *active) {
+    INST_DESC;
+    if (!active[blockIdx.y]) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.W * d.H) return;
+    int xi = i % d.W, yi = i / d.W;
+    float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
+    float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
+    float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
+    float z = d.ref_z[i];
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (z < -minDist && z > -maxDist) {
+        o.x = ((float)xi - cx) * z / fx;
+        o.y = ((float)yi - cy) * z / fy;
+        o.z = z;
+        o.w = 1.0f;
+    }
+    d.ref_pts[0][i] = o;
+}
+
 // computeNormalsCudaKernel, d2z.cu:503-537 (reference level 0)
 __global__ void k_normals(const InstDesc *D, const int *active) {
     INST_DESC;
@@ -553,6 +632,10 @@ __global__ void k_icp_compact(const InstDesc *D, int level) {
             d.icp_select[pos] = i;
             d.icp_r2[pos] = r2;
             d.icp_w[pos] = w0;
+            d.icp_pk_pts[pos] = d.ref_pts[level][i];
+            float4 nn = d.ref_nrm[level][i];
+            nn.w = w0;
+            d.icp_pk_nrm[pos] = nn;
             vsum += trunc_prod(r2, w0);
         }
         base += tot;
@@ -580,6 +663,7 @@ __global__ void k_icp_student(const InstDesc *D, int level, int pass) {
         if (pass == 3) wv = fminf(wv, 1.0f);
         else vsum = trunc_prod(r2, wv);
         d.icp_w[i] = wv;
+        d.icp_pk_nrm[i].w = wv;
     }
     if (pass < 3) block_add_ll(&d.icp_var[pass], vsum);
 }
@@ -709,7 +793,9 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
     }
 }
 
-// icpResidualIndexKernel2, rgb2gray.cu:323-390, for one point
+// icpResidualIndexKernel2, rgb2gray.cu:323-390, for one point.  The selected
+// reference point and normal were packed in selection order by k_icp_compact,
+// with the Student-t weight in the normal's fourth lane.
 __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int level, int idx, int nsel, float *j,
                                           float &res) {
     res = 0.0f;
@@ -720,9 +806,8 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     const float *K = d.calib + RC_KL;
     float a = 1.0f / (float)(1 << level);
     float b = 0.5f * (a - 1.0f);
-    int sel = d.icp_select[idx];
-    float4 p = d.ref_pts[level][sel];
-    float4 rn = d.ref_nrm[level][sel];
+    float4 p = __ldg(d.icp_pk_pts + idx);
+    float4 rn = __ldg(d.icp_pk_nrm + idx);
     float qx, qy, qz, cnx, cny, cnz;
     mul4(T, p.x, p.y, p.z, qx, qy, qz);
     rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
@@ -730,7 +815,7 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     float p2x = a * (K[0] * q2x + K[2]) + b;
     float p2y = a * (K[4] * q2y + K[5]) + b;
     if (!(p2x >= 0 && p2x < (w - 1) && p2y >= 0 && p2y < (h - 1))) return;
-    float weight = d.icp_w[idx];
+    float weight = rn.w;
     int xdi = ftoi(p2x), ydi = ftoi(p2y);
     float fx = p2x - xdi, fy = p2y - ydi;
     int off2 = xdi + ydi * w;
@@ -764,6 +849,7 @@ __device__ void icp_chunk(const InstDesc &d, IterShared &sh, int level, int chun
     float acc[27];
 #pragma unroll
     for (int q = 0; q < 27; q++) acc[q] = 0.0f;
+#pragma unroll
     for (int m = 0; m < 4; m++) {
         int idx = chunk * kChunk + threadIdx.x + kLanes * m;
         float j[6], r;
@@ -785,54 +871,14 @@ __device__ __forceinline__ void unpack27(const double *t, double *A, double *b) 
     for (int c = 0; c < 6; c++) b[c] = t[q++];
 }
 
-// One GN iteration at `level`, iteration `it`.  blockIdx.x == 0 is the
-// photometric CTA (updateLinearSystem, phototracker.cpp:505-511); blockIdx.x
-// >= 1 are ICP chunks (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).
-// The last CTA of an instance to finish fuses (linearFuse, shapetracker.cpp:392-394),
-// solves and applies the SE(3) update (estimateIncrement, phototracker.cpp:646-664).
-__global__ void __launch_bounds__(256) k_iter(const InstDesc *D, int level, int it) {
-    INST_DESC;
-    if (level >= d.L) return;
-    if (it >= d.iters[d.L - 1 - level]) return;
-    bool use_ph = d.mode != RECON_GEOMETRIC;
-    bool use_icp = d.mode != RECON_PHOTOMETRIC;
-    int nsel = use_icp ? d.icp_nsel[level] : 0;
-    int nchunks = (nsel + kChunk - 1) / kChunk;
-    // CTA 0 always takes part (it carries the photometric term when the mode
-    // has one), so every iteration is finalised exactly once
-    int expected = 1 + nchunks;
-    int role = blockIdx.x;
-    if (role >= 1 && role - 1 >= nchunks) return;
-    __shared__ IterShared sh;
-    if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
-    __syncthreads();
-    if (role == 0) {
-        if (use_ph) photo_iteration(d, sh, level);
-    } else {
-        icp_chunk(d, sh, level, role - 1, nsel);
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned int ticket = atomicAdd(d.counter, 1u);
-        sh.last = (ticket == (unsigned)(expected - 1));
-    }
-    __syncthreads();
-    if (!sh.last) return;
-    __threadfence();
-    // ---- finalize: ICP totals in chunk order, fuse, solve, update ----
-    if (threadIdx.x < 27) {
-        int q = threadIdx.x;
-        double tot = 0.0;
-        for (int c = 0; c < nchunks; c++) tot = tot + __ldcg(d.icp_part + (size_t)c * 27 + q);
-        sh.A_icp[q] = tot;
-        if (use_ph) sh.A_ph[q] = __ldcg(d.ph_part + q);
-    }
-    __syncthreads();
-    if (threadIdx.x >= 32) return;
+// Warp 0 of the finalising CTA: builds the system of the mode (fused in FP64
+// for BIOBJECTIVE, linearFuseKernel warp.cu:918-924), solves, updates the pose
+// and records statistics and the optional iteration trace.
+__device__ __noinline__ void finalize_solve(const InstDesc &d, IterShared &sh, int level, int it, bool use_ph,
+                                            bool use_icp, int nsel) {
     int lane = threadIdx.x;
     SolveScratch &S = sh.S;
-    bool ok = true;
+    int median = use_ph ? __ldcg(d.ph_hist + 512) : -1;
     if (lane == 0) {
         double Aph[36], bph[6], Aic[36], bic[6];
         for (int i = 0; i < 36; i++) { Aph[i] = 0.0; Aic[i] = 0.0; }
@@ -846,13 +892,13 @@ __global__ void __launch_bounds__(256) k_iter(const InstDesc *D, int level, int 
             for (int i = 0; i < 36; i++) S.A[i] = Aic[i];
             for (int i = 0; i < 6; i++) S.b[i] = bic[i];
         } else {
-            // linearFuseKernel (warp.cu:918-924) in FP64: (1-lambda)/N1 * photo + lambda/N2 * icp
+            // (1-lambda)/N1 * photo + lambda/N2 * icp
             double c1 = (double)(1.0f - d.lambda) / (double)d.P;
             double c2 = (double)d.lambda / (double)nsel;
             for (int i = 0; i < 36; i++) S.A[i] = c1 * Aph[i] + c2 * Aic[i];
             for (int i = 0; i < 6; i++) S.b[i] = c1 * bph[i] + c2 * bic[i];
         }
-        if (d.trace && it >= 0) {
+        if (d.trace) {
             int slot = *d.trace_count;
             if (slot < d.trace_max) {
                 recon_iter_trace *tr = d.trace + slot;
@@ -861,7 +907,7 @@ __global__ void __launch_bounds__(256) k_iter(const InstDesc *D, int level, int 
             }
         }
     }
-    if (use_icp && nsel <= 0) ok = false;  // ShapeTracker "not enough points": no solve
+    bool ok = !(use_icp && nsel <= 0);  // ShapeTracker "not enough points": no solve
     __syncwarp();
     int st = 0;
     if (ok) st = wsolve_update(S, d.solver, sh.T, (double)d.opt_out, lane);
@@ -870,7 +916,7 @@ __global__ void __launch_bounds__(256) k_iter(const InstDesc *D, int level, int 
         d.stats[ST_ITERS] += 1;
         if (ok) d.stats[ST_SOLVES] += 1;
         if (st != 0) d.stats[ST_NONSPD] += 1;
-        if (use_ph) d.stats[ST_MEDIAN] = sh.median;
+        if (use_ph) d.stats[ST_MEDIAN] = median;
         if (use_ph) d.work[0] += (unsigned long long)d.P;
         if (use_icp) d.work[1] += (unsigned long long)nsel;
         if (use_icp) d.stats[ST_ICPSEL0 + level] = nsel;
@@ -885,13 +931,202 @@ __global__ void __launch_bounds__(256) k_iter(const InstDesc *D, int level, int 
                 tr->status = st;
                 tr->icp_selected = use_icp ? nsel : 0;
                 for (int i = 0; i < 16; i++) tr->T[i] = sh.T[i];
-                tr->median_bin = use_ph ? sh.median : -1;
-                for (int k = 0; k < 256; k++) tr->hist[k] = (use_ph && k < d.hist_bins) ? sh.hist[k] : 0;
+                tr->median_bin = median;
+                for (int k = 0; k < 256; k++)
+                    tr->hist[k] = (use_ph && k < d.hist_bins) ? __ldcg(d.ph_hist + 256 + k) : 0;
             }
             *d.trace_count = slot + 1;
         }
         *d.counter = 0u;
     }
+}
+
+// Photometric pass A for chunk c of an instance (interpolateResidualKernel2,
+// warp.cu:269-332, and the histogram of histogram64.cu:115-145): residuals and
+// depth weights of 1024 points to global scratch, their MAD-histogram counts
+// added to the instance's global histogram.
+__device__ void photo_pass_a(const InstDesc &d, IterShared &sh, int level, int c) {
+    int P = d.P;
+    int w = d.W >> level, h = d.H >> level;
+    float a = 1.0f / (float)(1 << level);
+    float b = 0.5f * (a - 1.0f);
+    const float *img = d.cur_gray[level];
+    const float *I = d.sel_I[level];
+    int nb = d.hist_bins;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) sh.hist[k] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        int i = c * kChunk + threadIdx.x + kLanes * m;
+        float r, zw;
+        photo_residual(d.calib, sh.T, a, b, __ldg(d.sel_xyz + i), __ldg(d.sel_xyz + P + i),
+                       __ldg(d.sel_xyz + 2 * P + i), __ldg(I + i), img, w, h, d.cur_z, d.W, d.H, r, zw);
+        d.ph_r[i] = r;
+        d.ph_zw[i] = zw;
+        atomicAdd(&sh.hist[mad_bin(r, nb)], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nb; k += blockDim.x)
+        if (sh.hist[k]) atomicAdd(d.ph_hist + k, sh.hist[k]);
+}
+
+// Photometric pass B, run by the last pass-A CTA of an instance: median bin
+// (seekThreshold64Kernel, histogram64.cu:48-61), Tukey weights
+// (generateWeights64Kernel, 79-94) and the 27 terms over all points in the
+// canonical chunk order.
+__device__ void photo_pass_b(const InstDesc &d, IterShared &sh, int level) {
+    int P = d.P;
+    int nb = d.hist_bins;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+        int v = __ldcg(d.ph_hist + k);
+        sh.hist[k] = v;
+        d.ph_hist[256 + k] = v;  // kept for the iteration trace
+        d.ph_hist[k] = 0;        // ready for the next iteration
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int lane = threadIdx.x;
+        int per = (nb + 31) / 32;
+        int loc = 0;
+        for (int k = 0; k < per; k++) {
+            int bin = lane * per + k;
+            if (bin < nb) loc += sh.hist[bin];
+        }
+        int incl = loc;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        int half = P / 2;
+        unsigned int over = __ballot_sync(0xffffffffu, incl > half);
+        if (over) {
+            int l0 = __ffs(over) - 1;
+            if (lane == l0) {
+                int acc = incl - loc, med = 0;
+                for (int k = 0; k < per; k++) {
+                    int bin = lane * per + k;
+                    if (bin < nb) {
+                        acc += sh.hist[bin];
+                        if (acc > half) { med = bin; break; }
+                    }
+                }
+                sh.median = med;
+            }
+        } else if (lane == 0) {
+            sh.median = 0;
+        }
+    }
+    for (int q = threadIdx.x; q < 27; q += blockDim.x) sh.tot[q] = 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        d.ph_hist[512] = sh.median;
+        *d.ph_counter = 0u;
+    }
+    float s = mad_scale(sh.median, nb);
+    const float *J = d.sel_J[level];
+    int t = threadIdx.x;
+    for (int c = 0; c < P / kChunk; c++) {
+        float acc[27];
+#pragma unroll
+        for (int q = 0; q < 27; q++) acc[q] = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            int i = c * kChunk + t + kLanes * m;
+            float r = __ldcg(d.ph_r + i);
+            float wv = tukey_weight(r, __ldcg(d.ph_zw + i), s);
+            float jw[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) jw[k] = __ldg(J + k * P + i) * wv;
+            acc27(acc, jw, r * wv);
+        }
+        chunk_fold(sh, acc);
+    }
+    if (threadIdx.x < 27) {
+        sh.A_ph[threadIdx.x] = sh.tot[threadIdx.x];
+        d.ph_part[threadIdx.x] = sh.tot[threadIdx.x];
+    }
+}
+
+// One GN iteration at `level`, iteration `it`, for every instance.
+// blockIdx.x in [0, nph_grid): photometric pass A of chunk blockIdx.x (the last
+// of an instance's chunks also runs pass B) -- updateLinearSystem,
+// phototracker.cpp:505-511; blockIdx.x >= nph_grid: ICP chunks of 1024
+// correspondences (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).
+// The last participant of an instance to finish fuses (linearFuse,
+// shapetracker.cpp:392-394), solves and applies the SE(3) update
+// (estimateIncrement, phototracker.cpp:646-664).  No CTA waits for another:
+// completion is counted with atomic tickets.
+__global__ void __launch_bounds__(256, 3) k_iter(const InstDesc *D, int level, int it, int nph_grid) {
+    INST_DESC;
+    if (level >= d.L) return;
+    if (it >= d.iters[d.L - 1 - level]) return;
+    bool use_ph = d.mode != RECON_GEOMETRIC;
+    bool use_icp = d.mode != RECON_PHOTOMETRIC;
+    int nsel = use_icp ? d.icp_nsel[level] : 0;
+    int nchunks = (nsel + kChunk - 1) / kChunk;
+    int nph = d.P / kChunk;
+    int role = blockIdx.x;
+    bool is_ph = role < nph_grid;
+    if (is_ph) {
+        if (role >= nph) return;
+        if (!use_ph && role != 0) return;  // without a photometric term CTA 0 is a null participant
+    } else if (role - nph_grid >= nchunks) {
+        return;
+    }
+    // participants of the instance ticket: the photometric pass-B CTA (or the
+    // null participant) and every ICP chunk, so each iteration is finalised once
+    int expected = 1 + nchunks;
+    __shared__ IterShared sh;
+    if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
+    __syncthreads();
+    if (is_ph) {
+        if (use_ph) {
+            photo_pass_a(d, sh, level, role);
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned int ticket = atomicAdd(d.ph_counter, 1u);
+                sh.last = (ticket == (unsigned)(nph - 1));
+            }
+            __syncthreads();
+            if (!sh.last) return;
+            __threadfence();
+            photo_pass_b(d, sh, level);
+        }
+    } else {
+        icp_chunk(d, sh, level, role - nph_grid, nsel);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int ticket = atomicAdd(d.counter, 1u);
+        sh.last = (ticket == (unsigned)(expected - 1));
+    }
+    __syncthreads();
+    if (!sh.last) return;
+    __threadfence();
+    // ---- finalize: ICP totals in chunk order, fuse, solve, update ----
+    if (threadIdx.x < 27) {
+        int q = threadIdx.x;
+        double tot = 0.0;
+        int c = 0;
+        for (; c + 4 <= nchunks; c += 4) {
+            double v0 = __ldcg(d.icp_part + (size_t)(c + 0) * 27 + q);
+            double v1 = __ldcg(d.icp_part + (size_t)(c + 1) * 27 + q);
+            double v2 = __ldcg(d.icp_part + (size_t)(c + 2) * 27 + q);
+            double v3 = __ldcg(d.icp_part + (size_t)(c + 3) * 27 + q);
+            tot = tot + v0;
+            tot = tot + v1;
+            tot = tot + v2;
+            tot = tot + v3;
+        }
+        for (; c < nchunks; c++) tot = tot + __ldcg(d.icp_part + (size_t)c * 27 + q);
+        sh.A_icp[q] = tot;
+        if (use_ph) sh.A_ph[q] = __ldcg(d.ph_part + q);
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    finalize_solve(d, sh, level, it, use_ph, use_icp, nsel);
 }
 
 // ------------------------------------------------------------------

@@ -69,7 +69,7 @@ __device__ __forceinline__ int expm_squarings(double hnorm) {
 
 // exp(A) by the diagonal (6,6) Pade approximant with scaling and squaring (the
 // method of EXPOKIT zgpadm used at expmCuda.cu:1642), real FP64.  Result in S.E.
-__device__ void wexpm_twist(SolveScratch &S, const double *A, int lane) {
+static __device__ void wexpm_twist(SolveScratch &S, const double *A, int lane) {
     if (lane == 0) {
         double hnorm = 0.0;
         for (int r = 0; r < 4; r++) {
@@ -167,7 +167,7 @@ __device__ void wexpm_twist(SolveScratch &S, const double *A, int lane) {
 
 // generateA + expmKernel (warp.cu:910-915, expmCuda.cu:1989-2048): T <- T * exp(A(x)),
 // translation scaled by scaleOut, stored as float.  TF is shared memory or global.
-__device__ void wexpm_update(SolveScratch &S, const double *x, float *TF, double scaleOut, int lane) {
+static __device__ void wexpm_update(SolveScratch &S, const double *x, float *TF, double scaleOut, int lane) {
     double A[16] = {0, -x[2], x[1], x[3], x[2], 0, -x[0], x[4], -x[1], x[0], 0, x[5], 0, 0, 0, 0};
     double maxEntry = 0;
     for (int i = 0; i < 16; i++) {
@@ -197,7 +197,7 @@ __device__ void wexpm_update(SolveScratch &S, const double *x, float *TF, double
 }
 
 // FP64 Cholesky + substitutions (same order as the oracle). Returns 0 / -1.
-__device__ int wcholesky(SolveScratch &S, int lane) {
+static __device__ int wcholesky(SolveScratch &S, int lane) {
     const double *A = S.A;
     double *L = S.L;
     if (lane < 36) {
@@ -244,7 +244,7 @@ __device__ int wcholesky(SolveScratch &S, int lane) {
 }
 
 // conjugateGradientKernel, warp.cu:926-975 (lane 0)
-__device__ void cg_solve(const double *A, const double *bb, double tol, int maxSteps, double *x) {
+static __device__ void cg_solve(const double *A, const double *bb, double tol, int maxSteps, double *x) {
     double r[6], dir[6];
     for (int i = 0; i < 6; i++) { x[i] = 0.0; r[i] = bb[i]; dir[i] = bb[i]; }
     int nSteps = 0;
@@ -273,7 +273,7 @@ __device__ void cg_solve(const double *A, const double *bb, double tol, int maxS
 }
 
 // Solve S.A x = S.b and apply the update to TF.  Returns the solve status.
-__device__ int wsolve_update(SolveScratch &S, int solver, float *TF, double scaleOut, int lane) {
+static __device__ int wsolve_update(SolveScratch &S, int solver, float *TF, double scaleOut, int lane) {
     if (lane == 0) S.status = 0;
     __syncwarp();
     int st = 0;

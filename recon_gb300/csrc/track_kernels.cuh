@@ -42,13 +42,16 @@ struct InstDesc {
     // photometric scratch
     float *ph_r, *ph_zw;
     double *ph_part;  // 27
-    int *ph_hist;     // 256
+    int *ph_hist;     // [0,256) accumulation, [256,512) copy for the trace, [512] median
+    unsigned int *ph_counter;
     // ICP scratch
     float *icp_res;          // W*H full-grid residual
     uint8_t *icp_mask;       // W*H
     int *icp_blkcnt;         // blocks of 1024 pixels
     int *icp_select;         // W*H
     float *icp_r2, *icp_w;   // W*H
+    float4 *icp_pk_pts;      // W*H: selected reference points in selection order (x y z mask)
+    float4 *icp_pk_nrm;      // W*H: their normals, .w = Student-t weight
     unsigned long long *icp_var;  // 4
     int *icp_nsel;           // kMaxLevels
     double *icp_part;        // chunks * 27

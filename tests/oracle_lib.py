@@ -104,6 +104,7 @@ def lib() -> ctypes.CDLL:
             L.orc_convert_gray.argtypes = [vp, i32, vp]
             L.orc_convert_depth.argtypes = [vp, i32, vp]
             L.orc_rgbd_float4_to_gray_z.argtypes = [vp, i32, i32, vp, vp, vp]
+            L.orc_fuse_keyframe.argtypes = [vp, i32, vp, vp, f32]
             L.orc_num_threads.restype = i32
             L.orc_set_threads.argtypes = [i32]
             _lib = L
@@ -111,6 +112,8 @@ def lib() -> ctypes.CDLL:
 
 
 def ptr(a: np.ndarray) -> ctypes.c_void_p:
+    """Address of a numpy array.  The caller must keep `a` referenced until the
+    call that uses the address returns (bind temporaries to a name first)."""
     assert a.flags["C_CONTIGUOUS"]
     return ctypes.c_void_p(a.ctypes.data)
 
@@ -173,6 +176,13 @@ class OracleTracker:
         if n < 0:
             raise RuntimeError("oracle track failed")
         return Tin.reshape(4, 4), list(trace)[:min(n, max_trace)]
+
+    def fuse_keyframe(self, depths, Ts, gate: float = 30.0):
+        ds = [np.ascontiguousarray(d, np.uint16) for d in depths]
+        T = np.ascontiguousarray(np.asarray(Ts, np.float32).reshape(len(ds), 16))
+        rc = self.L.orc_fuse_keyframe(self.h, len(ds), ptrs(ds), ptr(T), gate)
+        if rc != 0:
+            raise RuntimeError("oracle fuse failed")
 
     def get(self, name: str, level: int, shape, dtype) -> np.ndarray:
         out = np.zeros(shape, dtype=dtype)

@@ -205,3 +205,65 @@ def test_pose_accuracy_against_ground_truth():
     trk, orc, T, st, To, tro = run_pair(p, rg.BIOBJECTIVE)
     dt, dr = synth.pose_error(p.T_gt, T.astype(np.float64))
     assert dt < 1.0 and dr < 0.05, (dt, dr)
+
+
+def _trajectory_frames(W, H, n, seed):
+    from recon_gb300 import synth
+    cal = synth.make_calibration(W, H)
+    sc = synth.make_scene(seed)
+    poses = synth.smooth_trajectory(n, seed + 2, max_step_mm=10.0, max_step_deg=0.7)
+    g, d = [], []
+    for f in range(n):
+        gf, df = O.render_pair(sc, synth.camera_struct(cal, "L", poses[f]), synth.camera_struct(cal, "R", poses[f]),
+                               noise_rel=0.01, noise_seed=seed + 1, frame=f)
+        g.append(gf)
+        d.append(df)
+    return cal, poses, g, d
+
+
+def test_sequence_tracking_matches_oracle():
+    W, H = 320, 240
+    cal, poses, g, d = _trajectory_frames(W, H, 6, seed=71)
+    cfg = rg.make_config(W, H, 3, mode=rg.BIOBJECTIVE, iters=(2, 3, 4))
+    b = rg.Batch([cfg], [cal.calib])
+    b.set_reference([g[0]], [d[0]])
+    T, st = b.track_sequence([[g[f]] for f in range(1, 6)], [[d[f]] for f in range(1, 6)])
+    orc = O.OracleTracker(O.make_config(W, H, 3, mode=O.BIOBJECTIVE, iters=(2, 3, 4)), cal.calib)
+    orc.set_reference(g[0], d[0])
+    To = None
+    for f in range(1, 6):
+        orc.set_current(g[f], d[f])
+        To, _ = orc.track(To)
+        assert_bitexact(T[f - 1, 0], To, f"frame {f}")
+    # host inputs (copied on the second stream) give the same poses
+    b.set_reference([g[0]], [d[0]])
+    T2, _ = b.track_sequence([[g[f]] for f in range(1, 6)], [[d[f]] for f in range(1, 6)])
+    assert_bitexact(T2, T, "host vs device inputs")
+
+
+def test_keyframe_fusion_matches_oracle():
+    W, H = 320, 240
+    cal, poses, g, d = _trajectory_frames(W, H, 8, seed=81)
+    cfg = rg.make_config(W, H, 3, mode=rg.BIOBJECTIVE, iters=(2, 3, 4))
+    b = rg.Batch([cfg], [cal.calib])
+    b.set_reference([g[0]], [d[0]])
+    T, _ = b.track_sequence([[g[f]] for f in range(1, 6)], [[d[f]] for f in range(1, 6)])
+    b.fuse_keyframe([[d[f]] for f in range(1, 6)], T[:, :, :, :], gate_mm=30.0)
+    T6, _ = b.track_sequence([[g[6]], [g[7]]], [[d[6]], [d[7]]])
+    orc = O.OracleTracker(O.make_config(W, H, 3, mode=O.BIOBJECTIVE, iters=(2, 3, 4)), cal.calib)
+    orc.set_reference(g[0], d[0])
+    To, Ts = None, []
+    for f in range(1, 6):
+        orc.set_current(g[f], d[f])
+        To, _ = orc.track(To)
+        Ts.append(To.copy())
+    orc.fuse_keyframe([d[f] for f in range(1, 6)], np.stack(Ts), gate=30.0)
+    assert_bitexact(b.get_array(0, "ref_z", 0, np.float32, W * H), orc.get("ref_z", 0, W * H, np.float32),
+                    "fused keyframe depth")
+    P = 8192
+    assert_bitexact(b.get_array(0, "sel_idx", 0, np.int32, P), orc.get("sel_idx", 0, P, np.int32),
+                    "selection after fusion")
+    for f in (6, 7):
+        orc.set_current(g[f], d[f])
+        To, _ = orc.track(To)
+        assert_bitexact(T6[f - 6, 0], To, f"frame {f} after fusion")

@@ -58,7 +58,8 @@ def _reference_prep(fp):
     """Oracle and reference vertex records + selection for the reference frame."""
     W, H, L, calib = fp["W"], fp["H"], fp["L"], fp["cal"].calib
     z = np.zeros(W * H, np.float32)
-    O.lib().orc_convert_depth(p(fp["d0"].reshape(-1).copy()), W * H, p(z))
+    d0 = fp["d0"].reshape(-1).copy()
+    O.lib().orc_convert_depth(p(d0), W * H, p(z))
     xyz_o = np.zeros(4 * W * H, np.float32)
     xyz_r = np.zeros(4 * W * H, np.float32)
     O.lib().orc_zmap_to_xyz(p(z), W, H, p(calib), p(xyz_o))
@@ -138,7 +139,8 @@ def test_residual_weights_match_reference(frame_pair):
     rec = vd_o.reshape(-1, 24)[idx]
     sel_xyz = np.ascontiguousarray(rec[:, :3].T).reshape(-1)
     zc = np.zeros(W * H, np.float32)
-    O.lib().orc_convert_depth(p(fp["d1"].reshape(-1).copy()), W * H, p(zc))
+    d1 = fp["d1"].reshape(-1).copy()
+    O.lib().orc_convert_depth(p(d1), W * H, p(zc))
     cur = _pyr(fp["g1"], L)
     # a pose between identity and the truth: residuals of mixed sign, some out of view
     T = np.ascontiguousarray((0.5 * (np.eye(4) + fp["T"])).astype(np.float32)).reshape(-1)
@@ -168,8 +170,9 @@ def test_icp_stages_match_reference(frame_pair):
     lib, ref = O.lib(), R.lib()
     zr = np.zeros(W * H, np.float32)
     zc = np.zeros(W * H, np.float32)
-    lib.orc_convert_depth(p(fp["d0"].reshape(-1).copy()), W * H, p(zr))
-    lib.orc_convert_depth(p(fp["d1"].reshape(-1).copy()), W * H, p(zc))
+    d0, d1 = fp["d0"].reshape(-1).copy(), fp["d1"].reshape(-1).copy()
+    lib.orc_convert_depth(p(d0), W * H, p(zr))
+    lib.orc_convert_depth(p(d1), W * H, p(zc))
     ro6, rm_o = np.zeros(6 * W * H, np.float32), np.zeros(W * H, np.int32)
     rr6, rm_r = np.zeros(6 * W * H, np.float32), np.zeros(W * H, np.int32)
     lib.orc_zmap_to_xyz6(p(zr), W, H, p(calib), p(ro6), p(rm_o))
@@ -237,7 +240,8 @@ def test_cg_solver_matches_reference():
         b = rng.normal(size=6).astype(np.float32)
         xo = np.zeros(6)
         xr = np.zeros(6)
-        O.lib().orc_solve_cg(p(A.astype(np.float64)), p(b.astype(np.float64)), 1e-8, 6, p(xo))
+        A64, b64 = A.astype(np.float64), b.astype(np.float64)  # alive across the call
+        O.lib().orc_solve_cg(p(A64), p(b64), 1e-8, 6, p(xo))
         R.lib().ref_conjugateGradient(p(A), p(b), p(xr))
         assert np.array_equal(xo, xr)
 
@@ -250,7 +254,8 @@ def test_expm_update_matches_reference_expm():
         T0 = synth.se3(synth.rodrigues(rng.normal(size=3) * 0.1), rng.normal(size=3) * 50).astype(np.float32)
         To = np.ascontiguousarray(T0).reshape(-1).copy()
         Tr = To.copy()
-        O.lib().orc_expm_update(p(x.astype(np.float64)), p(To), 1000.0)
+        x64 = x.astype(np.float64)
+        O.lib().orc_expm_update(p(x64), p(To), 1000.0)
         R.lib().ref_expm(p(x), p(Tr), 1000.0)
         # Pade(6) in real vs complex (EXPOKIT) arithmetic: FP64 rounding only
         np.testing.assert_allclose(To, Tr, rtol=0, atol=2e-5 * np.maximum(1, np.abs(Tr)).max())
