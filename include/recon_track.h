@@ -176,6 +176,40 @@ int64_t recon_launch_count(void);         /* kernels launched by the library so 
 int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, int32_t level, void *host_dst,
                               int64_t nbytes);
 
+/* ---- allocation-free photometric iteration ----
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they track -- a real-time frame loop where a cudaMalloc could
+ * synchronise the device and stall the frame, or a host framework that owns
+ * all device memory and hands a plug-in only buffers it created -- this runs
+ * one photometric Gauss-Newton iteration (residuals and depth weights,
+ * histogram-MAD Tukey weights, 27-term normal equations, FP64 solve, SE(3)
+ * update of T_dev) without allocating anything.  Its scratch is a fixed
+ * device array inside the library, sized for RECON_NOALLOC_MAX_POINTS points
+ * (128 KB, held on every GPU that loads the library until the process exits);
+ * larger n_points is rejected with RECON_ERR_INVALID_ARG.  Every call shares
+ * that array, so calls that overlap on the GPU (other streams or host threads)
+ * race and must be serialised by the caller.  The first call on a device looks
+ * up the array's device address; make that first call before any stream
+ * capture.  All pointers in the view and T_dev are device memory; the result
+ * equals one iteration of recon_batch_track in PHOTOMETRIC mode. */
+#define RECON_NOALLOC_MAX_POINTS 16384
+typedef struct recon_photo_view {
+    int32_t n_points;                 /* selected points P, multiple of 1024, <= RECON_NOALLOC_MAX_POINTS */
+    int32_t level;                    /* pyramid level of img */
+    int32_t img_width, img_height;    /* size of img: (depth_width >> level) x (depth_height >> level) */
+    int32_t depth_width, depth_height; /* level-0 size of depth */
+    int32_t hist_bins;                /* MAD histogram bins (64 in the reference) */
+    int32_t solver;                   /* RECON_SOLVER_* */
+    float opt_scale_out;              /* 1e3 */
+    float calib[RECON_CALIB_SIZE];
+    const float *xyz;                 /* 3 x P keyframe points (x block, y block, z block) */
+    const float *intensity;           /* P keyframe intensities at `level` */
+    const float *jacobian;            /* 6 x P precomputed photometric Jacobian at `level` */
+    const float *img;                 /* current gray image at `level`, values in [0,1] */
+    const float *depth;               /* current level-0 depth, z = -mm (0 = invalid) */
+} recon_photo_view;
+int recon_photometric_iteration_noalloc(const recon_photo_view *view, float *T_dev, void *stream);
+
 /* ---- single tracker (PhotoTracker-style handle = batch of one) ---- */
 typedef recon_batch recon_tracker;
 int recon_tracker_create(const recon_config *cfg, const float *calib, void *stream, recon_tracker **out);

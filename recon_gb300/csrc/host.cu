@@ -71,6 +71,14 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // reported as a failure of this library's launches.
 void clear_stale_error() { (void)cudaGetLastError(); }
 
+}  // namespace
+
+namespace rt {
+// lets other translation units of the library report a message through recon_last_error
+void set_last_error(const char *msg) { g_last_error = msg; }
+}  // namespace rt
+
+namespace {
 
 struct Arena {
     size_t off = 0;

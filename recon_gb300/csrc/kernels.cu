@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "scene.h"
 #include "solve.cuh"
 #include "track_kernels.cuh"
@@ -1147,3 +1149,126 @@ __global__ void k_render_gray(recon_scene sc, recon_camera cam, uint8_t *out) {
 }
 
 }  // namespace rt
+
+// ====================================================================
+// Allocation-free photometric iteration.
+//
+// Some callers cannot allocate device memory while they track: a host that
+// runs the tracker inside a real-time frame loop, where a cudaMalloc can
+// synchronise the device and stall the frame, or a host framework that owns
+// all device memory through its own allocator and hands plug-ins only the
+// buffers it created.  For them this variant of the photometric GN iteration
+// keeps its scratch (per-point residuals and depth weights) in a file-scope
+// device array instead of per-instance buffers from cudaMalloc.
+//
+// The array is a static __device__ symbol: every GPU that loads the library
+// holds it until the process exits, and every call shares it and finds the
+// previous call's contents there.  Calls that overlap on the GPU (different
+// streams, or different host threads on the same device) race on it and must
+// be serialised by the caller.  Nothing in it has to start at zero: the
+// residual and weight slots for the call's points are written before they
+// are read, and the partial sums live in shared memory.
+// ====================================================================
+
+namespace rt {
+
+constexpr int kNoAllocMaxPoints = RECON_NOALLOC_MAX_POINTS;
+
+// residual[P], depth weight[P], then 27 FP64 normal-equation terms:
+// 128 KB + 256 B for the 16384-point maximum
+static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocMaxPoints + 64];
+
+__global__ void __launch_bounds__(256) k_photo_iter_noalloc(recon_photo_view v, float *scratch, float *T) {
+    __shared__ IterShared sh;
+    __shared__ InstDesc d;  // view of the caller's buffers in the layout photo_iteration reads
+    if (threadIdx.x == 0) {
+        d.W = v.depth_width;
+        d.H = v.depth_height;
+        d.P = v.n_points;
+        d.hist_bins = v.hist_bins;
+        for (int i = 0; i < RECON_CALIB_SIZE; i++) d.calib[i] = v.calib[i];
+        for (int l = 0; l < kMaxLevels; l++) {
+            d.cur_gray[l] = nullptr;
+            d.sel_I[l] = nullptr;
+            d.sel_J[l] = nullptr;
+        }
+        d.cur_gray[v.level] = const_cast<float *>(v.img);
+        d.sel_I[v.level] = const_cast<float *>(v.intensity);
+        d.sel_J[v.level] = const_cast<float *>(v.jacobian);
+        d.sel_xyz = const_cast<float *>(v.xyz);
+        d.cur_z = const_cast<float *>(v.depth);
+        d.ph_r = scratch;
+        d.ph_zw = scratch + kNoAllocMaxPoints;
+        d.ph_part = reinterpret_cast<double *>(scratch + 2 * kNoAllocMaxPoints);
+    }
+    if (threadIdx.x < 16) sh.T[threadIdx.x] = T[threadIdx.x];
+    __syncthreads();
+    photo_iteration(d, sh, v.level);
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    int lane = threadIdx.x;
+    SolveScratch &S = sh.S;
+    if (lane == 0) unpack27(sh.A_ph, S.A, S.b);
+    __syncwarp();
+    wsolve_update(S, v.solver, sh.T, (double)v.opt_scale_out, lane);
+    if (lane < 16) T[lane] = sh.T[lane];
+}
+
+}  // namespace rt
+
+namespace rt {
+void set_last_error(const char *msg);
+}
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+
+int noalloc_reject(const char *msg) {
+    rt::set_last_error(msg);
+    return RECON_ERR_INVALID_ARG;
+}
+}  // namespace
+
+extern "C" int recon_photometric_iteration_noalloc(const recon_photo_view *v, float *T_dev, void *stream) {
+    if (!v || !T_dev || !v->xyz || !v->intensity || !v->jacobian || !v->img || !v->depth)
+        return noalloc_reject("recon_photometric_iteration_noalloc: null pointer");
+    if (v->n_points <= 0 || v->n_points % rt::kChunk)
+        return noalloc_reject("recon_photometric_iteration_noalloc: n_points must be a positive multiple of 1024");
+    if (v->n_points > rt::kNoAllocMaxPoints)
+        return noalloc_reject("recon_photometric_iteration_noalloc: n_points exceeds RECON_NOALLOC_MAX_POINTS "
+                              "(16384), the size of the built-in scratch array");
+    if (v->level < 0 || v->level >= rt::kMaxLevels || v->hist_bins < 2 || v->hist_bins > 256)
+        return noalloc_reject("recon_photometric_iteration_noalloc: level must be 0..3 and hist_bins 2..256");
+    if (v->img_width < 2 || v->img_height < 2 || v->img_width != (v->depth_width >> v->level) ||
+        v->img_height != (v->depth_height >> v->level))
+        return noalloc_reject("recon_photometric_iteration_noalloc: img must be the depth size >> level");
+    if (v->solver < 0 || v->solver > 1) return noalloc_reject("recon_photometric_iteration_noalloc: bad solver");
+    (void)cudaGetLastError();
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        rt::set_last_error("recon_photometric_iteration_noalloc: no current CUDA device");
+        return RECON_ERR_CUDA;
+    }
+    void *ptr = nullptr;
+    {
+        // set-up, once per device with that device current: the host-side name
+        // of a __device__ array is not a device address, so look it up
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            cudaError_t e = cudaGetSymbolAddress(&g_noalloc_ptr[dev], rt::g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_ptr[dev] = nullptr;
+                rt::set_last_error("recon_photometric_iteration_noalloc: cudaGetSymbolAddress failed");
+                return RECON_ERR_CUDA;
+            }
+        }
+        ptr = g_noalloc_ptr[dev];
+    }
+    rt::k_photo_iter_noalloc<<<1, rt::kLanes, 0, (cudaStream_t)stream>>>(*v, (float *)ptr, T_dev);
+    if (cudaGetLastError() != cudaSuccess) {
+        rt::set_last_error("recon_photometric_iteration_noalloc: kernel launch failed");
+        return RECON_ERR_CUDA;
+    }
+    return RECON_OK;
+}
