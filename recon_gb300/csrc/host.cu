@@ -119,6 +119,8 @@ struct recon_batch {
     // optional per-launch CUDA-event timing (kinds: see TimingKind)
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> graph_events, direct_events;
+    std::vector<cudaEvent_t> event_pool;  // reused by timed direct launches
+    size_t pool_next = 0;
     double t_ms[8] = {0};
     long long t_cnt[8] = {0};
     // sequence tracking: pointer tables, pose history, host-input double buffer
@@ -298,9 +300,22 @@ struct TimedScope {
         // inside a capture an event record must be external to become a graph node
         flags = in_graph ? cudaEventRecordExternal : cudaEventRecordDefault;
         if (!b->timing) return;
-        cudaEventCreate(&e1);
-        cudaEventCreate(&e2);
+        if (in_graph) {
+            cudaEventCreate(&e1);
+            cudaEventCreate(&e2);
+        } else {
+            e1 = take();
+            e2 = take();
+        }
         cudaEventRecordWithFlags(e1, s, flags);
+    }
+    cudaEvent_t take() {
+        if (b->pool_next == b->event_pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            b->event_pool.push_back(e);
+        }
+        return b->event_pool[b->pool_next++];
     }
     ~TimedScope() {
         if (!b->timing) return;
@@ -309,20 +324,20 @@ struct TimedScope {
     }
 };
 
+// pooled: the direct-launch events return to the pool instead of being destroyed
 void collect_events(recon_batch *b, std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> &list,
-                    bool destroy) {
+                    bool pooled) {
     for (auto &ev : list) {
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, ev.second.first, ev.second.second) == cudaSuccess) {
             b->t_ms[ev.first] += ms;
             b->t_cnt[ev.first] += 1;
         }
-        if (destroy) {
-            cudaEventDestroy(ev.second.first);
-            cudaEventDestroy(ev.second.second);
-        }
     }
-    if (destroy) list.clear();
+    if (pooled) {
+        list.clear();
+        b->pool_next = 0;
+    }
 }
 
 // reference preparation; from_inputs: convert the staged images (else rebuild
@@ -405,7 +420,7 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
         int nph = b->max_P / kChunk;
         for (int it = 0; it < maxit; it++) {
             TimedScope ts(b, s, TK_ITER, in_graph);
-            k_iter<<<dim3(nph + (any_icp ? nchunk : 0), n), kLanes, 0, s>>>(D, level, it, nph);
+            k_iter<<<dim3(nph + (any_icp ? nchunk : 0), n), 512, 0, s>>>(D, level, it, nph);
             b->graph_kernels++;
         }
     }
@@ -667,10 +682,7 @@ int recon_batch_destroy(recon_batch *b) {
         cudaEventDestroy(ev.second.first);
         cudaEventDestroy(ev.second.second);
     }
-    for (auto &ev : b->direct_events) {
-        cudaEventDestroy(ev.second.first);
-        cudaEventDestroy(ev.second.second);
-    }
+    for (cudaEvent_t e : b->event_pool) cudaEventDestroy(e);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RECON_OK;

@@ -674,8 +674,12 @@ __global__ void k_icp_student(const InstDesc *D, int level, int pass) {
 // one Gauss-Newton iteration for every instance
 // ------------------------------------------------------------------
 
+constexpr int kIterThreads = 512;  // k_iter block: 2 points per thread in the gather phase
+
 struct IterShared {
     float T[16];
+    float pts[7][kChunk];  // one chunk's per-point values: r (or r*w) and the 6 Jacobian columns
+    float wpf[8][28];      // FP32 warp totals of one chunk
     double wpart[8][27];
     double tot[27];
     double A_ph[27], A_icp[27];
@@ -711,6 +715,66 @@ __device__ __forceinline__ void chunk_fold(IterShared &sh, float *s) {
         int q = threadIdx.x;
         double c = 0.0;
         for (int w = 0; w < 8; w++) c = c + sh.wpart[w][q];
+        sh.tot[q] = sh.tot[q] + c;
+    }
+    __syncthreads();
+}
+
+// Canonical terms [LO, HI) of one point (the loops unroll, so q is a
+// compile-time constant and only HI-LO accumulators are live).
+template <int LO, int HI>
+__device__ __forceinline__ void acc_terms(float *s, const float *j, float r) {
+    int q = 0;
+#pragma unroll
+    for (int a = 0; a < 6; a++)
+#pragma unroll
+        for (int c = a; c < 6; c++) {
+            if (q >= LO && q < HI) s[q - LO] += j[a] * j[c];
+            q++;
+        }
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+        if (q >= LO && q < HI) s[q - LO] += j[c] * r;
+        q++;
+    }
+}
+
+template <int LO, int HI>
+__device__ __forceinline__ void lane_terms(IterShared &sh, int t) {
+    float s[HI - LO];
+#pragma unroll
+    for (int q = 0; q < HI - LO; q++) s[q] = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        int k = t + kLanes * m;
+        float j[6];
+#pragma unroll
+        for (int c = 0; c < 6; c++) j[c] = sh.pts[1 + c][k];
+        acc_terms<LO, HI>(s, j, sh.pts[0][k]);
+    }
+    int lane = threadIdx.x & 31, w8 = (threadIdx.x >> 5) & 7;
+#pragma unroll
+    for (int q = 0; q < HI - LO; q++) {
+        float v = s[q];
+        for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh.wpf[w8][LO + q] = v;
+    }
+}
+
+// The canonical reduction of the chunk held in sh.pts by a 512-thread CTA:
+// threads 0-255 are lanes 0-255 for terms 0-13, threads 256-511 the same lanes
+// for terms 14-26 (each term's lane sum, butterfly and warp order are those of
+// the canonical order); the 8 FP32 warp values of each term are converted to
+// FP64 by one thread and summed in warp order into sh.tot.
+__device__ __forceinline__ void accumulate_chunk(IterShared &sh) {
+    int t = threadIdx.x & (kLanes - 1);
+    if (threadIdx.x < kLanes) lane_terms<0, 14>(sh, t);
+    else lane_terms<14, 27>(sh, t);
+    __syncthreads();
+    if (threadIdx.x < 27) {
+        int q = threadIdx.x;
+        double c = 0.0;
+        for (int w = 0; w < 8; w++) c = c + (double)sh.wpf[w][q];
         sh.tot[q] = sh.tot[q] + c;
     }
     __syncthreads();
@@ -845,20 +909,21 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     }
 }
 
+// One ICP chunk (1024 correspondences) with a 512-thread CTA: each thread
+// evaluates two points into shared memory, then the chunk is reduced.
 __device__ void icp_chunk(const InstDesc &d, IterShared &sh, int level, int chunk, int nsel) {
     for (int q = threadIdx.x; q < 27; q += blockDim.x) sh.tot[q] = 0.0;
-    __syncthreads();
-    float acc[27];
 #pragma unroll
-    for (int q = 0; q < 27; q++) acc[q] = 0.0f;
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-        int idx = chunk * kChunk + threadIdx.x + kLanes * m;
+    for (int m = 0; m < 2; m++) {
+        int k = threadIdx.x + kIterThreads * m;
         float j[6], r;
-        icp_point(d, sh.T, level, idx, nsel, j, r);
-        acc27(acc, j, r);
+        icp_point(d, sh.T, level, chunk * kChunk + k, nsel, j, r);
+        sh.pts[0][k] = r;
+#pragma unroll
+        for (int c = 0; c < 6; c++) sh.pts[1 + c][k] = j[c];
     }
-    chunk_fold(sh, acc);
+    __syncthreads();
+    accumulate_chunk(sh);
     if (threadIdx.x < 27) d.icp_part[(size_t)chunk * 27 + threadIdx.x] = sh.tot[threadIdx.x];
 }
 
@@ -958,8 +1023,8 @@ __device__ void photo_pass_a(const InstDesc &d, IterShared &sh, int level, int c
     for (int k = threadIdx.x; k < nb; k += blockDim.x) sh.hist[k] = 0;
     __syncthreads();
 #pragma unroll
-    for (int m = 0; m < 4; m++) {
-        int i = c * kChunk + threadIdx.x + kLanes * m;
+    for (int m = 0; m < kChunk / kIterThreads; m++) {
+        int i = c * kChunk + threadIdx.x + kIterThreads * m;
         float r, zw;
         photo_residual(d.calib, sh.T, a, b, __ldg(d.sel_xyz + i), __ldg(d.sel_xyz + P + i),
                        __ldg(d.sel_xyz + 2 * P + i), __ldg(I + i), img, w, h, d.cur_z, d.W, d.H, r, zw);
@@ -1026,22 +1091,19 @@ __device__ void photo_pass_b(const InstDesc &d, IterShared &sh, int level) {
     }
     float s = mad_scale(sh.median, nb);
     const float *J = d.sel_J[level];
-    int t = threadIdx.x;
     for (int c = 0; c < P / kChunk; c++) {
-        float acc[27];
 #pragma unroll
-        for (int q = 0; q < 27; q++) acc[q] = 0.0f;
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-            int i = c * kChunk + t + kLanes * m;
+        for (int m = 0; m < kChunk / kIterThreads; m++) {
+            int k = threadIdx.x + kIterThreads * m;
+            int i = c * kChunk + k;
             float r = __ldcg(d.ph_r + i);
             float wv = tukey_weight(r, __ldcg(d.ph_zw + i), s);
-            float jw[6];
+            sh.pts[0][k] = r * wv;
 #pragma unroll
-            for (int k = 0; k < 6; k++) jw[k] = __ldg(J + k * P + i) * wv;
-            acc27(acc, jw, r * wv);
+            for (int q = 0; q < 6; q++) sh.pts[1 + q][k] = __ldg(J + q * P + i) * wv;
         }
-        chunk_fold(sh, acc);
+        __syncthreads();
+        accumulate_chunk(sh);
     }
     if (threadIdx.x < 27) {
         sh.A_ph[threadIdx.x] = sh.tot[threadIdx.x];
@@ -1058,7 +1120,7 @@ __device__ void photo_pass_b(const InstDesc &d, IterShared &sh, int level) {
 // shapetracker.cpp:392-394), solves and applies the SE(3) update
 // (estimateIncrement, phototracker.cpp:646-664).  No CTA waits for another:
 // completion is counted with atomic tickets.
-__global__ void __launch_bounds__(256, 3) k_iter(const InstDesc *D, int level, int it, int nph_grid) {
+__global__ void __launch_bounds__(kIterThreads, 2) k_iter(const InstDesc *D, int level, int it, int nph_grid) {
     INST_DESC;
     if (level >= d.L) return;
     if (it >= d.iters[d.L - 1 - level]) return;
