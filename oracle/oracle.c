@@ -6,8 +6,10 @@
  * cites the file:line it follows.  FP32 expressions are written in the
  * reference's source order; the library is compiled with -ffp-contract=off so
  * that no multiply-add is fused.  Reductions follow the canonical chunked tree
- * described at orc_reduce27 (the reference's own order is available as
- * orc_reduce27_refordered for comparison).
+ * described at orc_reduce27; the tracker folds its FP32 warp values exactly in
+ * fixed point (orc_reduce27_fx), the reference-named shim in FP64 order
+ * (orc_reduce27).  The reference's own order is available as
+ * orc_reduce27_refordered for comparison.
  */
 #define _POSIX_C_SOURCE 200809L
 #include "oracle.h"
@@ -583,40 +585,37 @@ int orc_generate_weights(const float *r, const float *zw, int N, int nbins, int3
  * FP64 and summed in warp order; chunk values are summed in chunk order in FP64.
  * Term order: the 21 upper-triangle JtJ terms (j <= i, row-major over j), then
  * the 6 Jtr terms. */
-void orc_reduce27(const float *const *J6, const float *r, int N, double A[36], double b[6]) {
-    int nchunks = N / ORC_CHUNK;
-    double tot[27];
-    for (int q = 0; q < 27; q++) tot[q] = 0.0;
-    for (int k = 0; k < nchunks; k++) {
-        double chunk[27];
-        for (int q = 0; q < 27; q++) chunk[q] = 0.0;
-        for (int wi = 0; wi < 8; wi++) {
-            float lane[32][27];
-            for (int l = 0; l < 32; l++) {
-                int t = wi * 32 + l;
-                float s[27];
-                for (int q = 0; q < 27; q++) s[q] = 0.0f;
-                for (int m = 0; m < 4; m++) {
-                    int i = k * ORC_CHUNK + t + 256 * m;
-                    float jv[6];
-                    for (int c = 0; c < 6; c++) jv[c] = J6[c][i];
-                    int q = 0;
-                    for (int j = 0; j < 6; j++)
-                        for (int ii = j; ii < 6; ii++) s[q++] += jv[j] * jv[ii];
-                    for (int c = 0; c < 6; c++) s[q++] += jv[c] * r[i];
-                }
-                for (int q = 0; q < 27; q++) lane[l][q] = s[q];
+/* The FP32 stage of the canonical order for chunk k: wv[w][q] is the value
+ * warp w (lanes 32w..32w+31) holds for term q after its xor butterfly. */
+static void chunk_warp_values(const float *const *J6, const float *r, int k, float wv[8][27]) {
+    for (int wi = 0; wi < 8; wi++) {
+        float lane[32][27];
+        for (int l = 0; l < 32; l++) {
+            int t = wi * 32 + l;
+            float s[27];
+            for (int q = 0; q < 27; q++) s[q] = 0.0f;
+            for (int m = 0; m < 4; m++) {
+                int i = k * ORC_CHUNK + t + 256 * m;
+                float jv[6];
+                for (int c = 0; c < 6; c++) jv[c] = J6[c][i];
+                int q = 0;
+                for (int j = 0; j < 6; j++)
+                    for (int ii = j; ii < 6; ii++) s[q++] += jv[j] * jv[ii];
+                for (int c = 0; c < 6; c++) s[q++] += jv[c] * r[i];
             }
-            for (int off = 16; off >= 1; off >>= 1) {
-                float nl[32][27];
-                for (int l = 0; l < 32; l++)
-                    for (int q = 0; q < 27; q++) nl[l][q] = lane[l][q] + lane[l ^ off][q];
-                memcpy(lane, nl, sizeof(nl));
-            }
-            for (int q = 0; q < 27; q++) chunk[q] = chunk[q] + (double)lane[0][q];
+            for (int q = 0; q < 27; q++) lane[l][q] = s[q];
         }
-        for (int q = 0; q < 27; q++) tot[q] = tot[q] + chunk[q];
+        for (int off = 16; off >= 1; off >>= 1) {
+            float nl[32][27];
+            for (int l = 0; l < 32; l++)
+                for (int q = 0; q < 27; q++) nl[l][q] = lane[l][q] + lane[l ^ off][q];
+            memcpy(lane, nl, sizeof(nl));
+        }
+        for (int q = 0; q < 27; q++) wv[wi][q] = lane[0][q];
     }
+}
+
+static void unpack27(const double *tot, double A[36], double b[6]) {
     int q = 0;
     for (int j = 0; j < 6; j++)
         for (int i = j; i < 6; i++) {
@@ -625,6 +624,102 @@ void orc_reduce27(const float *const *J6, const float *r, int N, double A[36], d
             q++;
         }
     for (int c = 0; c < 6; c++) b[c] = tot[q++];
+}
+
+void orc_reduce27(const float *const *J6, const float *r, int N, double A[36], double b[6]) {
+    int nchunks = N / ORC_CHUNK;
+    double tot[27];
+    for (int q = 0; q < 27; q++) tot[q] = 0.0;
+    for (int k = 0; k < nchunks; k++) {
+        float wv[8][27];
+        chunk_warp_values(J6, r, k, wv);
+        double chunk[27];
+        for (int q = 0; q < 27; q++) chunk[q] = 0.0;
+        for (int wi = 0; wi < 8; wi++)
+            for (int q = 0; q < 27; q++) chunk[q] = chunk[q] + (double)wv[wi][q];
+        for (int q = 0; q < 27; q++) tot[q] = tot[q] + chunk[q];
+    }
+    unpack27(tot, A, b);
+}
+
+/* Fixed-point accumulation.  The 27 terms of the tracker's normal equations are
+ * the exact sum of every FP32 warp value of the canonical order above (lanes
+ * and butterflies as in orc_reduce27), each truncated toward zero at 2^-64,
+ * rounded once to FP64 (round to nearest even).  The sum does not depend on
+ * the order in which chunks and warps are added, which lets the GPU add them
+ * with integer atomics from any CTA in any order. */
+void orc_fx_add(long long L[ORC_FX_LIMBS], float v, int *bad) {
+    uint32_t bits;
+    memcpy(&bits, &v, 4);
+    uint32_t E = (bits >> 23) & 0xffu, M = bits & 0x7fffffu;
+    if (E == 0xffu) { *bad = 1; return; }            /* Inf / NaN */
+    uint64_t m;
+    int e;
+    if (E == 0) { m = M; e = -149; } else { m = M | 0x800000u; e = (int)E - 150; }
+    if (m == 0) return;
+    if (e >= 25) { *bad = 1; return; }               /* |v| >= 2^48 */
+    int s = e + 64;                                  /* bit of m's lsb in units of 2^-64 */
+    if (s < 0) {
+        m = (-s >= 24) ? 0 : (m >> -s);
+        s = 0;
+    }
+    if (m == 0) return;
+    int k0 = s >> 5;
+    uint64_t t = m << (s & 31);
+    long long lo = (long long)(t & 0xffffffffu), hi = (long long)(t >> 32);
+    if (bits >> 31) { lo = -lo; hi = -hi; }
+    L[k0] += lo;
+    if (hi) L[k0 + 1] += hi;
+}
+
+double orc_fx_to_double(const long long L[ORC_FX_LIMBS]) {
+    /* Q = sum_k L[k] 2^(32k) in two's complement 128-bit arithmetic */
+    unsigned __int128 Q = 0;
+    for (int k = ORC_FX_LIMBS - 1; k >= 0; k--) Q = (Q << 32) + (unsigned __int128)(__int128)L[k];
+    int neg = (int)(Q >> 127);
+    unsigned __int128 U = neg ? (unsigned __int128)0 - Q : Q;
+    if (U == 0) return 0.0;
+    uint64_t hi = (uint64_t)(U >> 64), lo = (uint64_t)U;
+    int n = hi ? 127 - __builtin_clzll(hi) : 63 - __builtin_clzll(lo); /* top bit */
+    uint64_t mant;
+    int e2; /* value = mant * 2^e2 */
+    if (n <= 52) {
+        mant = (uint64_t)U << (52 - n);
+        e2 = -64 - (52 - n);
+    } else {
+        int sh = n - 52;
+        mant = (uint64_t)(U >> sh);
+        unsigned __int128 rem = U - ((unsigned __int128)mant << sh);
+        unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1))) mant++;
+        if (mant >> 53) { mant >>= 1; sh++; }
+        e2 = sh - 64;
+    }
+    /* mant in [2^52, 2^53): biased exponent of mant * 2^e2 */
+    uint64_t out = ((uint64_t)(e2 + 52 + 1023) << 52) | (mant & ((1ull << 52) - 1));
+    if (neg) out |= 1ull << 63;
+    double d;
+    memcpy(&d, &out, 8);
+    return d;
+}
+
+void orc_fx27_clear(orc_fx27 *acc) { memset(acc, 0, sizeof(*acc)); }
+
+void orc_reduce27_fx(const float *const *J6, const float *r, int N, orc_fx27 *acc) {
+    int nchunks = N / ORC_CHUNK;
+    for (int k = 0; k < nchunks; k++) {
+        float wv[8][27];
+        chunk_warp_values(J6, r, k, wv);
+        for (int wi = 0; wi < 8; wi++)
+            for (int q = 0; q < 27; q++) orc_fx_add(acc->L[q], wv[wi][q], &acc->bad);
+    }
+}
+
+/* The 27 accumulated terms as the system (A, b); all NaN if any input was out of range. */
+void orc_fx27_value(const orc_fx27 *acc, double A[36], double b[6]) {
+    double tot[27];
+    for (int q = 0; q < 27; q++) tot[q] = acc->bad ? NAN : orc_fx_to_double(acc->L[q]);
+    unpack27(tot, A, b);
 }
 
 /* The reference's own order: reduceProduct6<float,256> (reduction_kernel.cu:262-317)
@@ -900,39 +995,42 @@ void orc_icp_residual_jacobian(const float *ref6, const int32_t *select, int nse
 /* 6x6 solve and SE(3) exponential                                     */
 /* ------------------------------------------------------------------ */
 
-/* FP64 Cholesky A = L L^T with forward/back substitution.  The reference's
- * Cholesky kernel (warp.cu:978-1007) is compiled but not launched; the CPU
- * alternative is cv::solve(DECOMP_CHOLESKY) (phototracker.cpp:649-660).
- * Returns 0 on success, -1 when a pivot is not positive (x set to 0). */
+/* FP64 Cholesky in its square-root-free form A = L D L^T (unit lower L), with
+ * reciprocal pivots.  The reference's Cholesky kernel (warp.cu:978-1007) is
+ * compiled but not launched; the CPU alternative is cv::solve(DECOMP_CHOLESKY)
+ * (phototracker.cpp:649-660).  The operation order below is the GPU's: row i
+ * of column j is s = A_ij - sum_{k<j} L_ik U_jk (k ascending) with U_jk the
+ * unscaled value s of row j at column k; D_j = s_jj, L_ij = s_ij * (1 / D_j);
+ * the substitutions run column by column.  Returns 0 on success, -1 when a
+ * pivot is not positive (x set to 0). */
 int orc_solve_cholesky(const double A[36], const double b[6], double x[6]) {
-    double L[36];
-    for (int i = 0; i < 36; i++) L[i] = 0.0;
+    double L[36], U[36], inv[6];
+    for (int i = 0; i < 36; i++) { L[i] = 0.0; U[i] = 0.0; }
     for (int j = 0; j < 6; j++) {
-        double d = A[j * 6 + j];
-        for (int k = 0; k < j; k++) d = d - L[j * 6 + k] * L[j * 6 + k];
-        if (!(d > 0.0)) {
+        double sv[6];
+        for (int i = j; i < 6; i++) {
+            double v = A[i * 6 + j];
+            for (int k = 0; k < j; k++) v = v - L[i * 6 + k] * U[j * 6 + k];
+            sv[i] = v;
+        }
+        if (!(sv[j] > 0.0)) {
             for (int i = 0; i < 6; i++) x[i] = 0.0;
             return -1;
         }
-        double ljj = sqrt(d);
-        L[j * 6 + j] = ljj;
+        inv[j] = 1.0 / sv[j];
         for (int i = j + 1; i < 6; i++) {
-            double s = A[i * 6 + j];
-            for (int k = 0; k < j; k++) s = s - L[i * 6 + k] * L[j * 6 + k];
-            L[i * 6 + j] = s / ljj;
+            U[i * 6 + j] = sv[i];
+            L[i * 6 + j] = sv[i] * inv[j];
         }
     }
-    double y[6];
-    for (int i = 0; i < 6; i++) {
-        double s = b[i];
-        for (int k = 0; k < i; k++) s = s - L[i * 6 + k] * y[k];
-        y[i] = s / L[i * 6 + i];
-    }
-    for (int i = 5; i >= 0; i--) {
-        double s = y[i];
-        for (int k = i + 1; k < 6; k++) s = s - L[k * 6 + i] * x[k];
-        x[i] = s / L[i * 6 + i];
-    }
+    double z[6];
+    for (int i = 0; i < 6; i++) z[i] = b[i];
+    for (int k = 0; k < 6; k++)
+        for (int i = k + 1; i < 6; i++) z[i] = z[i] - L[i * 6 + k] * z[k];
+    for (int i = 0; i < 6; i++) z[i] = z[i] * inv[i];
+    for (int k = 5; k >= 0; k--)
+        for (int i = 0; i < k; i++) z[i] = z[i] - L[k * 6 + i] * z[k];
+    for (int i = 0; i < 6; i++) x[i] = z[i];
     return 0;
 }
 
@@ -979,21 +1077,27 @@ static void mat4d(const double *M1, const double *M2, double *R) {
     memcpy(R, t, sizeof(t));
 }
 
-/* normalizeMat4RealSafe, expmCuda.cu:1955-1980 (lengths through single-precision sqrtf) */
+/* normalizeMat4RealSafe, expmCuda.cu:1955-1980: lengths through single-precision
+ * sqrtf, the length of the old first column used for the new one, and the
+ * divisions written as products with the FP64 reciprocal of each length. */
 static void normalize_mat4_safe(double *T) {
     double u[3] = {T[0], T[4], T[8]};
     double v[3] = {T[1], T[5], T[9]};
     double w[3] = {T[2], T[6], T[10]};
     double lenU = (double)sqrtf((float)(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
     double lenW = (double)sqrtf((float)(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]));
-    if (lenW > 1e-8f) { w[0] /= lenW; w[1] /= lenW; w[2] /= lenW; }
-    else { w[0] = 0; w[1] = 0; w[2] = 1; }
+    if (lenW > 1e-8f) {
+        double iw = 1.0 / lenW;
+        w[0] = w[0] * iw; w[1] = w[1] * iw; w[2] = w[2] * iw;
+    } else { w[0] = 0; w[1] = 0; w[2] = 1; }
     /* crossproductReal(v, w, u), expmCuda.cu:1934-1938 */
     u[0] = v[1] * w[2] - v[2] * w[1];
     u[1] = -(v[0] * w[2] - v[2] * w[0]);
     u[2] = v[0] * w[1] - v[1] * w[0];
-    if (lenU > 1e-8f) { u[0] /= lenU; u[1] /= lenU; u[2] /= lenU; }
-    else { u[0] = 1; u[1] = 0; u[2] = 0; }
+    if (lenU > 1e-8f) {
+        double iu = 1.0 / lenU;
+        u[0] = u[0] * iu; u[1] = u[1] * iu; u[2] = u[2] * iu;
+    } else { u[0] = 1; u[1] = 0; u[2] = 0; }
     v[0] = w[1] * u[2] - w[2] * u[1];
     v[1] = -(w[0] * u[2] - w[2] * u[0]);
     v[2] = w[0] * u[1] - w[1] * u[0];
@@ -1015,13 +1119,17 @@ static int expm_squarings(double hnorm) {
     return ns < 0 ? 0 : ns;
 }
 
-/* 4x4 LU solve with partial pivoting: X = D^{-1} N.  Returns -1 if singular. */
+/* X = D^{-1} N for the Pade denominator and numerator of a twist.  Their last
+ * rows are exactly (0 0 0 1) (a twist's last row is zero), so the elimination
+ * with partial pivoting runs over rows 0..2 (pivot: first row of largest
+ * |D_ik|), with reciprocal pivots; back substitution is column-oriented from
+ * row 3 up.  Returns -1 if a pivot is zero. */
 static int solve4(double *D, double *N) {
-    int piv[4] = {0, 1, 2, 3};
-    for (int k = 0; k < 4; k++) {
+    double inv[3];
+    for (int k = 0; k < 3; k++) {
         int p = k;
         double best = fabs(D[k * 4 + k]);
-        for (int i = k + 1; i < 4; i++) {
+        for (int i = k + 1; i < 3; i++) {
             double v = fabs(D[i * 4 + k]);
             if (v > best) { best = v; p = i; }
         }
@@ -1031,26 +1139,28 @@ static int solve4(double *D, double *N) {
                 double t = D[k * 4 + c]; D[k * 4 + c] = D[p * 4 + c]; D[p * 4 + c] = t;
                 t = N[k * 4 + c]; N[k * 4 + c] = N[p * 4 + c]; N[p * 4 + c] = t;
             }
-            int t = piv[k]; piv[k] = piv[p]; piv[p] = t;
         }
-        for (int i = k + 1; i < 4; i++) {
-            double f = D[i * 4 + k] / D[k * 4 + k];
-            for (int c = k; c < 4; c++) D[i * 4 + c] = D[i * 4 + c] - f * D[k * 4 + c];
+        inv[k] = 1.0 / D[k * 4 + k];
+        for (int i = k + 1; i < 3; i++) {
+            double f = D[i * 4 + k] * inv[k];
+            for (int c = k + 1; c < 4; c++) D[i * 4 + c] = D[i * 4 + c] - f * D[k * 4 + c];
             for (int c = 0; c < 4; c++) N[i * 4 + c] = N[i * 4 + c] - f * N[k * 4 + c];
         }
     }
-    for (int c = 0; c < 4; c++)
-        for (int i = 3; i >= 0; i--) {
-            double s = N[i * 4 + c];
-            for (int k = i + 1; k < 4; k++) s = s - D[i * 4 + k] * N[k * 4 + c];
-            N[i * 4 + c] = s / D[i * 4 + i];
+    for (int k = 3; k >= 1; k--) {
+        for (int c = 0; c < 4; c++) {
+            double xk = N[k * 4 + c];
+            for (int i = 0; i < k; i++) N[i * 4 + c] = N[i * 4 + c] - D[i * 4 + k] * xk;
         }
+        for (int c = 0; c < 4; c++) N[(k - 1) * 4 + c] = N[(k - 1) * 4 + c] * inv[k - 1];
+    }
     return 0;
 }
 
 /* exp(A) of a 4x4 twist by the diagonal (6,6) Pade approximant with scaling and
  * squaring (the method of EXPOKIT's zgpadm, Sidje 1998, used by the reference at
- * expmCuda.cu:1642 / expm.c:1669), in real FP64 arithmetic. */
+ * expmCuda.cu:1642 / expm.c:1669), in real FP64 arithmetic.  U0 and V are
+ * evaluated by the one formula ((a I + b X2) + c X4) + d X6 (d = 0 for U0). */
 void orc_expm_twist(const double A[16], double E[16]) {
     double hnorm = 0.0;
     for (int r = 0; r < 4; r++) {
@@ -1072,8 +1182,8 @@ void orc_expm_twist(const double A[16], double E[16]) {
     double U0[16], U[16], V[16];
     for (int i = 0; i < 16; i++) {
         double I = (i % 5 == 0) ? 1.0 : 0.0;
-        U0[i] = c[1] * I + c[3] * X2[i] + c[5] * X4[i];
-        V[i] = c[0] * I + c[2] * X2[i] + c[4] * X4[i] + c[6] * X6[i];
+        U0[i] = ((c[1] * I + c[3] * X2[i]) + c[5] * X4[i]) + 0.0 * X6[i];
+        V[i] = ((c[0] * I + c[2] * X2[i]) + c[4] * X4[i]) + c[6] * X6[i];
     }
     mat4d(X, U0, U);
     double Nm[16], Dm[16];
@@ -1415,7 +1525,10 @@ int orc_track(orc_tracker *t, float *Tio, orc_iter_trace *trace, int max_trace) 
                     for (int i = 0; i < P; i++) t->Jw[c][i] = t->sel_J[layer][c * P + i] * t->w[i];
                 const float *J6[6];
                 for (int c = 0; c < 6; c++) J6[c] = t->Jw[c];
-                orc_reduce27(J6, t->rw, P, A_ph, b_ph);
+                orc_fx27 acc;
+                orc_fx27_clear(&acc);
+                orc_reduce27_fx(J6, t->rw, P, &acc);
+                orc_fx27_value(&acc, A_ph, b_ph);
             }
             if (mode == ORC_GEOMETRIC || mode == ORC_BIOBJECTIVE) {
                 if (j == 0) {
@@ -1441,7 +1554,10 @@ int orc_track(orc_tracker *t, float *Tio, orc_iter_trace *trace, int max_trace) 
                                               t->cfg.opt_scale_in);
                     const float *J6[6];
                     for (int c = 0; c < 6; c++) J6[c] = t->icp_J + (size_t)c * np;
-                    orc_reduce27(J6, t->icp_res, np, A_icp, b_icp);
+                    orc_fx27 acc;
+                    orc_fx27_clear(&acc);
+                    orc_reduce27_fx(J6, t->icp_res, np, &acc);
+                    orc_fx27_value(&acc, A_icp, b_icp);
                 }
             }
             double A[36], b[6];

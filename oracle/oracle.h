@@ -97,6 +97,20 @@ int orc_generate_weights(const float *r, const float *zw, int N, int nbins, int3
 void orc_reduce27(const float *const *J6, const float *r, int N, double A[36], double b[6]);
 void orc_reduce27_refordered(const float *const *J6, const float *r, int N, float A[36], float b[6]);
 
+/* Exact fixed-point accumulation of FP32 values (the tracker's reduction): a
+ * value v is the integer sum_k L[k] * 2^(32k) in units of 2^-64; FP32 inputs
+ * are truncated toward zero at 2^-64 and must satisfy |v| < 2^48 (else `bad`). */
+#define ORC_FX_LIMBS 4
+typedef struct orc_fx27 {
+    long long L[27][ORC_FX_LIMBS];
+    int bad;
+} orc_fx27;
+void orc_fx_add(long long L[ORC_FX_LIMBS], float v, int *bad);
+double orc_fx_to_double(const long long L[ORC_FX_LIMBS]);
+void orc_fx27_clear(orc_fx27 *acc);
+void orc_reduce27_fx(const float *const *J6, const float *r, int N, orc_fx27 *acc);
+void orc_fx27_value(const orc_fx27 *acc, double A[36], double b[6]);
+
 /* ---- ICP ---- */
 void orc_zmap_to_xyz6(const float *z, int W, int H, const float *calib, float *pts6, int32_t *mask);
 void orc_compute_normals6(float *pts6, int32_t *mask, int W, int H);

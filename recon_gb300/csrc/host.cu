@@ -6,6 +6,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <cmath>
 #include <atomic>
 #include <mutex>
@@ -28,7 +29,7 @@ __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
 __global__ void k_icp_compact(const InstDesc *D, int level);
 __global__ void k_icp_student(const InstDesc *D, int level, int pass);
-__global__ void k_iter(const InstDesc *D, int level, int it, int nph_grid);
+__global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
 __global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
                                uint16_t *out);
 __global__ void k_render_gray(recon_scene sc, recon_camera cam, uint8_t *out);
@@ -198,9 +199,7 @@ size_t layout(InstDesc &d, char *base) {
     d.sel_xyz = a.take<float>(3 * (size_t)P);
     d.ph_r = a.take<float>(P);
     d.ph_zw = a.take<float>(P);
-    d.ph_part = a.take<double>(27);
     d.ph_hist = a.take<int>(1024);
-    d.ph_counter = a.take<unsigned int>(4);
     d.icp_res = a.take<float>(n);
     d.icp_mask = a.take<uint8_t>(n);
     int nblk = (n + kChunk - 1) / kChunk;
@@ -212,7 +211,9 @@ size_t layout(InstDesc &d, char *base) {
     d.icp_pk_nrm = a.take<float4>(n);
     d.icp_var = a.take<unsigned long long>(4);
     d.icp_nsel = a.take<int>(kMaxLevels);
-    d.icp_part = a.take<double>((size_t)nblk * 27);
+    d.fuse_c2 = a.take<double>(kMaxLevels);
+    d.fx = a.take<unsigned long long>(2 * 27 * kFxLimbs);
+    d.fx_bad = a.take<int>(2);
     d.work = a.take<unsigned long long>(4);
     d.counter = a.take<unsigned int>(4);
     d.T = a.take<float>(16);
@@ -417,10 +418,15 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
             }
             b->graph_kernels += 5;
         }
-        int nph = b->max_P / kChunk;
+        // ICP chunks per CTA: enough CTAs for about four waves of the batch's
+        // chunks, at most 8 chunks each (the result does not depend on it)
+        int per_cta = std::min(8, std::max(1, (n * nchunk) / (8 * kIterCtaSlots)));
+        int ncta = (nchunk + per_cta - 1) / per_cta;
+        // the photometric cluster, then the ICP CTAs rounded up to whole clusters
+        int gx = kIterCluster + (any_icp ? (ncta + kIterCluster - 1) / kIterCluster * kIterCluster : 0);
         for (int it = 0; it < maxit; it++) {
             TimedScope ts(b, s, TK_ITER, in_graph);
-            k_iter<<<dim3(nph + (any_icp ? nchunk : 0), n), 512, 0, s>>>(D, level, it, nph);
+            k_iter<<<dim3(gx, n), kIterBlock, 0, s>>>(D, level, it, per_cta);
             b->graph_kernels++;
         }
     }
@@ -504,10 +510,10 @@ __global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_i
     if (t < ST_COUNT) d.stats[t] = 0;
     if (t == 0) {
         *d.counter = 0u;
-        *d.ph_counter = 0u;
         if (d.trace_count) *d.trace_count = 0;
     }
-    for (int k = t; k < 256; k += blockDim.x) d.ph_hist[k] = 0;
+    for (int k = t; k < 2 * 27 * kFxLimbs; k += blockDim.x) d.fx[k] = 0ull;
+    if (t < 2) d.fx_bad[t] = 0;
 }
 
 }  // namespace rt
@@ -608,6 +614,7 @@ int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs,
         d.mode = c.mode;
         d.solver = c.solver;
         d.lambda = c.lambda;
+        d.fuse_c1 = (double)(1.0f - c.lambda) / (double)c.n_select;
         d.opt_in = c.opt_scale_in;
         d.opt_out = c.opt_scale_out;
         d.precision = c.precision;
@@ -818,6 +825,7 @@ int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambd
     b->cfg[inst] = c;
     b->desc[inst].mode = c.mode;
     b->desc[inst].lambda = c.lambda;
+    b->desc[inst].fuse_c1 = (double)(1.0f - c.lambda) / (double)c.n_select;
     b->graph_dirty = true;
     return upload_desc(b);
 }

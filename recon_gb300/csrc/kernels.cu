@@ -10,6 +10,7 @@
 #include <mutex>
 
 #include "scene.h"
+#include "fx.cuh"
 #include "solve.cuh"
 #include "track_kernels.cuh"
 #include "track_math.cuh"
@@ -612,7 +613,11 @@ __global__ void k_icp_compact(const InstDesc *D, int level) {
         if (threadIdx.x == 0) { s_base = pre; s_tot = tot; }
     }
     __syncthreads();
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.icp_nsel[level] = s_tot;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        d.icp_nsel[level] = s_tot;
+        // ICP weight of the fused system, kept off the iteration's critical path
+        d.fuse_c2[level] = (double)d.lambda / (double)s_tot;
+    }
     int base = s_base;
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     long long vsum = 0;
@@ -674,20 +679,70 @@ __global__ void k_icp_student(const InstDesc *D, int level, int pass) {
 // one Gauss-Newton iteration for every instance
 // ------------------------------------------------------------------
 
-constexpr int kIterThreads = 512;  // k_iter block: 2 points per thread in the gather phase
+constexpr int kIterThreads = kIterBlock;  // one canonical lane (4 points of a chunk) per thread
+constexpr int kCluster = kIterCluster;
+constexpr int kFxTerms = 27 * kFxLimbs;
 
 struct IterShared {
     float T[16];
-    float pts[7][kChunk];  // one chunk's per-point values: r (or r*w) and the 6 Jacobian columns
-    float wpf[8][28];      // FP32 warp totals of one chunk
-    double wpart[8][27];
-    double tot[27];
+    long long fx[27][kFxLimbs];  // this CTA's fixed-point sums of its warp totals
+    int fx_bad;
     double A_ph[27], A_icp[27];
-    int hist[256];
+    int hist[256];      // this CTA's photometric histogram (read by its cluster)
+    int hist_all[256];  // the instance's histogram
     int median;
     int last;
     SolveScratch S;
 };
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory"); }
+
+// address of `p` (a shared-memory variable of this CTA) in CTA `rank` of the cluster
+template <class T> __device__ __forceinline__ T *cluster_peer(T *p, int rank) {
+    unsigned long long out;
+    asm volatile("mapa.u64 %0, %1, %2;\n" : "=l"(out) : "l"((unsigned long long)p), "r"(rank));
+    return reinterpret_cast<T *>(out);
+}
+
+__device__ __forceinline__ void fx_clear(IterShared &sh) {
+    for (int k = threadIdx.x; k < kFxTerms; k += blockDim.x) (&sh.fx[0][0])[k] = 0;
+    if (threadIdx.x == 0) sh.fx_bad = 0;
+}
+
+// A lane's running fixed-point sum of one term (the term whose warp totals the
+// lane receives from warp_terms).
+struct FxReg {
+    long long l0 = 0, l1 = 0, l2 = 0, l3 = 0;
+    int bad = 0;
+    __device__ __forceinline__ void add(float v) {
+        int k0;
+        long long lo, hi;
+        fx_split(v, k0, lo, hi, bad);  // k0 <= 2 for every in-range value
+        l0 += (k0 == 0) ? lo : 0;
+        l1 += (k0 == 1) ? lo : ((k0 == 0) ? hi : 0);
+        l2 += (k0 == 2) ? lo : ((k0 == 1) ? hi : 0);
+        l3 += (k0 == 2) ? hi : 0;
+    }
+    // adds lane q's sums (q < 27) into the CTA's
+    __device__ __forceinline__ void merge(IterShared &sh, int q) const {
+        unsigned long long *f = reinterpret_cast<unsigned long long *>(sh.fx[q]);
+        if (l0) atomicAdd(f + 0, (unsigned long long)l0);
+        if (l1) atomicAdd(f + 1, (unsigned long long)l1);
+        if (l2) atomicAdd(f + 2, (unsigned long long)l2);
+        if (l3) atomicAdd(f + 3, (unsigned long long)l3);
+        if (bad) sh.fx_bad = 1;
+    }
+};
+
+// Adds the CTA's fixed-point sums to the instance's (after a __syncthreads).
+__device__ __forceinline__ void fx_flush(const IterShared &sh, unsigned long long *dst, int *dst_bad) {
+    if (threadIdx.x < kFxTerms) {
+        long long v = (&sh.fx[0][0])[threadIdx.x];
+        if (v) atomicAdd(dst + threadIdx.x, (unsigned long long)v);
+    }
+    if (threadIdx.x == 0 && sh.fx_bad) atomicOr(dst_bad, 1);
+}
 
 // canonical per-lane accumulation of the 27 normal-equation terms
 __device__ __forceinline__ void acc27(float *s, const float *j, float r) {
@@ -700,86 +755,86 @@ __device__ __forceinline__ void acc27(float *s, const float *j, float r) {
     for (int c = 0; c < 6; c++) s[q++] += j[c] * r;
 }
 
-// warp butterfly (xor 16..1) in FP32, then the chunk value in FP64 summed
-// over the CTA's 8 warps in warp order; accumulated into sh.tot.
-__device__ __forceinline__ void chunk_fold(IterShared &sh, float *s) {
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+// Warp totals of the 27 terms by recursive halving: at the step with offset o
+// each lane keeps half of its values and adds the partner's copy of them, so
+// lane q ends with term q.  Every addition pairs the same two partial sums as
+// the canonical xor butterfly (offsets 16, 8, 4, 2, 1), so the totals are the
+// butterfly's bit for bit, with 31 shuffles instead of 135.
+__device__ __forceinline__ float warp_terms(const float *v) {
+    int lane = threadIdx.x & 31;
+    float a[16];
+    bool h = lane & 16;
 #pragma unroll
-    for (int q = 0; q < 27; q++) {
-        float v = s[q];
-        for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) sh.wpart[wid][q] = (double)v;
+    for (int i = 0; i < 16; i++) {
+        float x = v[i], y = (i + 16 < 27) ? v[i + 16] : 0.0f;
+        float send = h ? x : y, keep = h ? y : x;
+        a[i] = keep + __shfl_xor_sync(kFull, send, 16);
     }
-    __syncthreads();
-    if (threadIdx.x < 27) {
-        int q = threadIdx.x;
-        double c = 0.0;
-        for (int w = 0; w < 8; w++) c = c + sh.wpart[w][q];
-        sh.tot[q] = sh.tot[q] + c;
+    float b[8];
+    h = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        float send = h ? a[i] : a[i + 8], keep = h ? a[i + 8] : a[i];
+        b[i] = keep + __shfl_xor_sync(kFull, send, 8);
     }
-    __syncthreads();
+    float c[4];
+    h = lane & 4;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float send = h ? b[i] : b[i + 4], keep = h ? b[i + 4] : b[i];
+        c[i] = keep + __shfl_xor_sync(kFull, send, 4);
+    }
+    float e[2];
+    h = lane & 2;
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        float send = h ? c[i] : c[i + 2], keep = h ? c[i + 2] : c[i];
+        e[i] = keep + __shfl_xor_sync(kFull, send, 2);
+    }
+    h = lane & 1;
+    float send = h ? e[0] : e[1], keep = h ? e[1] : e[0];
+    return keep + __shfl_xor_sync(kFull, send, 1);
 }
 
-// Canonical terms [LO, HI) of one point (the loops unroll, so q is a
-// compile-time constant and only HI-LO accumulators are live).
-template <int LO, int HI>
-__device__ __forceinline__ void acc_terms(float *s, const float *j, float r) {
-    int q = 0;
-#pragma unroll
-    for (int a = 0; a < 6; a++)
-#pragma unroll
-        for (int c = a; c < 6; c++) {
-            if (q >= LO && q < HI) s[q - LO] += j[a] * j[c];
-            q++;
+// Median bin of an instance histogram (seekThreshold64Kernel,
+// histogram64.cu:48-61): first bin whose cumulative count exceeds P/2.  Warp 0.
+__device__ __forceinline__ void hist_median(IterShared &sh, const int *hist, int nb, int P) {
+    if (threadIdx.x >= 32) return;
+    int lane = threadIdx.x;
+    int per = (nb + 31) / 32;
+    int loc = 0;
+    for (int k = 0; k < per; k++) {
+        int bin = lane * per + k;
+        if (bin < nb) loc += hist[bin];
+    }
+    int incl = loc;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    int half = P / 2;
+    unsigned int over = __ballot_sync(0xffffffffu, incl > half);
+    if (over) {
+        int l0 = __ffs(over) - 1;
+        if (lane == l0) {
+            int acc = incl - loc, med = 0;
+            for (int k = 0; k < per; k++) {
+                int bin = lane * per + k;
+                if (bin < nb) {
+                    acc += hist[bin];
+                    if (acc > half) { med = bin; break; }
+                }
+            }
+            sh.median = med;
         }
-#pragma unroll
-    for (int c = 0; c < 6; c++) {
-        if (q >= LO && q < HI) s[q - LO] += j[c] * r;
-        q++;
+    } else if (lane == 0) {
+        sh.median = 0;
     }
 }
 
-template <int LO, int HI>
-__device__ __forceinline__ void lane_terms(IterShared &sh, int t) {
-    float s[HI - LO];
-#pragma unroll
-    for (int q = 0; q < HI - LO; q++) s[q] = 0.0f;
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-        int k = t + kLanes * m;
-        float j[6];
-#pragma unroll
-        for (int c = 0; c < 6; c++) j[c] = sh.pts[1 + c][k];
-        acc_terms<LO, HI>(s, j, sh.pts[0][k]);
-    }
-    int lane = threadIdx.x & 31, w8 = (threadIdx.x >> 5) & 7;
-#pragma unroll
-    for (int q = 0; q < HI - LO; q++) {
-        float v = s[q];
-        for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) sh.wpf[w8][LO + q] = v;
-    }
-}
-
-// The canonical reduction of the chunk held in sh.pts by a 512-thread CTA:
-// threads 0-255 are lanes 0-255 for terms 0-13, threads 256-511 the same lanes
-// for terms 14-26 (each term's lane sum, butterfly and warp order are those of
-// the canonical order); the 8 FP32 warp values of each term are converted to
-// FP64 by one thread and summed in warp order into sh.tot.
-__device__ __forceinline__ void accumulate_chunk(IterShared &sh) {
-    int t = threadIdx.x & (kLanes - 1);
-    if (threadIdx.x < kLanes) lane_terms<0, 14>(sh, t);
-    else lane_terms<14, 27>(sh, t);
-    __syncthreads();
-    if (threadIdx.x < 27) {
-        int q = threadIdx.x;
-        double c = 0.0;
-        for (int w = 0; w < 8; w++) c = c + (double)sh.wpf[w][q];
-        sh.tot[q] = sh.tot[q] + c;
-    }
-    __syncthreads();
-}
-
+// One photometric iteration by a single 256-thread CTA (the allocation-free
+// entry point): residuals, histogram, median, weights and the fixed-point sums
+// of all P points; the 27 terms end in sh.A_ph.
 __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
     int P = d.P;
     int w = d.W >> level, h = d.H >> level;
@@ -789,6 +844,7 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
     const float *I = d.sel_I[level];
     int nb = d.hist_bins;
     for (int k = threadIdx.x; k < nb; k += blockDim.x) sh.hist[k] = 0;
+    fx_clear(sh);
     __syncthreads();
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
         float r, zw;
@@ -799,45 +855,12 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
         atomicAdd(&sh.hist[mad_bin(r, nb)], 1);
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        // first bin whose cumulative count exceeds P/2 (seekThreshold64Kernel, histogram64.cu:48-61)
-        int lane = threadIdx.x;
-        int per = (nb + 31) / 32;
-        int loc = 0;
-        for (int k = 0; k < per; k++) {
-            int bin = lane * per + k;
-            if (bin < nb) loc += sh.hist[bin];
-        }
-        int incl = loc;
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        int half = P / 2;
-        unsigned int over = __ballot_sync(0xffffffffu, incl > half);
-        int med = 0;
-        if (over) {
-            int l0 = __ffs(over) - 1;
-            if (lane == l0) {
-                int acc = incl - loc;
-                for (int k = 0; k < per; k++) {
-                    int bin = lane * per + k;
-                    if (bin < nb) {
-                        acc += sh.hist[bin];
-                        if (acc > half) { med = bin; break; }
-                    }
-                }
-                sh.median = med;
-            }
-        } else if (lane == 0) {
-            sh.median = 0;
-        }
-    }
-    for (int q = threadIdx.x; q < 27; q += blockDim.x) sh.tot[q] = 0.0;
+    hist_median(sh, sh.hist, nb, P);
     __syncthreads();
     float s = mad_scale(sh.median, nb);
     const float *J = d.sel_J[level];
-    int t = threadIdx.x;
+    int t = threadIdx.x, lane = t & 31;
+    FxReg F;
     for (int c = 0; c < P / kChunk; c++) {
         float acc[27];
 #pragma unroll
@@ -851,11 +874,16 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
             for (int k = 0; k < 6; k++) jw[k] = J[k * P + i] * wv;
             acc27(acc, jw, r * wv);
         }
-        chunk_fold(sh, acc);
+        float v = warp_terms(acc);
+        if (lane < 27) F.add(v);
     }
+    if (lane < 27) F.merge(sh, lane);
+    __syncthreads();
     if (threadIdx.x < 27) {
-        sh.A_ph[threadIdx.x] = sh.tot[threadIdx.x];
-        d.ph_part[threadIdx.x] = sh.tot[threadIdx.x];
+        long long L[kFxLimbs];
+#pragma unroll
+        for (int k = 0; k < kFxLimbs; k++) L[k] = sh.fx[threadIdx.x][k];
+        sh.A_ph[threadIdx.x] = sh.fx_bad ? __longlong_as_double(0x7ff8000000000000LL) : fx_to_double(L);
     }
 }
 
@@ -891,236 +919,261 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     float optScaleIn = d.opt_in;
     float rvx = cx - qx, rvy = cy - qy, rvz = cz - qz;
     res = optScaleIn * weight * (rvx * cnx + rvy * cny + rvz * cnz);
-    const float dP[3][3] = {{0, -p.z, p.y}, {p.z, 0, -p.x}, {-p.y, p.x, 0}};
-    const float dNv[3][3] = {{0, -rn.z, rn.y}, {rn.z, 0, -rn.x}, {-rn.y, rn.x, 0}};
+    // The reference rotates the columns of [p]x and [n]x and the unit vectors
+    // with full 3x3 products.  The terms it multiplies by an exact 0 or 1 are
+    // dropped here: for a finite pose that changes at most the sign of a zero
+    // Jacobian entry, and signed zeros add nothing to the fixed-point sums, so
+    // the normal equations are bit-identical.
+    float b0x = T[1] * (-p.z) + T[2] * p.y, b0y = T[5] * (-p.z) + T[6] * p.y, b0z = T[9] * (-p.z) + T[10] * p.y;
+    float b1x = T[0] * p.z + T[2] * (-p.x), b1y = T[4] * p.z + T[6] * (-p.x), b1z = T[8] * p.z + T[10] * (-p.x);
+    float b2x = T[0] * (-p.y) + T[1] * p.x, b2y = T[4] * (-p.y) + T[5] * p.x, b2z = T[8] * (-p.y) + T[9] * p.x;
+    float n0x = T[1] * (-rn.z) + T[2] * rn.y, n0y = T[5] * (-rn.z) + T[6] * rn.y, n0z = T[9] * (-rn.z) + T[10] * rn.y;
+    float n1x = T[0] * rn.z + T[2] * (-rn.x), n1y = T[4] * rn.z + T[6] * (-rn.x), n1z = T[8] * rn.z + T[10] * (-rn.x);
+    float n2x = T[0] * (-rn.y) + T[1] * rn.x, n2y = T[4] * (-rn.y) + T[5] * rn.x, n2z = T[8] * (-rn.y) + T[9] * rn.x;
+    float so = -optScaleIn * weight;
+    j[0] = so * (-cnx * b0x - cny * b0y - cnz * b0z + rvx * n0x + rvy * n0y + rvz * n0z);
+    j[1] = so * (-cnx * b1x - cny * b1y - cnz * b1z + rvx * n1x + rvy * n1y + rvz * n1z);
+    j[2] = so * (-cnx * b2x - cny * b2y - cnz * b2z + rvx * n2x + rvy * n2y + rvz * n2z);
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float bx, by, bz, nx, ny, nz;
-        rot4(T, dP[c][0], dP[c][1], dP[c][2], bx, by, bz);
-        rot4(T, dNv[c][0], dNv[c][1], dNv[c][2], nx, ny, nz);
-        j[c] = -optScaleIn * weight * (-cnx * bx - cny * by - cnz * bz + rvx * nx + rvy * ny + rvz * nz);
-    }
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float e0 = c == 0 ? 1.0f : 0.0f, e1 = c == 1 ? 1.0f : 0.0f, e2 = c == 2 ? 1.0f : 0.0f;
-        float bx, by, bz;
-        rot4(T, e0, e1, e2, bx, by, bz);
-        j[3 + c] = -weight * (-cnx * bx - cny * by - cnz * bz);
-    }
+    for (int c = 0; c < 3; c++) j[3 + c] = -weight * (-cnx * T[c] - cny * T[4 + c] - cnz * T[8 + c]);
 }
 
-// One ICP chunk (1024 correspondences) with a 512-thread CTA: each thread
-// evaluates two points into shared memory, then the chunk is reduced.
-__device__ void icp_chunk(const InstDesc &d, IterShared &sh, int level, int chunk, int nsel) {
-    for (int q = threadIdx.x; q < 27; q += blockDim.x) sh.tot[q] = 0.0;
-#pragma unroll
-    for (int m = 0; m < 2; m++) {
-        int k = threadIdx.x + kIterThreads * m;
-        float j[6], r;
-        icp_point(d, sh.T, level, chunk * kChunk + k, nsel, j, r);
-        sh.pts[0][k] = r;
-#pragma unroll
-        for (int c = 0; c < 6; c++) sh.pts[1 + c][k] = j[c];
-    }
-    __syncthreads();
-    accumulate_chunk(sh);
-    if (threadIdx.x < 27) d.icp_part[(size_t)chunk * 27 + threadIdx.x] = sh.tot[threadIdx.x];
-}
-
-__device__ __forceinline__ void unpack27(const double *t, double *A, double *b) {
-    int q = 0;
-    for (int j = 0; j < 6; j++)
-        for (int i = j; i < 6; i++) {
-            A[i + j * 6] = t[q];
-            A[i * 6 + j] = t[q];
-            q++;
-        }
-    for (int c = 0; c < 6; c++) b[c] = t[q++];
-}
-
-// Warp 0 of the finalising CTA: builds the system of the mode (fused in FP64
-// for BIOBJECTIVE, linearFuseKernel warp.cu:918-924), solves, updates the pose
-// and records statistics and the optional iteration trace.
-__device__ __noinline__ void finalize_solve(const InstDesc &d, IterShared &sh, int level, int it, bool use_ph,
-                                            bool use_icp, int nsel) {
-    int lane = threadIdx.x;
-    SolveScratch &S = sh.S;
-    int median = use_ph ? __ldcg(d.ph_hist + 512) : -1;
-    if (lane == 0) {
-        double Aph[36], bph[6], Aic[36], bic[6];
-        for (int i = 0; i < 36; i++) { Aph[i] = 0.0; Aic[i] = 0.0; }
-        for (int i = 0; i < 6; i++) { bph[i] = 0.0; bic[i] = 0.0; }
-        if (use_ph) unpack27(sh.A_ph, Aph, bph);
-        if (use_icp && nsel > 0) unpack27(sh.A_icp, Aic, bic);
-        if (d.mode == RECON_PHOTOMETRIC) {
-            for (int i = 0; i < 36; i++) S.A[i] = Aph[i];
-            for (int i = 0; i < 6; i++) S.b[i] = bph[i];
-        } else if (d.mode == RECON_GEOMETRIC) {
-            for (int i = 0; i < 36; i++) S.A[i] = Aic[i];
-            for (int i = 0; i < 6; i++) S.b[i] = bic[i];
-        } else {
-            // (1-lambda)/N1 * photo + lambda/N2 * icp
-            double c1 = (double)(1.0f - d.lambda) / (double)d.P;
-            double c2 = (double)d.lambda / (double)nsel;
-            for (int i = 0; i < 36; i++) S.A[i] = c1 * Aph[i] + c2 * Aic[i];
-            for (int i = 0; i < 6; i++) S.b[i] = c1 * bph[i] + c2 * bic[i];
-        }
-        if (d.trace) {
-            int slot = *d.trace_count;
-            if (slot < d.trace_max) {
-                recon_iter_trace *tr = d.trace + slot;
-                for (int i = 0; i < 36; i++) { tr->A[i] = S.A[i]; tr->A_ph[i] = Aph[i]; tr->A_icp[i] = Aic[i]; }
-                for (int i = 0; i < 6; i++) { tr->b[i] = S.b[i]; tr->b_ph[i] = bph[i]; tr->b_icp[i] = bic[i]; }
-            }
-        }
-    }
-    bool ok = !(use_icp && nsel <= 0);  // ShapeTracker "not enough points": no solve
-    __syncwarp();
-    int st = 0;
-    if (ok) st = wsolve_update(S, d.solver, sh.T, (double)d.opt_out, lane);
-    if (lane < 16) d.T[lane] = sh.T[lane];
-    if (lane == 0) {
-        d.stats[ST_ITERS] += 1;
-        if (ok) d.stats[ST_SOLVES] += 1;
-        if (st != 0) d.stats[ST_NONSPD] += 1;
-        if (use_ph) d.stats[ST_MEDIAN] = median;
-        if (use_ph) d.work[0] += (unsigned long long)d.P;
-        if (use_icp) d.work[1] += (unsigned long long)nsel;
-        if (use_icp) d.stats[ST_ICPSEL0 + level] = nsel;
-        if (d.trace) {
-            int slot = *d.trace_count;
-            if (slot < d.trace_max) {
-                recon_iter_trace *tr = d.trace + slot;
-                tr->level = level;
-                tr->iter = it;
-                tr->mode = d.mode;
-                tr->solved = ok ? 1 : 0;
-                tr->status = st;
-                tr->icp_selected = use_icp ? nsel : 0;
-                for (int i = 0; i < 16; i++) tr->T[i] = sh.T[i];
-                tr->median_bin = median;
-                for (int k = 0; k < 256; k++)
-                    tr->hist[k] = (use_ph && k < d.hist_bins) ? __ldcg(d.ph_hist + 256 + k) : 0;
-            }
-            *d.trace_count = slot + 1;
-        }
-        *d.counter = 0u;
-    }
-}
-
-// Photometric pass A for chunk c of an instance (interpolateResidualKernel2,
-// warp.cu:269-332, and the histogram of histogram64.cu:115-145): residuals and
-// depth weights of 1024 points to global scratch, their MAD-histogram counts
-// added to the instance's global histogram.
-__device__ void photo_pass_a(const InstDesc &d, IterShared &sh, int level, int c) {
+// Photometric residuals of lane t's 4 points of chunk c
+// (interpolateResidualKernel2, warp.cu:269-332).
+__device__ __forceinline__ void photo_lane_residuals(const InstDesc &d, const float *T, int level, int c, int t,
+                                                     float *r, float *zw) {
     int P = d.P;
     int w = d.W >> level, h = d.H >> level;
     float a = 1.0f / (float)(1 << level);
     float b = 0.5f * (a - 1.0f);
     const float *img = d.cur_gray[level];
     const float *I = d.sel_I[level];
-    int nb = d.hist_bins;
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) sh.hist[k] = 0;
-    __syncthreads();
 #pragma unroll
-    for (int m = 0; m < kChunk / kIterThreads; m++) {
-        int i = c * kChunk + threadIdx.x + kIterThreads * m;
-        float r, zw;
-        photo_residual(d.calib, sh.T, a, b, __ldg(d.sel_xyz + i), __ldg(d.sel_xyz + P + i),
-                       __ldg(d.sel_xyz + 2 * P + i), __ldg(I + i), img, w, h, d.cur_z, d.W, d.H, r, zw);
-        d.ph_r[i] = r;
-        d.ph_zw[i] = zw;
-        atomicAdd(&sh.hist[mad_bin(r, nb)], 1);
+    for (int m = 0; m < 4; m++) {
+        int i = c * kChunk + t + kLanes * m;
+        photo_residual(d.calib, T, a, b, __ldg(d.sel_xyz + i), __ldg(d.sel_xyz + P + i), __ldg(d.sel_xyz + 2 * P + i),
+                       __ldg(I + i), img, w, h, d.cur_z, d.W, d.H, r[m], zw[m]);
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < nb; k += blockDim.x)
-        if (sh.hist[k]) atomicAdd(d.ph_hist + k, sh.hist[k]);
 }
 
-// Photometric pass B, run by the last pass-A CTA of an instance: median bin
-// (seekThreshold64Kernel, histogram64.cu:48-61), Tukey weights
-// (generateWeights64Kernel, 79-94) and the 27 terms over all points in the
-// canonical chunk order.
-__device__ void photo_pass_b(const InstDesc &d, IterShared &sh, int level) {
-    int P = d.P;
-    int nb = d.hist_bins;
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
-        int v = __ldcg(d.ph_hist + k);
-        sh.hist[k] = v;
-        d.ph_hist[256 + k] = v;  // kept for the iteration trace
-        d.ph_hist[k] = 0;        // ready for the next iteration
-    }
+// The photometric term of an instance by its cluster of 8 CTAs: CTA `rank`
+// evaluates chunks rank, rank + 8, ...; the cluster adds its histograms
+// (histogram64.cu:115-145) through distributed shared memory, every CTA finds
+// the median bin (seekThreshold64Kernel, histogram64.cu:48-61) and weighs its
+// own points (generateWeights64Kernel, 79-94) into the lane's fixed-point sum.
+// Returns whether this CTA had a chunk.
+__device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int rank, FxReg &F) {
+    int P = d.P, nph = P / kChunk, nb = d.hist_bins;
+    int t = threadIdx.x, lane = t & 31;
+    const float *J = d.sel_J[level];
+    for (int k = t; k < nb; k += blockDim.x) sh.hist[k] = 0;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        int lane = threadIdx.x;
-        int per = (nb + 31) / 32;
-        int loc = 0;
-        for (int k = 0; k < per; k++) {
-            int bin = lane * per + k;
-            if (bin < nb) loc += sh.hist[bin];
-        }
-        int incl = loc;
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        int half = P / 2;
-        unsigned int over = __ballot_sync(0xffffffffu, incl > half);
-        if (over) {
-            int l0 = __ffs(over) - 1;
-            if (lane == l0) {
-                int acc = incl - loc, med = 0;
-                for (int k = 0; k < per; k++) {
-                    int bin = lane * per + k;
-                    if (bin < nb) {
-                        acc += sh.hist[bin];
-                        if (acc > half) { med = bin; break; }
-                    }
-                }
-                sh.median = med;
+    float r0[4], zw0[4];
+    for (int c = rank; c < nph; c += kCluster) {
+        float r[4], zw[4];
+        photo_lane_residuals(d, sh.T, level, c, t, r, zw);
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            atomicAdd(&sh.hist[mad_bin(r[m], nb)], 1);
+            if (c == rank) {
+                r0[m] = r[m];
+                zw0[m] = zw[m];
+            } else {  // later chunks of this CTA go through global scratch
+                int i = c * kChunk + t + kLanes * m;
+                d.ph_r[i] = r[m];
+                d.ph_zw[i] = zw[m];
             }
-        } else if (lane == 0) {
-            sh.median = 0;
         }
     }
-    for (int q = threadIdx.x; q < 27; q += blockDim.x) sh.tot[q] = 0.0;
+    // the first chunk's Jacobian: its loads overlap the histogram exchange
+    float j0[4][6];
+    if (rank < nph) {
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int k = 0; k < 6; k++) j0[m][k] = __ldg(J + k * P + rank * kChunk + t + kLanes * m);
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        d.ph_hist[512] = sh.median;
-        *d.ph_counter = 0u;
+    cluster_arrive();
+    cluster_wait();  // every CTA's histogram is complete
+    for (int k = t; k < nb; k += blockDim.x) {
+        int s = 0;
+#pragma unroll
+        for (int q = 0; q < kCluster; q++) s += *cluster_peer(&sh.hist[k], q);
+        sh.hist_all[k] = s;
+    }
+    cluster_arrive();  // done reading the others' histograms; the wait is before this CTA leaves
+    __syncthreads();
+    hist_median(sh, sh.hist_all, nb, P);
+    __syncthreads();
+    if (rank == 0) {
+        for (int k = t; k < nb; k += blockDim.x) d.ph_hist[256 + k] = sh.hist_all[k];  // for the trace
+        if (t == 0) d.ph_hist[512] = sh.median;
     }
     float s = mad_scale(sh.median, nb);
-    const float *J = d.sel_J[level];
-    for (int c = 0; c < P / kChunk; c++) {
+    for (int c = rank; c < nph; c += kCluster) {
+        float acc[27];
 #pragma unroll
-        for (int m = 0; m < kChunk / kIterThreads; m++) {
-            int k = threadIdx.x + kIterThreads * m;
-            int i = c * kChunk + k;
-            float r = __ldcg(d.ph_r + i);
-            float wv = tukey_weight(r, __ldcg(d.ph_zw + i), s);
-            sh.pts[0][k] = r * wv;
+        for (int q = 0; q < 27; q++) acc[q] = 0.0f;
 #pragma unroll
-            for (int q = 0; q < 6; q++) sh.pts[1 + q][k] = __ldg(J + q * P + i) * wv;
+        for (int m = 0; m < 4; m++) {
+            int i = c * kChunk + t + kLanes * m;
+            float r, zw, jv[6];
+            if (c == rank) {
+                r = r0[m];
+                zw = zw0[m];
+#pragma unroll
+                for (int k = 0; k < 6; k++) jv[k] = j0[m][k];
+            } else {
+                r = d.ph_r[i];  // written by this thread above
+                zw = d.ph_zw[i];
+#pragma unroll
+                for (int k = 0; k < 6; k++) jv[k] = __ldg(J + k * P + i);
+            }
+            float wv = tukey_weight(r, zw, s);
+            float jw[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) jw[k] = jv[k] * wv;
+            acc27(acc, jw, r * wv);
         }
-        __syncthreads();
-        accumulate_chunk(sh);
+        float v = warp_terms(acc);
+        if (lane < 27) F.add(v);
     }
-    if (threadIdx.x < 27) {
-        sh.A_ph[threadIdx.x] = sh.tot[threadIdx.x];
-        d.ph_part[threadIdx.x] = sh.tot[threadIdx.x];
+    cluster_wait();
+    return rank < nph;
+}
+
+// ICP chunks [c0, c1) of an instance: lane t evaluates points t + 256m of each
+// chunk (icpResidualIndexKernel2 and the reference's per-point Jacobian), the
+// warp totals of each chunk go into the lane's fixed-point sum.
+__device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0, int c1, int nsel, FxReg &F) {
+    int t = threadIdx.x, lane = t & 31;
+    for (int c = c0; c < c1; c++) {
+        float acc[27];
+#pragma unroll
+        for (int q = 0; q < 27; q++) acc[q] = 0.0f;
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            int i = c * kChunk + t + kLanes * (2 * g);
+            float ja[6], ra, jb[6], rb;
+            icp_point(d, sh.T, level, i, nsel, ja, ra);
+            icp_point(d, sh.T, level, i + kLanes, nsel, jb, rb);
+            acc27(acc, ja, ra);
+            acc27(acc, jb, rb);
+        }
+        float v = warp_terms(acc);
+        if (lane < 27) F.add(v);
     }
 }
 
-// One GN iteration at `level`, iteration `it`, for every instance.
-// blockIdx.x in [0, nph_grid): photometric pass A of chunk blockIdx.x (the last
-// of an instance's chunks also runs pass B) -- updateLinearSystem,
-// phototracker.cpp:505-511; blockIdx.x >= nph_grid: ICP chunks of 1024
-// correspondences (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).
-// The last participant of an instance to finish fuses (linearFuse,
-// shapetracker.cpp:392-394), solves and applies the SE(3) update
-// (estimateIncrement, phototracker.cpp:646-664).  No CTA waits for another:
-// completion is counted with atomic tickets.
-__global__ void __launch_bounds__(kIterThreads, 2) k_iter(const InstDesc *D, int level, int it, int nph_grid) {
+__device__ __forceinline__ int packed_index(int r, int c) {
+    int a = r < c ? r : c, b = r < c ? c : r;
+    return a * 6 - (a * (a - 1)) / 2 + (b - a);
+}
+
+// Run by the CTA that completes an iteration of an instance: the accumulated
+// terms in FP64 (reset for the next iteration), the system of the mode (fused
+// in FP64 for BIOBJECTIVE with the weights precomputed off this path,
+// linearFuseKernel warp.cu:918-924), the solve and SE(3) update (warp 0), the
+// statistics and the optional trace.
+__device__ __noinline__ void finalize_iter(const InstDesc &d, IterShared &sh, int level, int it, bool use_ph,
+                                           bool use_icp, int nsel) {
+    int t = threadIdx.x;
+    SolveScratch &S = sh.S;
+    if (t < 54) {
+        int set = t / 27, q = t % 27;
+        unsigned long long *src = d.fx + set * kFxTerms + q * kFxLimbs;
+        long long L[kFxLimbs];
+#pragma unroll
+        for (int k = 0; k < kFxLimbs; k++) L[k] = (long long)__ldcg(src + k);
+        int bad = __ldcg(d.fx_bad + set);
+        double v = bad ? __longlong_as_double(0x7ff8000000000000LL) : fx_to_double(L);
+        (set ? sh.A_icp : sh.A_ph)[q] = v;
+#pragma unroll
+        for (int k = 0; k < kFxLimbs; k++) src[k] = 0ull;
+    }
+    __syncthreads();
+    if (t < 2) d.fx_bad[t] = 0;
+    bool ok = !(use_icp && nsel <= 0);  // ShapeTracker "not enough points": no solve
+    int slot = d.trace ? *d.trace_count : 0;
+    bool tr_on = d.trace && slot < d.trace_max;
+    recon_iter_trace *tr = tr_on ? d.trace + slot : nullptr;
+    if (t < 42) {
+        int q = (t < 36) ? packed_index(t / 6, t % 6) : 21 + (t - 36);
+        double aph = sh.A_ph[q], aic = sh.A_icp[q];
+        double v;
+        if (d.mode == RECON_PHOTOMETRIC) v = aph;
+        else if (d.mode == RECON_GEOMETRIC) v = aic;
+        else v = ok ? d.fuse_c1 * aph + d.fuse_c2[level] * aic : aph;  // (1-lambda)/P * photo + lambda/N * icp
+        if (t < 36) S.A[t] = v;
+        else S.b[t - 36] = v;
+        if (tr) {
+            if (t < 36) {
+                tr->A[t] = v;
+                tr->A_ph[t] = aph;
+                tr->A_icp[t] = aic;
+            } else {
+                tr->b[t - 36] = v;
+                tr->b_ph[t - 36] = aph;
+                tr->b_icp[t - 36] = aic;
+            }
+        }
+    }
+    int median = use_ph ? __ldcg(d.ph_hist + 512) : -1;
+    if (tr && t >= 64) {
+        for (int k = t - 64; k < 256; k += blockDim.x - 64)
+            tr->hist[k] = (use_ph && k < d.hist_bins) ? __ldcg(d.ph_hist + 256 + k) : 0;
+    }
+    __syncthreads();
+    if (t >= 32) return;
+    int lane = t;
+    int st = 0;
+    if (ok) st = wsolve_update(S, d.solver, sh.T, (double)d.opt_out, lane);
+    if (lane < 16) d.T[lane] = sh.T[lane];
+    if (tr && lane < 16) tr->T[lane] = sh.T[lane];
+    if (lane == 0) {
+        // loads first, then stores: the counters are independent
+        int *stt = d.stats;
+        unsigned long long *wk = d.work;
+        int s_it = stt[ST_ITERS], s_so = stt[ST_SOLVES], s_ns = stt[ST_NONSPD];
+        unsigned long long w0 = wk[0], w1 = wk[1];
+        stt[ST_ITERS] = s_it + 1;
+        if (ok) stt[ST_SOLVES] = s_so + 1;
+        if (st != 0) stt[ST_NONSPD] = s_ns + 1;
+        if (use_ph) stt[ST_MEDIAN] = median;
+        if (use_ph) wk[0] = w0 + (unsigned long long)d.P;
+        if (use_icp) wk[1] = w1 + (unsigned long long)nsel;
+        if (use_icp) stt[ST_ICPSEL0 + level] = nsel;
+        if (tr) {
+            tr->level = level;
+            tr->iter = it;
+            tr->mode = d.mode;
+            tr->solved = ok ? 1 : 0;
+            tr->status = st;
+            tr->icp_selected = use_icp ? nsel : 0;
+            tr->median_bin = median;
+        }
+        if (d.trace) *d.trace_count = slot + 1;
+        *d.counter = 0u;
+    }
+}
+
+// One GN iteration at `level`, iteration `it`, for every instance
+// (blockIdx.y).  blockIdx.x 0..7: the photometric cluster of the instance
+// (updateLinearSystem, phototracker.cpp:505-511); blockIdx.x = 8 + j: ICP
+// chunks [j K, (j+1) K) of 1024 correspondences, K = icp_per_cta
+// (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).  Every
+// participant adds its fixed-point sums to the instance's with integer atomics,
+// so the result does not depend on K or on the order in which CTAs finish; the
+// last to finish fuses (linearFuse, shapetracker.cpp:392-394), solves and
+// applies the SE(3) update (estimateIncrement, phototracker.cpp:646-664).  No
+// CTA waits for another outside its cluster barrier: completion is counted
+// with an atomic ticket.
+#ifndef RECON_ITER_MIN_BLOCKS
+#define RECON_ITER_MIN_BLOCKS 3
+#endif
+__global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads, RECON_ITER_MIN_BLOCKS)
+    k_iter(const InstDesc *D, int level, int it, int icp_per_cta) {
     INST_DESC;
     if (level >= d.L) return;
     if (it >= d.iters[d.L - 1 - level]) return;
@@ -1128,38 +1181,42 @@ __global__ void __launch_bounds__(kIterThreads, 2) k_iter(const InstDesc *D, int
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
     int nsel = use_icp ? d.icp_nsel[level] : 0;
     int nchunks = (nsel + kChunk - 1) / kChunk;
+    int nicp = (nchunks + icp_per_cta - 1) / icp_per_cta;
     int nph = d.P / kChunk;
+    int expected = (use_ph ? min(nph, kCluster) : 0) + nicp;
     int role = blockIdx.x;
-    bool is_ph = role < nph_grid;
-    if (is_ph) {
-        if (role >= nph) return;
-        if (!use_ph && role != 0) return;  // without a photometric term CTA 0 is a null participant
-    } else if (role - nph_grid >= nchunks) {
+    int set = -1;  // which sums this CTA adds to: 0 photometric, 1 ICP, -1 none
+    if (role < kCluster) {
+        if (use_ph) {
+            set = 0;
+        } else {
+            // without a photometric term CTA 0 is a null participant when there
+            // is no ICP chunk either, so the iteration is still finalised
+            if (!(role == 0 && nchunks == 0)) return;
+            expected = 1;
+        }
+    } else if (role - kCluster >= nicp) {
         return;
+    } else {
+        set = 1;
     }
-    // participants of the instance ticket: the photometric pass-B CTA (or the
-    // null participant) and every ICP chunk, so each iteration is finalised once
-    int expected = 1 + nchunks;
     __shared__ IterShared sh;
     if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
+    fx_clear(sh);
     __syncthreads();
-    if (is_ph) {
-        if (use_ph) {
-            photo_pass_a(d, sh, level, role);
-            __threadfence();
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                unsigned int ticket = atomicAdd(d.ph_counter, 1u);
-                sh.last = (ticket == (unsigned)(nph - 1));
-            }
-            __syncthreads();
-            if (!sh.last) return;
-            __threadfence();
-            photo_pass_b(d, sh, level);
-        }
-    } else {
-        icp_chunk(d, sh, level, role - nph_grid, nsel);
+    FxReg F;
+    bool participant = true;
+    if (set == 0) {
+        participant = photo_cluster(d, sh, level, role, F);
+    } else if (set == 1) {
+        int c0 = (role - kCluster) * icp_per_cta;
+        icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), nsel, F);
     }
+    if (!participant) return;
+    int lane = threadIdx.x & 31;
+    if (set >= 0 && lane < 27) F.merge(sh, lane);
+    __syncthreads();
+    if (set >= 0) fx_flush(sh, d.fx + set * kFxTerms, d.fx_bad + set);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1169,28 +1226,7 @@ __global__ void __launch_bounds__(kIterThreads, 2) k_iter(const InstDesc *D, int
     __syncthreads();
     if (!sh.last) return;
     __threadfence();
-    // ---- finalize: ICP totals in chunk order, fuse, solve, update ----
-    if (threadIdx.x < 27) {
-        int q = threadIdx.x;
-        double tot = 0.0;
-        int c = 0;
-        for (; c + 4 <= nchunks; c += 4) {
-            double v0 = __ldcg(d.icp_part + (size_t)(c + 0) * 27 + q);
-            double v1 = __ldcg(d.icp_part + (size_t)(c + 1) * 27 + q);
-            double v2 = __ldcg(d.icp_part + (size_t)(c + 2) * 27 + q);
-            double v3 = __ldcg(d.icp_part + (size_t)(c + 3) * 27 + q);
-            tot = tot + v0;
-            tot = tot + v1;
-            tot = tot + v2;
-            tot = tot + v3;
-        }
-        for (; c < nchunks; c++) tot = tot + __ldcg(d.icp_part + (size_t)c * 27 + q);
-        sh.A_icp[q] = tot;
-        if (use_ph) sh.A_ph[q] = __ldcg(d.ph_part + q);
-    }
-    __syncthreads();
-    if (threadIdx.x >= 32) return;
-    finalize_solve(d, sh, level, it, use_ph, use_icp, nsel);
+    finalize_iter(d, sh, level, it, use_ph, use_icp, nsel);
 }
 
 // ------------------------------------------------------------------
@@ -1236,9 +1272,8 @@ namespace rt {
 
 constexpr int kNoAllocMaxPoints = RECON_NOALLOC_MAX_POINTS;
 
-// residual[P], depth weight[P], then 27 FP64 normal-equation terms:
-// 128 KB + 256 B for the 16384-point maximum
-static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocMaxPoints + 64];
+// residual[P], depth weight[P]: 128 KB for the 16384-point maximum
+static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocMaxPoints];
 
 __global__ void __launch_bounds__(256) k_photo_iter_noalloc(recon_photo_view v, float *scratch, float *T) {
     __shared__ IterShared sh;
@@ -1261,7 +1296,6 @@ __global__ void __launch_bounds__(256) k_photo_iter_noalloc(recon_photo_view v, 
         d.cur_z = const_cast<float *>(v.depth);
         d.ph_r = scratch;
         d.ph_zw = scratch + kNoAllocMaxPoints;
-        d.ph_part = reinterpret_cast<double *>(scratch + 2 * kNoAllocMaxPoints);
     }
     if (threadIdx.x < 16) sh.T[threadIdx.x] = T[threadIdx.x];
     __syncthreads();
@@ -1270,7 +1304,11 @@ __global__ void __launch_bounds__(256) k_photo_iter_noalloc(recon_photo_view v, 
     if (threadIdx.x >= 32) return;
     int lane = threadIdx.x;
     SolveScratch &S = sh.S;
-    if (lane == 0) unpack27(sh.A_ph, S.A, S.b);
+    for (int k = lane; k < 42; k += 32) {
+        int q = (k < 36) ? packed_index(k / 6, k % 6) : 21 + (k - 36);
+        if (k < 36) S.A[k] = sh.A_ph[q];
+        else S.b[k - 36] = sh.A_ph[q];
+    }
     __syncwarp();
     wsolve_update(S, v.solver, sh.T, (double)v.opt_scale_out, lane);
     if (lane < 16) T[lane] = sh.T[lane];

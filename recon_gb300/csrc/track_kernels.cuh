@@ -13,6 +13,10 @@ constexpr int kChunk = 1024;     // canonical reduction chunk (points)
 constexpr int kLanes = 256;      // lanes per chunk, 4 points each
 constexpr int kSegments = 512;   // pixel-selection segments (filterIndex256.cu:183)
 constexpr int kVtxPlanes = 9;    // x y z px py gx gy gmag gray
+constexpr int kIterCluster = 8;  // CTAs of the photometric cluster of the GN iteration kernel
+constexpr int kIterBlock = 256;  // threads of a GN iteration CTA
+constexpr int kIterCtaSlots = 3 * 152;  // GN iteration CTAs resident on a 152-SM GB300
+constexpr int kFxLimbs = 4;      // limbs of a fixed-point sum (fx.cuh)
 
 enum StatSlot { ST_ITERS = 0, ST_SOLVES, ST_NONSPD, ST_STATUS, ST_MEDIAN, ST_ICPSEL0, ST_COUNT = 16 };
 
@@ -21,6 +25,7 @@ struct InstDesc {
     int hist_bins, select_bins, mode, solver;
     float lambda, opt_in, opt_out;
     int precision;
+    double fuse_c1;  // (double)(1 - lambda) / P, the photometric weight of the fused system
     int iters[kMaxLevels];
     float calib[RECON_CALIB_SIZE];
     // reference (keyframe)
@@ -41,9 +46,7 @@ struct InstDesc {
     float4 *cur_pts[kMaxLevels];  // x y z mask
     // photometric scratch
     float *ph_r, *ph_zw;
-    double *ph_part;  // 27
-    int *ph_hist;     // [0,256) accumulation, [256,512) copy for the trace, [512] median
-    unsigned int *ph_counter;
+    int *ph_hist;     // [256,512) the last histogram (for the trace), [512] its median bin
     // ICP scratch
     float *icp_res;          // W*H full-grid residual
     uint8_t *icp_mask;       // W*H
@@ -54,7 +57,10 @@ struct InstDesc {
     float4 *icp_pk_nrm;      // W*H: their normals, .w = Student-t weight
     unsigned long long *icp_var;  // 4
     int *icp_nsel;           // kMaxLevels
-    double *icp_part;        // chunks * 27
+    double *fuse_c2;         // kMaxLevels: lambda / (ICP correspondences) of the level
+    // fixed-point sums of the current iteration: [0,108) photometric, [108,216) ICP
+    unsigned long long *fx;
+    int *fx_bad;             // 2: an accumulated value was out of range
     unsigned long long *work; // [0] photometric point-iterations, [1] ICP point-iterations, [2] ICP mask pixels
     unsigned int *counter;
     float *T;                // 16, device pose (reference IR -> current IR)

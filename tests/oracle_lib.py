@@ -78,6 +78,12 @@ def lib() -> ctypes.CDLL:
             L.orc_solve_cg.argtypes = [vp, vp, ctypes.c_double, i32, vp]
             L.orc_reduce27.argtypes = [vp, vp, i32, vp, vp]
             L.orc_reduce27_refordered.argtypes = [vp, vp, i32, vp, vp]
+            L.orc_fx_add.argtypes = [vp, f32, vp]
+            L.orc_fx_to_double.argtypes = [vp]
+            L.orc_fx_to_double.restype = ctypes.c_double
+            L.orc_fx27_clear.argtypes = [vp]
+            L.orc_reduce27_fx.argtypes = [vp, vp, i32, vp]
+            L.orc_fx27_value.argtypes = [vp, vp, vp]
             L.orc_generate_weights.argtypes = [vp, vp, i32, i32, vp, vp, vp]
             L.orc_student_t.argtypes = [vp, i32, vp]
             L.orc_filter_indices.argtypes = [vp, i32, vp, i32, i32, vp]
