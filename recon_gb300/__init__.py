@@ -329,7 +329,8 @@ class Batch:
         return out[: n // out.itemsize]
 
 
-TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_compact", "icp_student_t", "prep_current", "prep_reference"]
+TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_compact", "icp_student_t", "prep_current", "prep_reference",
+                "gn_solve"]
 
 
 def launch_count() -> int:

@@ -30,6 +30,7 @@ __global__ void k_icp_mask(const InstDesc *D, int level);
 __global__ void k_icp_compact(const InstDesc *D, int level);
 __global__ void k_icp_student(const InstDesc *D, int level, int pass);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
+__global__ void k_solve(const InstDesc *D, int level, int it);
 __global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
                                uint16_t *out);
 __global__ void k_render_gray(recon_scene sc, recon_camera cam, uint8_t *out);
@@ -284,7 +285,7 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
 
 dim3 grid_pix(int pix, int n, int block = 256) { return dim3((pix + block - 1) / block, n, 1); }
 
-enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_COMPACT, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_COUNT };
+enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_COMPACT, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_COUNT };
 
 // brackets one launch with a pair of events when timing is enabled; events
 // recorded during stream capture become graph nodes and are re-recorded by
@@ -425,9 +426,15 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
         // the photometric cluster, then the ICP CTAs rounded up to whole clusters
         int gx = kIterCluster + (any_icp ? (ncta + kIterCluster - 1) / kIterCluster * kIterCluster : 0);
         for (int it = 0; it < maxit; it++) {
-            TimedScope ts(b, s, TK_ITER, in_graph);
-            k_iter<<<dim3(gx, n), kIterBlock, 0, s>>>(D, level, it, per_cta);
-            b->graph_kernels++;
+            {
+                TimedScope ts(b, s, TK_ITER, in_graph);
+                k_iter<<<dim3(gx, n), kIterBlock, 0, s>>>(D, level, it, per_cta);
+            }
+            {
+                TimedScope ts(b, s, TK_SOLVE, in_graph);
+                k_solve<<<n, kSolveThreads, 0, s>>>(D, level, it);
+            }
+            b->graph_kernels += 2;
         }
     }
     CK(cudaGetLastError());

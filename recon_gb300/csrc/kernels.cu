@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstddef>
 #include <mutex>
 
 #include "scene.h"
@@ -638,11 +639,8 @@ __global__ void k_icp_compact(const InstDesc *D, int level) {
             float w0 = 6 / (5 + r2 / 100.0f);
             d.icp_select[pos] = i;
             d.icp_r2[pos] = r2;
-            d.icp_w[pos] = w0;
             d.icp_pk_pts[pos] = d.ref_pts[level][i];
-            float4 nn = d.ref_nrm[level][i];
-            nn.w = w0;
-            d.icp_pk_nrm[pos] = nn;
+            d.icp_pk_nrm[pos] = d.ref_nrm[level][i];
             vsum += trunc_prod(r2, w0);
         }
         base += tot;
@@ -652,7 +650,8 @@ __global__ void k_icp_compact(const InstDesc *D, int level) {
 }
 
 // updateWeightsKernel / clampWeightsKernel (rgb2gray.cu:549-569) with the
-// variance of the previous pass; the final pass clamps at 1.
+// variance of the previous pass; the final pass clamps at 1.  Only the final
+// pass's weights are used, so passes 1 and 2 produce just their variance sums.
 __global__ void k_icp_student(const InstDesc *D, int level, int pass) {
     INST_DESC;
     if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
@@ -667,10 +666,8 @@ __global__ void k_icp_student(const InstDesc *D, int level, int pass) {
         float sigma2 = var / (float)nsel;
         float r2 = d.icp_r2[i];
         float wv = 6 / (5 + r2 / sigma2);
-        if (pass == 3) wv = fminf(wv, 1.0f);
+        if (pass == 3) d.icp_w[i] = fminf(wv, 1.0f);
         else vsum = trunc_prod(r2, wv);
-        d.icp_w[i] = wv;
-        d.icp_pk_nrm[i].w = wv;
     }
     if (pass < 3) block_add_ll(&d.icp_var[pass], vsum);
 }
@@ -683,15 +680,25 @@ constexpr int kIterThreads = kIterBlock;  // one canonical lane (4 points of a c
 constexpr int kCluster = kIterCluster;
 constexpr int kFxTerms = 27 * kFxLimbs;
 
-struct IterShared {
+// 16-byte aligned: J is the destination of 16-byte cp.async copies
+struct __align__(16) IterShared {
     float T[16];
     long long fx[27][kFxLimbs];  // this CTA's fixed-point sums of its warp totals
     int fx_bad;
-    double A_ph[27], A_icp[27];
+    double A_ph[27];    // the allocation-free entry point's photometric terms
+    __align__(16) float J[6][kChunk];  // the photometric Jacobian of this CTA's first chunk
     int hist[256];      // this CTA's photometric histogram (read by its cluster)
     int hist_all[256];  // the instance's histogram
     int median;
-    int last;
+    SolveScratch S;     // the allocation-free entry point's solve
+};
+
+static_assert(alignof(IterShared) >= 16 && offsetof(IterShared, J) % 16 == 0 && (kChunk * sizeof(float)) % 16 == 0,
+              "cp.async destinations must be 16-byte aligned");
+
+struct SolveShared {
+    float T[16];
+    double A_ph[27], A_icp[27];
     SolveScratch S;
 };
 
@@ -710,30 +717,16 @@ __device__ __forceinline__ void fx_clear(IterShared &sh) {
     if (threadIdx.x == 0) sh.fx_bad = 0;
 }
 
-// A lane's running fixed-point sum of one term (the term whose warp totals the
-// lane receives from warp_terms).
-struct FxReg {
-    long long l0 = 0, l1 = 0, l2 = 0, l3 = 0;
-    int bad = 0;
-    __device__ __forceinline__ void add(float v) {
-        int k0;
-        long long lo, hi;
-        fx_split(v, k0, lo, hi, bad);  // k0 <= 2 for every in-range value
-        l0 += (k0 == 0) ? lo : 0;
-        l1 += (k0 == 1) ? lo : ((k0 == 0) ? hi : 0);
-        l2 += (k0 == 2) ? lo : ((k0 == 1) ? hi : 0);
-        l3 += (k0 == 2) ? hi : 0;
-    }
-    // adds lane q's sums (q < 27) into the CTA's
-    __device__ __forceinline__ void merge(IterShared &sh, int q) const {
-        unsigned long long *f = reinterpret_cast<unsigned long long *>(sh.fx[q]);
-        if (l0) atomicAdd(f + 0, (unsigned long long)l0);
-        if (l1) atomicAdd(f + 1, (unsigned long long)l1);
-        if (l2) atomicAdd(f + 2, (unsigned long long)l2);
-        if (l3) atomicAdd(f + 3, (unsigned long long)l3);
-        if (bad) sh.fx_bad = 1;
-    }
-};
+// Adds warp total v of term q (lane q of warp_terms) to the CTA's fixed-point
+// sums; the 8 warps of a CTA add to the same limbs with shared-memory atomics.
+__device__ __forceinline__ void fx_add_term(IterShared &sh, int q, float v) {
+    int k0, bad = 0;
+    long long lo, hi;
+    fx_split(v, k0, lo, hi, bad);
+    if (lo) atomicAdd(reinterpret_cast<unsigned long long *>(&sh.fx[q][k0]), (unsigned long long)lo);
+    if (hi) atomicAdd(reinterpret_cast<unsigned long long *>(&sh.fx[q][k0 + 1]), (unsigned long long)hi);
+    if (bad) sh.fx_bad = 1;
+}
 
 // Adds the CTA's fixed-point sums to the instance's (after a __syncthreads).
 __device__ __forceinline__ void fx_flush(const IterShared &sh, unsigned long long *dst, int *dst_bad) {
@@ -860,7 +853,6 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
     float s = mad_scale(sh.median, nb);
     const float *J = d.sel_J[level];
     int t = threadIdx.x, lane = t & 31;
-    FxReg F;
     for (int c = 0; c < P / kChunk; c++) {
         float acc[27];
 #pragma unroll
@@ -875,9 +867,8 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
             acc27(acc, jw, r * wv);
         }
         float v = warp_terms(acc);
-        if (lane < 27) F.add(v);
+        if (lane < 27) fx_add_term(sh, lane, v);
     }
-    if (lane < 27) F.merge(sh, lane);
     __syncthreads();
     if (threadIdx.x < 27) {
         long long L[kFxLimbs];
@@ -888,8 +879,8 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
 }
 
 // icpResidualIndexKernel2, rgb2gray.cu:323-390, for one point.  The selected
-// reference point and normal were packed in selection order by k_icp_compact,
-// with the Student-t weight in the normal's fourth lane.
+// reference point and normal were packed in selection order by k_icp_compact;
+// the Student-t weight is the last pass's.
 __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int level, int idx, int nsel, float *j,
                                           float &res) {
     res = 0.0f;
@@ -902,6 +893,7 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     float b = 0.5f * (a - 1.0f);
     float4 p = __ldg(d.icp_pk_pts + idx);
     float4 rn = __ldg(d.icp_pk_nrm + idx);
+    float weight = __ldg(d.icp_w + idx);
     float qx, qy, qz, cnx, cny, cnz;
     mul4(T, p.x, p.y, p.z, qx, qy, qz);
     rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
@@ -909,7 +901,6 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     float p2x = a * (K[0] * q2x + K[2]) + b;
     float p2y = a * (K[4] * q2y + K[5]) + b;
     if (!(p2x >= 0 && p2x < (w - 1) && p2y >= 0 && p2y < (h - 1))) return;
-    float weight = rn.w;
     int xdi = ftoi(p2x), ydi = ftoi(p2y);
     float fx = p2x - xdi, fy = p2y - ydi;
     int off2 = xdi + ydi * w;
@@ -960,12 +951,23 @@ __device__ __forceinline__ void photo_lane_residuals(const InstDesc &d, const fl
 // evaluates chunks rank, rank + 8, ...; the cluster adds its histograms
 // (histogram64.cu:115-145) through distributed shared memory, every CTA finds
 // the median bin (seekThreshold64Kernel, histogram64.cu:48-61) and weighs its
-// own points (generateWeights64Kernel, 79-94) into the lane's fixed-point sum.
+// own points (generateWeights64Kernel, 79-94) into the CTA's fixed-point sums.
 // Returns whether this CTA had a chunk.
-__device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int rank, FxReg &F) {
+__device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int rank) {
     int P = d.P, nph = P / kChunk, nb = d.hist_bins;
     int t = threadIdx.x, lane = t & 31;
     const float *J = d.sel_J[level];
+    // the first chunk's Jacobian does not depend on the pose: copy it to shared
+    // memory asynchronously while the residuals are evaluated
+    if (rank < nph) {
+        for (int k = t; k < 6 * (kChunk / 4); k += blockDim.x) {
+            int col = k / (kChunk / 4), q4 = k % (kChunk / 4);
+            const float *src = J + (size_t)col * P + rank * kChunk + 4 * q4;
+            unsigned int dst = (unsigned int)__cvta_generic_to_shared(&sh.J[col][4 * q4]);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
     for (int k = t; k < nb; k += blockDim.x) sh.hist[k] = 0;
     __syncthreads();
     float r0[4], zw0[4];
@@ -974,7 +976,10 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
         photo_lane_residuals(d, sh.T, level, c, t, r, zw);
 #pragma unroll
         for (int m = 0; m < 4; m++) {
-            atomicAdd(&sh.hist[mad_bin(r[m], nb)], 1);
+            // one shared-memory atomic per distinct bin of the warp
+            int bin = mad_bin(r[m], nb);
+            unsigned int peers = __match_any_sync(kFull, bin);
+            if ((t & 31) == __ffs(peers) - 1) atomicAdd(&sh.hist[bin], __popc(peers));
             if (c == rank) {
                 r0[m] = r[m];
                 zw0[m] = zw[m];
@@ -985,14 +990,7 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
             }
         }
     }
-    // the first chunk's Jacobian: its loads overlap the histogram exchange
-    float j0[4][6];
-    if (rank < nph) {
-#pragma unroll
-        for (int m = 0; m < 4; m++)
-#pragma unroll
-            for (int k = 0; k < 6; k++) j0[m][k] = __ldg(J + k * P + rank * kChunk + t + kLanes * m);
-    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
     cluster_arrive();
     cluster_wait();  // every CTA's histogram is complete
@@ -1023,7 +1021,7 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
                 r = r0[m];
                 zw = zw0[m];
 #pragma unroll
-                for (int k = 0; k < 6; k++) jv[k] = j0[m][k];
+                for (int k = 0; k < 6; k++) jv[k] = sh.J[k][t + kLanes * m];
             } else {
                 r = d.ph_r[i];  // written by this thread above
                 zw = d.ph_zw[i];
@@ -1037,7 +1035,7 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
             acc27(acc, jw, r * wv);
         }
         float v = warp_terms(acc);
-        if (lane < 27) F.add(v);
+        if (lane < 27) fx_add_term(sh, lane, v);
     }
     cluster_wait();
     return rank < nph;
@@ -1045,8 +1043,8 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
 
 // ICP chunks [c0, c1) of an instance: lane t evaluates points t + 256m of each
 // chunk (icpResidualIndexKernel2 and the reference's per-point Jacobian), the
-// warp totals of each chunk go into the lane's fixed-point sum.
-__device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0, int c1, int nsel, FxReg &F) {
+// warp totals of each chunk go into the CTA's fixed-point sums.
+__device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0, int c1, int nsel) {
     int t = threadIdx.x, lane = t & 31;
     for (int c = c0; c < c1; c++) {
         float acc[27];
@@ -1062,7 +1060,7 @@ __device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0,
             acc27(acc, jb, rb);
         }
         float v = warp_terms(acc);
-        if (lane < 27) F.add(v);
+        if (lane < 27) fx_add_term(sh, lane, v);
     }
 }
 
@@ -1071,13 +1069,13 @@ __device__ __forceinline__ int packed_index(int r, int c) {
     return a * 6 - (a * (a - 1)) / 2 + (b - a);
 }
 
-// Run by the CTA that completes an iteration of an instance: the accumulated
-// terms in FP64 (reset for the next iteration), the system of the mode (fused
-// in FP64 for BIOBJECTIVE with the weights precomputed off this path,
-// linearFuseKernel warp.cu:918-924), the solve and SE(3) update (warp 0), the
-// statistics and the optional trace.
-__device__ __noinline__ void finalize_iter(const InstDesc &d, IterShared &sh, int level, int it, bool use_ph,
-                                           bool use_icp, int nsel) {
+// The end of an iteration of an instance: the accumulated terms in FP64 (reset
+// for the next iteration), the system of the mode (fused in FP64 for
+// BIOBJECTIVE with weights precomputed off this path, linearFuseKernel
+// warp.cu:918-924), the solve and SE(3) update (warp 0), the statistics and
+// the optional trace.
+__device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh, int level, int it, bool use_ph,
+                                              bool use_icp, int nsel) {
     int t = threadIdx.x;
     SolveScratch &S = sh.S;
     if (t < 54) {
@@ -1120,8 +1118,8 @@ __device__ __noinline__ void finalize_iter(const InstDesc &d, IterShared &sh, in
         }
     }
     int median = use_ph ? __ldcg(d.ph_hist + 512) : -1;
-    if (tr && t >= 64) {
-        for (int k = t - 64; k < 256; k += blockDim.x - 64)
+    if (tr) {
+        for (int k = t; k < 256; k += blockDim.x)
             tr->hist[k] = (use_ph && k < d.hist_bins) ? __ldcg(d.ph_hist + 256 + k) : 0;
     }
     __syncthreads();
@@ -1154,78 +1152,80 @@ __device__ __noinline__ void finalize_iter(const InstDesc &d, IterShared &sh, in
             tr->median_bin = median;
         }
         if (d.trace) *d.trace_count = slot + 1;
-        *d.counter = 0u;
     }
 }
 
-// One GN iteration at `level`, iteration `it`, for every instance
-// (blockIdx.y).  blockIdx.x 0..7: the photometric cluster of the instance
-// (updateLinearSystem, phototracker.cpp:505-511); blockIdx.x = 8 + j: ICP
-// chunks [j K, (j+1) K) of 1024 correspondences, K = icp_per_cta
-// (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).  Every
-// participant adds its fixed-point sums to the instance's with integer atomics,
-// so the result does not depend on K or on the order in which CTAs finish; the
-// last to finish fuses (linearFuse, shapetracker.cpp:392-394), solves and
-// applies the SE(3) update (estimateIncrement, phototracker.cpp:646-664).  No
-// CTA waits for another outside its cluster barrier: completion is counted
-// with an atomic ticket.
+// Copies an instance descriptor (pointers, sizes, calibration) into shared
+// memory with one parallel load instead of a chain of dependent global loads.
+__device__ __forceinline__ void load_desc(InstDesc &sd, const InstDesc *src_desc) {
+    const int *src = reinterpret_cast<const int *>(src_desc);
+    int *dst = reinterpret_cast<int *>(&sd);
+    for (int k = threadIdx.x; k < (int)(sizeof(InstDesc) / sizeof(int)); k += blockDim.x) dst[k] = __ldg(src + k);
+}
+
+// The linearisation of one GN iteration at `level`, iteration `it`, for every
+// instance (blockIdx.y).  blockIdx.x 0..7: the photometric cluster of the
+// instance (updateLinearSystem, phototracker.cpp:505-511); blockIdx.x = 8 + j:
+// ICP chunks [j K, (j+1) K) of 1024 correspondences, K = icp_per_cta
+// (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).  Every CTA adds
+// its fixed-point sums to the instance's with integer atomics, so the result
+// does not depend on K or on the order in which CTAs finish; k_solve then
+// fuses, solves and updates the pose.
 #ifndef RECON_ITER_MIN_BLOCKS
-#define RECON_ITER_MIN_BLOCKS 3
+#define RECON_ITER_MIN_BLOCKS 4
 #endif
 __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads, RECON_ITER_MIN_BLOCKS)
     k_iter(const InstDesc *D, int level, int it, int icp_per_cta) {
-    INST_DESC;
+    __shared__ InstDesc sd;
+    load_desc(sd, D + blockIdx.y);
+    __syncthreads();
+    const InstDesc &d = sd;
     if (level >= d.L) return;
     if (it >= d.iters[d.L - 1 - level]) return;
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
-    int nsel = use_icp ? d.icp_nsel[level] : 0;
+    int nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
     int nchunks = (nsel + kChunk - 1) / kChunk;
     int nicp = (nchunks + icp_per_cta - 1) / icp_per_cta;
-    int nph = d.P / kChunk;
-    int expected = (use_ph ? min(nph, kCluster) : 0) + nicp;
     int role = blockIdx.x;
-    int set = -1;  // which sums this CTA adds to: 0 photometric, 1 ICP, -1 none
+    int set;  // which sums this CTA adds to: 0 photometric, 1 ICP
     if (role < kCluster) {
-        if (use_ph) {
-            set = 0;
-        } else {
-            // without a photometric term CTA 0 is a null participant when there
-            // is no ICP chunk either, so the iteration is still finalised
-            if (!(role == 0 && nchunks == 0)) return;
-            expected = 1;
-        }
-    } else if (role - kCluster >= nicp) {
-        return;
+        if (!use_ph) return;
+        set = 0;
     } else {
+        if (role - kCluster >= nicp) return;
         set = 1;
     }
     __shared__ IterShared sh;
     if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
     fx_clear(sh);
     __syncthreads();
-    FxReg F;
-    bool participant = true;
     if (set == 0) {
-        participant = photo_cluster(d, sh, level, role, F);
-    } else if (set == 1) {
+        if (!photo_cluster(d, sh, level, role)) return;
+    } else {
         int c0 = (role - kCluster) * icp_per_cta;
-        icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), nsel, F);
-    }
-    if (!participant) return;
-    int lane = threadIdx.x & 31;
-    if (set >= 0 && lane < 27) F.merge(sh, lane);
-    __syncthreads();
-    if (set >= 0) fx_flush(sh, d.fx + set * kFxTerms, d.fx_bad + set);
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned int ticket = atomicAdd(d.counter, 1u);
-        sh.last = (ticket == (unsigned)(expected - 1));
+        icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), nsel);
     }
     __syncthreads();
-    if (!sh.last) return;
-    __threadfence();
+    fx_flush(sh, d.fx + set * kFxTerms, d.fx_bad + set);
+}
+
+// The rest of a GN iteration, one CTA per instance after k_iter: the normal
+// equations from the fixed-point sums, fusion, solve and SE(3) update
+// (estimateIncrement, phototracker.cpp:646-664; linearFuse,
+// shapetracker.cpp:392-394).
+__global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int level, int it) {
+    __shared__ InstDesc sd;
+    load_desc(sd, D + blockIdx.x);
+    __syncthreads();
+    const InstDesc &d = sd;
+    if (level >= d.L) return;
+    if (it >= d.iters[d.L - 1 - level]) return;
+    bool use_ph = d.mode != RECON_GEOMETRIC;
+    bool use_icp = d.mode != RECON_PHOTOMETRIC;
+    int nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
+    __shared__ SolveShared sh;
+    if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
     finalize_iter(d, sh, level, it, use_ph, use_icp, nsel);
 }
 

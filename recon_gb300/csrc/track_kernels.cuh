@@ -15,7 +15,8 @@ constexpr int kSegments = 512;   // pixel-selection segments (filterIndex256.cu:
 constexpr int kVtxPlanes = 9;    // x y z px py gx gy gmag gray
 constexpr int kIterCluster = 8;  // CTAs of the photometric cluster of the GN iteration kernel
 constexpr int kIterBlock = 256;  // threads of a GN iteration CTA
-constexpr int kIterCtaSlots = 3 * 152;  // GN iteration CTAs resident on a 152-SM GB300
+constexpr int kIterCtaSlots = 4 * 152;  // GN iteration CTAs resident on a 152-SM GB300
+constexpr int kSolveThreads = 64;        // threads of the per-instance solve CTA
 constexpr int kFxLimbs = 4;      // limbs of a fixed-point sum (fx.cuh)
 
 enum StatSlot { ST_ITERS = 0, ST_SOLVES, ST_NONSPD, ST_STATUS, ST_MEDIAN, ST_ICPSEL0, ST_COUNT = 16 };
@@ -54,7 +55,7 @@ struct InstDesc {
     int *icp_select;         // W*H
     float *icp_r2, *icp_w;   // W*H
     float4 *icp_pk_pts;      // W*H: selected reference points in selection order (x y z mask)
-    float4 *icp_pk_nrm;      // W*H: their normals, .w = Student-t weight
+    float4 *icp_pk_nrm;      // W*H: their normals
     unsigned long long *icp_var;  // 4
     int *icp_nsel;           // kMaxLevels
     double *fuse_c2;         // kMaxLevels: lambda / (ICP correspondences) of the level
@@ -69,5 +70,8 @@ struct InstDesc {
     int trace_max;
     int *trace_count;
 };
+
+// k_iter copies a descriptor into shared memory as 32-bit words
+static_assert(sizeof(InstDesc) % sizeof(int) == 0, "InstDesc must be a whole number of words");
 
 }  // namespace rt
