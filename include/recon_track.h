@@ -147,6 +147,21 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
  * filterDepthIIRKernel (warp.cu:398-467, disabled), updateVoxelsKernel's
  * running mean (VoxelGrid_cuda.cu:1005-1013), KeyFrameModel::integrateDepthMaps
  * (KeyFrameModel.cpp:537-583, not compiled). */
+/* Learned initialisation (include/recon_initnet.h; no counterpart in the
+ * reference, which starts every frame from the previous frame's pose).  With a
+ * network attached, each tracked frame (recon_batch_track without a T_init,
+ * recon_batch_track_sequence) first predicts the motion from the previous
+ * frame (the keyframe for the first frame) to the current one, takes the
+ * predicted start pose where its coarse-level photometric residual is lower,
+ * and runs `iters` (coarse to fine) instead of each instance's own schedule.
+ * Frames must be uint8 / uint16 and a multiple of 80x60.  net = NULL restores
+ * the plain tracker and the configured schedules.  The network object must
+ * outlive its use by the batch. */
+typedef struct recon_initnet recon_initnet;
+int recon_batch_set_init_net(recon_batch *b, recon_initnet *net, const int32_t iters[RECON_MAX_LEVELS]);
+/* The last frame's gate decisions (1: learned start pose) and network outputs [n][6]. */
+int recon_batch_get_init(recon_batch *b, int32_t *choice, float *net_out);
+
 int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *const *depth, const float *T_host,
                               int32_t on_device, float gate_mm);
 

@@ -1496,6 +1496,44 @@ int orc_set_current(orc_tracker *t, const uint8_t *gray, const uint16_t *depth) 
     return 0;
 }
 
+/* The learned start pose (k_init_gate): x = net_out * scale (FP32), D =
+ * exp(A(x)) applied to the identity by orc_expm_update, candidate D * T; the
+ * candidate replaces T when its integer cost sum_i min(trunc(|r_i| * 1024),
+ * 1024) over the coarsest level's photometric residuals is strictly lower.
+ * Returns 1 when the candidate was taken. */
+static long long gate_cost(orc_tracker *t, const float *T) {
+    int L = t->L, layer = L - 1, P = t->P;
+    orc_interpolate_residual(P, t->sel_xyz, t->sel_I[layer], T, t->calib, layer, t->cur_gray[layer], t->W >> layer,
+                             t->H >> layer, t->cur_z, t->W, t->H, t->r, t->zw);
+    long long c = 0;
+    for (int i = 0; i < P; i++) {
+        float u = fabsf(t->r[i]) * 1024.0f;
+        c += (u >= 1024.0f || !(u == u)) ? 1024 : (long long)u;
+    }
+    return c;
+}
+
+int orc_init_gate(orc_tracker *t, const float net_out[6], const float scale[6]) {
+    float Dm[16], Tc[16];
+    for (int i = 0; i < 16; i++) Dm[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    double x[6];
+    for (int k = 0; k < 6; k++) x[k] = (double)(net_out[k] * scale[k]);
+    orc_expm_update(x, Dm, (double)t->cfg.opt_scale_out);
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++)
+            Tc[r * 4 + c] = Dm[r * 4 + 0] * t->T[0 * 4 + c] + Dm[r * 4 + 1] * t->T[1 * 4 + c] +
+                            Dm[r * 4 + 2] * t->T[2 * 4 + c] + Dm[r * 4 + 3] * t->T[3 * 4 + c];
+    long long c0 = gate_cost(t, t->T), c1 = gate_cost(t, Tc);
+    if (c1 < c0) {
+        memcpy(t->T, Tc, sizeof(Tc));
+        return 1;
+    }
+    return 0;
+}
+
+void orc_set_pose(orc_tracker *t, const float T[16]) { memcpy(t->T, T, sizeof(t->T)); }
+void orc_get_pose(orc_tracker *t, float T[16]) { memcpy(T, t->T, sizeof(t->T)); }
+
 static int padded_len(int n) { return ((n + ORC_CHUNK - 1) / ORC_CHUNK) * ORC_CHUNK; }
 
 /* PhotoTracker::gpuEstimateIncrement (phototracker.cpp:666-689) with

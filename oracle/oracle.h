@@ -145,6 +145,10 @@ int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0)
 int orc_set_current(orc_tracker *t, const uint8_t *gray, const uint16_t *depth);
 int orc_fuse_keyframe(orc_tracker *t, int nframes, const uint16_t *const *depth, const float *Tframes, float gate);
 int orc_track(orc_tracker *t, float *T, orc_iter_trace *trace, int max_trace);
+/* learned start pose gate (k_init_gate); 1 when the network's candidate was taken */
+int orc_init_gate(orc_tracker *t, const float net_out[6], const float scale[6]);
+void orc_set_pose(orc_tracker *t, const float T[16]);
+void orc_get_pose(orc_tracker *t, float T[16]);
 int orc_get_array(orc_tracker *t, const char *name, int level, void *dst, int64_t nbytes);
 int orc_n_icp_selected(orc_tracker *t, int level);
 

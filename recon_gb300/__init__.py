@@ -115,6 +115,8 @@ def lib() -> ctypes.CDLL:
             L.recon_batch_enable_trace.argtypes = [vp, i32]
             L.recon_batch_get_trace.argtypes = [vp, i32, vp, i32]
             L.recon_batch_get_array.argtypes = [vp, i32, ctypes.c_char_p, i32, vp, i64]
+            L.recon_batch_set_init_net.argtypes = [vp, vp, vp]
+            L.recon_batch_get_init.argtypes = [vp, vp, vp]
             L.recon_batch_get_array.restype = i64
             L.recon_calib_setup.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, i32, vp]
@@ -322,6 +324,24 @@ class Batch:
         buf = (IterTrace * max_iters)()
         n = check(lib().recon_batch_get_trace(self.h, inst, ctypes.cast(buf, ctypes.c_void_p), max_iters))
         return list(buf)[:n]
+
+    def set_init_net(self, net, iters=None):
+        """Attaches a learned initialisation network (recon_gb300.initnet.InitNet)
+        with schedule `iters` (coarse to fine); None detaches it."""
+        if net is None:
+            check(lib().recon_batch_set_init_net(self.h, None, None))
+            self._net = None
+            return
+        it = (ctypes.c_int32 * 4)(*(list(iters) + [0] * 4)[:4])
+        check(lib().recon_batch_set_init_net(self.h, net.h, ctypes.cast(it, ctypes.c_void_p)))
+        self._net = net  # keep it alive while attached
+
+    def init_choice(self):
+        """The last frame's learned start-pose decisions [n] and network outputs [n, 6]."""
+        ch = np.zeros(self.n, np.int32)
+        out = np.zeros((self.n, 6), np.float32)
+        check(lib().recon_batch_get_init(self.h, _ptr(ch), _ptr(out)))
+        return ch, out
 
     def get_array(self, inst: int, name: str, level: int, dtype, count: int) -> np.ndarray:
         out = np.zeros(count, dtype)

@@ -1,6 +1,6 @@
 """Builds librecon_track.so (sm_103a) in-tree with nvcc.
 
-Three translation units (kernels.cu, host.cu, refshim.cu) compiled in parallel and linked
+Four translation units (kernels.cu, host.cu, refshim.cu, initnet.cu) compiled in parallel and linked
 into recon_gb300/librecon_track.so.  -fmad=false keeps every floating-point
 multiply and add separately rounded (the bit-exactness contract of the
 kernels); -lineinfo keeps source lines for profiling.
@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librecon_track.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-UNITS = ["kernels.cu", "host.cu", "refshim.cu"]
+UNITS = ["kernels.cu", "host.cu", "refshim.cu", "initnet.cu"]
 HEADERS = ["scene.h", "fx.cuh", "solve.cuh", "track_kernels.cuh", "track_math.cuh"]
 
 
@@ -34,6 +34,7 @@ def _sources():
     srcs = [os.path.join(CSRC, u) for u in UNITS] + [os.path.join(CSRC, h) for h in HEADERS]
     srcs.append(os.path.join(ROOT, "include", "recon_track.h"))
     srcs.append(os.path.join(ROOT, "include", "recon_ref_shim.h"))
+    srcs.append(os.path.join(ROOT, "include", "recon_initnet.h"))
     srcs.append(os.path.abspath(__file__))
     return srcs
 

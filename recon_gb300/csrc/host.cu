@@ -13,6 +13,9 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
+
+#include "../../include/recon_initnet.h"
 #include "scene.h"
 #include "track_kernels.cuh"
 
@@ -41,7 +44,15 @@ __global__ void k_store_pose(const InstDesc *D, float *dst);
 __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const uint16_t *const *depth,
                              const float *Tf, float gate, const int *active);
 __global__ void k_ref_from_z(const InstDesc *D, const int *active);
+__global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
+                             __nv_bfloat16 *out);
+__global__ void k_init_gate(const InstDesc *D, const float *net_out, const float *scale, int *choice);
 }  // namespace rt
+
+namespace nn {
+int forward_on(recon_initnet *net, const uint16_t *in_bf16, int n, float *out, cudaStream_t s);
+const float *scale_dev(recon_initnet *net);
+}  // namespace nn
 
 using namespace rt;
 
@@ -147,6 +158,14 @@ struct recon_batch {
     // host pose bookkeeping for the single-tracker API (applyIncrement)
     double global_pose[16];
     float T_prev[16];
+    // learned initialisation (recon_batch_set_init_net)
+    recon_initnet *net = nullptr;
+    uint16_t *d_coarse[2] = {nullptr, nullptr};  // coarse images [n][60][80][2] BF16: previous / current frame
+    int coarse_prev = 0;
+    uint16_t *d_netin = nullptr;  // [n][60][80][4]
+    float *d_netout = nullptr;    // [n][6]
+    int *d_choice = nullptr;      // [n]: 1 where the learned start pose was taken
+    std::vector<std::vector<int>> plain_iters;  // schedules restored when the network is detached
 };
 
 namespace {
@@ -482,6 +501,41 @@ int run_schedule(recon_batch *b) {
     return RECON_OK;
 }
 
+// Learned start poses for the frame whose uint8 / uint16 inputs the pointer
+// table `row` (gray pointers, then depth pointers) holds: coarse image, network
+// on (previous, current), gate.  The current coarse image becomes the previous.
+int learned_start(recon_batch *b, const void **row) {
+    int n = b->n;
+    int cur = 1 - b->coarse_prev;
+    k_net_coarse<<<dim3((kNetW * kNetH + 255) / 256, n), 256, 0, b->stream>>>(
+        b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n), (__nv_bfloat16 *)b->d_coarse[cur]);
+    g_launches += 1;
+    int rc = recon_initnet_pair(b->d_coarse[b->coarse_prev], b->d_coarse[cur], n, b->d_netin, b->stream);
+    if (rc) return rc;
+    g_launches += 1;
+    rc = nn::forward_on(b->net, b->d_netin, n, b->d_netout, b->stream);
+    if (rc) return rc;
+    g_launches += 8;  // six convolutions, pooling + linear layer, output copy
+    k_init_gate<<<n, 256, 0, b->stream>>>(b->d_desc, b->d_netout, nn::scale_dev(b->net), b->d_choice);
+    g_launches += 1;
+    b->coarse_prev = cur;
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
+// coarse image of the keyframe: the "previous frame" of the first tracked frame
+int learned_keyframe(recon_batch *b) {
+    if (!b->net) return RECON_OK;
+    int n = b->n;
+    const void **row = b->d_inptr;
+    k_net_coarse<<<dim3((kNetW * kNetH + 255) / 256, n), 256, 0, b->stream>>>(
+        b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n),
+        (__nv_bfloat16 *)b->d_coarse[b->coarse_prev]);
+    g_launches += 1;
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
 int upload_desc(recon_batch *b) {
     CK(cudaMemcpyAsync(b->d_desc, b->desc.data(), b->n * sizeof(InstDesc), cudaMemcpyHostToDevice, b->stream));
     CK(cudaStreamSynchronize(b->stream));
@@ -697,6 +751,11 @@ int recon_batch_destroy(recon_batch *b) {
         cudaEventDestroy(ev.second.second);
     }
     for (cudaEvent_t e : b->event_pool) cudaEventDestroy(e);
+    for (int k = 0; k < 2; k++)
+        if (b->d_coarse[k]) cudaFree(b->d_coarse[k]);
+    if (b->d_netin) cudaFree(b->d_netin);
+    if (b->d_netout) cudaFree(b->d_netout);
+    if (b->d_choice) cudaFree(b->d_choice);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RECON_OK;
@@ -711,6 +770,8 @@ int recon_batch_set_reference(recon_batch *b, const uint8_t *const *gray, const 
     int rc = stage_inputs(b, gray, depth, nullptr, on_device);
     if (rc) return rc;
     rc = prepare_reference(b);
+    if (rc) return rc;
+    rc = learned_keyframe(b);
     if (rc) return rc;
     CK(cudaStreamSynchronize(b->stream));
     b->have_ref = true;
@@ -766,6 +827,10 @@ int recon_batch_track_async(recon_batch *b, const float *T_init_host) {
     k_begin_track<<<dim3(1, b->n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, T_init_host ? 1 : 0);
     g_launches += 1;
     CK(cudaGetLastError());
+    if (b->net && !T_init_host) {
+        int rc = learned_start(b, b->d_inptr);
+        if (rc) return rc;
+    }
     return run_schedule(b);
 }
 
@@ -1050,6 +1115,10 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         if (!on_device) CK(cudaEventRecord(b->ev_free[f & 1], b->stream));
         k_begin_track<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, 0);
         g_launches += 1;
+        if (b->net) {
+            rc = learned_start(b, row);
+            if (rc) return rc;
+        }
         rc = run_schedule(b);
         if (rc) return rc;
         k_store_pose<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tseq + (size_t)f * n * 16);
@@ -1059,6 +1128,70 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     b->have_cur = true;
     if (T_out) CK(cudaMemcpyAsync(T_out, b->d_Tseq, need_T * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
     return recon_batch_get_poses(b, nullptr, stats);
+}
+
+int recon_batch_set_init_net(recon_batch *b, recon_initnet *net, const int32_t iters[RECON_MAX_LEVELS]) {
+    clear_stale_error();
+    if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
+    int n = b->n;
+    if (!net) {
+        if (b->net) {
+            for (int i = 0; i < n; i++) {
+                for (int l = 0; l < kMaxLevels; l++) {
+                    b->cfg[i].iters[l] = b->plain_iters[i][l];
+                    b->desc[i].iters[l] = b->plain_iters[i][l];
+                }
+            }
+        }
+        b->net = nullptr;
+        b->graph_dirty = true;
+        return upload_desc(b);
+    }
+    if (!iters) return fail(RECON_ERR_INVALID_ARG, "null schedule");
+    for (int i = 0; i < n; i++) {
+        const recon_config &c = b->cfg[i];
+        if (c.width % kNetW || c.height % kNetH)
+            return fail(RECON_ERR_INVALID_ARG, "the learned initialisation needs frames of a multiple of 80x60");
+        recon_config t = c;
+        for (int l = 0; l < RECON_MAX_LEVELS; l++) t.iters[l] = iters[l];
+        int rc = validate(t);
+        if (rc) return rc;
+    }
+    if (!b->d_netin) {
+        size_t px = (size_t)n * kNetW * kNetH;
+        for (int k = 0; k < 2; k++) CK(cudaMalloc(&b->d_coarse[k], px * 2 * sizeof(uint16_t)));
+        CK(cudaMalloc(&b->d_netin, px * 4 * sizeof(uint16_t)));
+        CK(cudaMalloc(&b->d_netout, (size_t)n * 6 * sizeof(float)));
+        CK(cudaMalloc(&b->d_choice, (size_t)n * sizeof(int)));
+        CK(cudaMemsetAsync(b->d_coarse[0], 0, px * 2 * sizeof(uint16_t), b->stream));
+        CK(cudaMemsetAsync(b->d_coarse[1], 0, px * 2 * sizeof(uint16_t), b->stream));
+    }
+    if (!b->net) {
+        b->plain_iters.assign(n, std::vector<int>(kMaxLevels));
+        for (int i = 0; i < n; i++)
+            for (int l = 0; l < kMaxLevels; l++) b->plain_iters[i][l] = b->cfg[i].iters[l];
+    }
+    for (int i = 0; i < n; i++)
+        for (int l = 0; l < kMaxLevels; l++) {
+            b->cfg[i].iters[l] = iters[l];
+            b->desc[i].iters[l] = iters[l];
+        }
+    b->net = net;
+    b->graph_dirty = true;
+    int rc = upload_desc(b);
+    if (rc) return rc;
+    if (b->have_ref) return learned_keyframe(b);
+    return RECON_OK;
+}
+
+int recon_batch_get_init(recon_batch *b, int32_t *choice, float *net_out) {
+    clear_stale_error();
+    if (!b || !b->net) return fail(RECON_ERR_STATE, "no network attached");
+    if (choice) CK(cudaMemcpyAsync(choice, b->d_choice, (size_t)b->n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    if (net_out)
+        CK(cudaMemcpyAsync(net_out, b->d_netout, (size_t)b->n * 6 * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return RECON_OK;
 }
 
 int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *const *depth, const float *T_host,

@@ -1,0 +1,601 @@
+// initnet.cu -- the learned initialisation network (include/recon_initnet.h):
+// BF16 tensor-core convolutions (mma.sync m16n8k16, FP32 accumulation) for the
+// forward pass, FP32 CUDA-core kernels for the backward pass and Adam.
+//
+// Every kernel reduces in a fixed order (no floating-point atomics), so a
+// training run is deterministic.  The shapes are small (about 10 MFLOP per
+// sample): one warp computes a 16-pixel by Cout output tile directly from the
+// NHWC input (implicit GEMM, no im2col buffer).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <math.h>
+
+#include <string>
+
+#include "../../include/recon_initnet.h"
+#include "../../include/recon_track.h"
+
+namespace rt {
+void set_last_error(const char *msg);
+}
+
+namespace nn {
+
+constexpr int kLayers = 6;
+constexpr int kCin[kLayers] = {4, 16, 32, 64, 64, 128};
+constexpr int kCout[kLayers] = {16, 32, 64, 64, 128, 128};
+constexpr int kHt[kLayers + 1] = {60, 30, 15, 8, 4, 2, 1};
+constexpr int kWd[kLayers + 1] = {80, 40, 20, 10, 5, 3, 2};
+constexpr int kFeat = 128;
+constexpr int kOut = RECON_NET_OUT;
+constexpr int kMaxSplit = 256;
+
+constexpr int kpad(int cin) { return (9 * cin + 15) / 16 * 16; }
+
+struct Offsets {
+    int64_t w[kLayers], b[kLayers], wfc, bfc, scale, total;
+};
+
+Offsets offsets() {
+    Offsets o;
+    int64_t p = 0;
+    for (int l = 0; l < kLayers; l++) {
+        o.w[l] = p;
+        p += (int64_t)kCout[l] * kpad(kCin[l]);
+        o.b[l] = p;
+        p += kCout[l];
+    }
+    o.wfc = p;
+    p += (int64_t)kOut * kFeat;
+    o.bfc = p;
+    p += kOut;
+    o.scale = p;
+    p += kOut;
+    o.total = p;
+    return o;
+}
+
+__device__ __forceinline__ float bf(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+
+// out[m][co] = relu(bias[co] + sum_k A[m][k] W[co][k]) with A the 3x3 / stride 2
+// / pad 1 patches of `in` (k = tap * Cin + c); one warp per 16 output pixels.
+template <int COUT>
+__global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16 *in, int N, int H, int W, int Cin, int Kp,
+                                                  const __nv_bfloat16 *w, const float *bias, __nv_bfloat16 *out,
+                                                  int Ho, int Wo) {
+    int lane = threadIdx.x & 31;
+    long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    long long M = (long long)N * Ho * Wo;
+    long long m0 = warp * 16;
+    if (m0 >= M) return;
+    int g = lane >> 2, tig = lane & 3;
+    long long rr[2] = {m0 + g, m0 + g + 8};
+    bool rv[2];
+    int rn[2], ry[2], rx[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        rv[h] = rr[h] < M;
+        long long mm = rv[h] ? rr[h] : 0;
+        rx[h] = (int)(mm % Wo);
+        ry[h] = (int)((mm / Wo) % Ho);
+        rn[h] = (int)(mm / ((long long)Wo * Ho));
+    }
+    float acc[COUT / 8][4];
+#pragma unroll
+    for (int f = 0; f < COUT / 8; f++) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
+    int K = 9 * Cin;
+    for (int kb = 0; kb < Kp; kb += 16) {
+        // A fragment: a0 (row g, k 2t..2t+1), a1 (row g+8), a2 (row g, k+8), a3 (row g+8, k+8)
+        uint32_t a[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int h = q & 1;
+            int k = kb + 2 * tig + ((q >> 1) ? 8 : 0);
+            uint32_t v = 0;
+            if (rv[h] && k < K) {
+                int tap = k / Cin, c = k - tap * Cin;
+                int ky = tap / 3, kx = tap - ky * 3;
+                int iy = 2 * ry[h] - 1 + ky, ix = 2 * rx[h] - 1 + kx;
+                if (iy >= 0 && iy < H && ix >= 0 && ix < W)
+                    v = *reinterpret_cast<const uint32_t *>(in + (((long long)rn[h] * H + iy) * W + ix) * Cin + c);
+            }
+            a[q] = v;
+        }
+#pragma unroll
+        for (int f = 0; f < COUT / 8; f++) {
+            // B fragment: b0 (k 2t..2t+1, n g), b1 (k + 8)
+            const __nv_bfloat16 *wr = w + (long long)(f * 8 + g) * Kp + kb + 2 * tig;
+            uint32_t b0 = *reinterpret_cast<const uint32_t *>(wr);
+            uint32_t b1 = *reinterpret_cast<const uint32_t *>(wr + 8);
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                "{%0,%1,%2,%3};\n"
+                : "+f"(acc[f][0]), "+f"(acc[f][1]), "+f"(acc[f][2]), "+f"(acc[f][3])
+                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+        }
+    }
+    // C fragment: c0 c1 (row g, cols 2t, 2t+1), c2 c3 (row g+8)
+#pragma unroll
+    for (int f = 0; f < COUT / 8; f++) {
+        int col = f * 8 + 2 * tig;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (!rv[h]) continue;
+            float v0 = acc[f][2 * h] + bias[col], v1 = acc[f][2 * h + 1] + bias[col + 1];
+            v0 = v0 > 0.0f ? v0 : 0.0f;
+            v1 = v1 > 0.0f ? v1 : 0.0f;
+            __nv_bfloat162 pr = __floats2bfloat162_rn(v0, v1);
+            *reinterpret_cast<__nv_bfloat162 *>(out + rr[h] * COUT + col) = pr;
+        }
+    }
+}
+
+// global average pooling of the last activation and the linear layer; one CTA
+// (kFeat threads) per sample
+__global__ void k_head_fwd(const __nv_bfloat16 *a6, int P, const float *wfc, const float *bfc, float *feat, float *y) {
+    __shared__ float f[kFeat];
+    int n = blockIdx.x, c = threadIdx.x;
+    float s = 0.0f;
+    for (int p = 0; p < P; p++) s += bf(a6 + ((long long)n * P + p) * kFeat + c);
+    s = s / (float)P;
+    f[c] = s;
+    feat[(long long)n * kFeat + c] = s;
+    __syncthreads();
+    if (c < kOut) {
+        float v = bfc[c];
+        for (int k = 0; k < kFeat; k++) v += wfc[c * kFeat + k] * f[k];
+        y[(long long)n * kOut + c] = v;
+    }
+}
+
+// loss, and the gradients of the linear layer (one CTA of kOut*kFeat threads)
+__global__ void k_head_grad(const float *y, const float *t, const float *feat, int N, float *gwfc, float *gbfc,
+                            float *loss) {
+    int i = threadIdx.x;  // j * kFeat + c
+    int j = i / kFeat, c = i % kFeat;
+    float inv = 2.0f / (float)(kOut * N);
+    float s = 0.0f, sb = 0.0f;
+    for (int n = 0; n < N; n++) {
+        float dy = (y[n * kOut + j] - t[n * kOut + j]) * inv;
+        s += dy * feat[(long long)n * kFeat + c];
+        sb += dy;
+    }
+    gwfc[i] = s;
+    if (c == 0) gbfc[j] = sb;
+    if (i == 0) {
+        float l = 0.0f;
+        for (int n = 0; n < N; n++)
+            for (int k = 0; k < kOut; k++) {
+                float d = y[n * kOut + k] - t[n * kOut + k];
+                l += d * d;
+            }
+        *loss = l / (float)(kOut * N);
+    }
+}
+
+// gradient at the last convolution's pre-activation: d feat / P through the
+// pooling, masked by the ReLU
+__global__ void k_head_back(const float *y, const float *t, const float *wfc, const __nv_bfloat16 *a6, int N, int P,
+                            float *dz6) {
+    int n = blockIdx.x, c = threadIdx.x;
+    float inv = 2.0f / (float)(kOut * N);
+    float df = 0.0f;
+    for (int j = 0; j < kOut; j++) df += wfc[j * kFeat + c] * ((y[n * kOut + j] - t[n * kOut + j]) * inv);
+    df = df / (float)P;
+    for (int p = 0; p < P; p++) {
+        long long o = ((long long)n * P + p) * kFeat + c;
+        dz6[o] = bf(a6 + o) > 0.0f ? df : 0.0f;
+    }
+}
+
+// weight and bias gradients of a convolution, split over the output pixels:
+// partial[s][co][k] for k < Kp (k = Kp: the bias)
+__global__ void k_conv_wgrad(const float *dz, const __nv_bfloat16 *in, int N, int H, int W, int Cin, int Kp, int Cout,
+                             int Ho, int Wo, int nsplit, float *partial) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = blockIdx.y;
+    int row = Kp + 1;
+    if (idx >= Cout * row) return;
+    int co = idx / row, k = idx % row;
+    long long M = (long long)N * Ho * Wo;
+    long long per = (M + nsplit - 1) / nsplit;
+    long long mb = per * s, me = mb + per < M ? mb + per : M;
+    float acc = 0.0f;
+    if (k == Kp) {
+        for (long long m = mb; m < me; m++) acc += dz[m * Cout + co];
+    } else if (k < 9 * Cin) {
+        int tap = k / Cin, c = k - tap * Cin;
+        int ky = tap / 3, kx = tap - ky * 3;
+        for (long long m = mb; m < me; m++) {
+            int ox = (int)(m % Wo), oy = (int)((m / Wo) % Ho), n = (int)(m / ((long long)Wo * Ho));
+            int iy = 2 * oy - 1 + ky, ix = 2 * ox - 1 + kx;
+            if (iy >= 0 && iy < H && ix >= 0 && ix < W)
+                acc += dz[m * Cout + co] * bf(in + (((long long)n * H + iy) * W + ix) * Cin + c);
+        }
+    }
+    partial[((long long)s * Cout + co) * row + k] = acc;
+}
+
+// sums the splits in order into the flat gradient (weights, then the bias)
+__global__ void k_wgrad_reduce(const float *partial, int nsplit, int Cout, int Kp, float *gw, float *gb) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    int row = Kp + 1;
+    if (idx >= Cout * row) return;
+    float s = 0.0f;
+    for (int q = 0; q < nsplit; q++) s += partial[(long long)q * Cout * row + idx];
+    int co = idx / row, k = idx % row;
+    if (k == Kp) gb[co] = s;
+    else gw[co * Kp + k] = s;
+}
+
+// gradient at the previous layer's pre-activation: the transposed convolution
+// of dz, masked by that layer's ReLU output a_prev
+__global__ void k_conv_dgrad(const float *dz, const __nv_bfloat16 *w, const __nv_bfloat16 *a_prev, int N, int H, int W,
+                             int Cin, int Kp, int Cout, int Ho, int Wo, float *dz_prev) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long tot = (long long)N * H * W * Cin;
+    if (idx >= tot) return;
+    int c = (int)(idx % Cin);
+    long long pix = idx / Cin;
+    int x = (int)(pix % W), y = (int)((pix / W) % H), n = (int)(pix / ((long long)W * H));
+    if (!(bf(a_prev + idx) > 0.0f)) {
+        dz_prev[idx] = 0.0f;
+        return;
+    }
+    float acc = 0.0f;
+    for (int ky = 0; ky < 3; ky++) {
+        int ty = y + 1 - ky;
+        if (ty < 0 || (ty & 1)) continue;
+        int oy = ty >> 1;
+        if (oy >= Ho) continue;
+        for (int kx = 0; kx < 3; kx++) {
+            int tx = x + 1 - kx;
+            if (tx < 0 || (tx & 1)) continue;
+            int ox = tx >> 1;
+            if (ox >= Wo) continue;
+            int k = (ky * 3 + kx) * Cin + c;
+            const float *d = dz + (((long long)n * Ho + oy) * Wo + ox) * Cout;
+            for (int co = 0; co < Cout; co++) acc += bf(w + (long long)co * Kp + k) * d[co];
+        }
+    }
+    dz_prev[idx] = acc;
+}
+
+__global__ void k_adam(float *p, const float *g, float *m, float *v, int64_t n, float lr, float bc1, float bc2) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    float gi = g[i];
+    float mi = b1 * m[i] + (1.0f - b1) * gi;
+    float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+__global__ void k_to_bf16(const float *p, __nv_bfloat16 *q, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = __float2bfloat16_rn(p[i]);
+}
+
+__global__ void k_coarse(const uint8_t *gray, const uint16_t *depth, int n, int W, int H, __nv_bfloat16 *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int per = RECON_NET_W * RECON_NET_H;
+    if (i >= n * per) return;
+    int f = i / per, p = i % per;
+    int ox = p % RECON_NET_W, oy = p / RECON_NET_W;
+    int bx = W / RECON_NET_W, by = H / RECON_NET_H;
+    const uint8_t *g = gray + (long long)f * W * H;
+    const uint16_t *dp = depth + (long long)f * W * H;
+    int gs = 0, cnt = 0;
+    long long ds = 0;
+    for (int y = 0; y < by; y++)
+        for (int x = 0; x < bx; x++) {
+            long long o = (long long)(oy * by + y) * W + ox * bx + x;
+            gs += g[o];
+            int dv = dp[o];
+            if (dv) {
+                ds += dv;
+                cnt++;
+            }
+        }
+    float gv = (float)gs / (255.0f * (float)(bx * by));
+    float dv = cnt ? ((float)ds / (float)cnt) / 4000.0f : 0.0f;
+    out[2 * (long long)i] = __float2bfloat16_rn(gv);
+    out[2 * (long long)i + 1] = __float2bfloat16_rn(dv);
+}
+
+__global__ void k_pair(const __nv_bfloat16 *prev, const __nv_bfloat16 *cur, int n, __nv_bfloat16 *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int per = RECON_NET_W * RECON_NET_H;
+    if (i >= n * per) return;
+    out[4 * (long long)i + 0] = prev[2 * (long long)i];
+    out[4 * (long long)i + 1] = prev[2 * (long long)i + 1];
+    out[4 * (long long)i + 2] = cur[2 * (long long)i];
+    out[4 * (long long)i + 3] = cur[2 * (long long)i + 1];
+}
+
+}  // namespace nn
+
+using namespace nn;
+
+struct recon_initnet {
+    int max_batch = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    Offsets off;
+    float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *pbf = nullptr;
+    __nv_bfloat16 *act[kLayers] = {nullptr};
+    float *dz[kLayers] = {nullptr};
+    float *feat = nullptr, *y = nullptr, *partial = nullptr, *loss = nullptr;
+    int64_t partial_floats = 0;
+    int64_t step = 0;
+};
+
+namespace {
+
+int net_fail(int code, const std::string &msg) {
+    rt::set_last_error(msg.c_str());
+    return code;
+}
+
+#define NCK(call)                                                                                    \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return net_fail(RECON_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int64_t act_count(int l, int n) { return (int64_t)n * kHt[l + 1] * kWd[l + 1] * kCout[l]; }
+
+int nsplit_for(int l, int n) {
+    long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
+    long long s = M / 512;
+    return (int)(s < 1 ? 1 : (s > kMaxSplit ? kMaxSplit : s));
+}
+
+int conv_forward(recon_initnet *net, int l, const __nv_bfloat16 *in, int n) {
+    int Cin = kCin[l], Cout = kCout[l], Kp = kpad(Cin);
+    long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
+    int warps = (int)((M + 15) / 16);
+    dim3 grid((warps * 32 + 127) / 128);
+    const __nv_bfloat16 *w = net->pbf + net->off.w[l];
+    const float *b = net->params + net->off.b[l];
+    int H = kHt[l], W = kWd[l], Ho = kHt[l + 1], Wo = kWd[l + 1];
+    switch (Cout) {
+        case 16: k_conv_fwd<16><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+        case 32: k_conv_fwd<32><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+        case 64: k_conv_fwd<64><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+        default: k_conv_fwd<128><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+    }
+    return RECON_OK;
+}
+
+int forward(recon_initnet *net, const __nv_bfloat16 *in, int n) {
+    const __nv_bfloat16 *x = in;
+    for (int l = 0; l < kLayers; l++) {
+        conv_forward(net, l, x, n);
+        x = net->act[l];
+    }
+    int P = kHt[kLayers] * kWd[kLayers];
+    k_head_fwd<<<n, kFeat, 0, net->stream>>>(net->act[kLayers - 1], P, net->params + net->off.wfc,
+                                             net->params + net->off.bfc, net->feat, net->y);
+    NCK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int backward(recon_initnet *net, const __nv_bfloat16 *in, const float *target, int n, float *grad, float *loss) {
+    int P = kHt[kLayers] * kWd[kLayers];
+    k_head_grad<<<1, kOut * kFeat, 0, net->stream>>>(net->y, target, net->feat, n, grad + net->off.wfc,
+                                                    grad + net->off.bfc, loss);
+    k_head_back<<<n, kFeat, 0, net->stream>>>(net->y, target, net->params + net->off.wfc, net->act[kLayers - 1], n, P,
+                                              net->dz[kLayers - 1]);
+    for (int l = kLayers - 1; l >= 0; l--) {
+        int Cin = kCin[l], Cout = kCout[l], Kp = kpad(Cin);
+        int H = kHt[l], W = kWd[l], Ho = kHt[l + 1], Wo = kWd[l + 1];
+        const __nv_bfloat16 *lin = l ? net->act[l - 1] : in;
+        int ns = nsplit_for(l, n);
+        int row = Kp + 1;
+        dim3 g1((Cout * row + 127) / 128, ns);
+        k_conv_wgrad<<<g1, 128, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Cout, Ho, Wo, ns, net->partial);
+        k_wgrad_reduce<<<(Cout * row + 127) / 128, 128, 0, net->stream>>>(net->partial, ns, Cout, Kp,
+                                                                           grad + net->off.w[l], grad + net->off.b[l]);
+        if (l > 0) {
+            long long tot = (long long)n * H * W * Cin;
+            k_conv_dgrad<<<(unsigned)((tot + 255) / 256), 256, 0, net->stream>>>(
+                net->dz[l], net->pbf + net->off.w[l], net->act[l - 1], n, H, W, Cin, Kp, Cout, Ho, Wo, net->dz[l - 1]);
+        }
+    }
+    NCK(cudaMemsetAsync(grad + net->off.scale, 0, kOut * sizeof(float), net->stream));
+    NCK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int check_batch(recon_initnet *net, int n) {
+    if (!net) return net_fail(RECON_ERR_INVALID_ARG, "null network");
+    if (n <= 0 || n > net->max_batch) return net_fail(RECON_ERR_INVALID_ARG, "batch size outside 1..max_batch");
+    return RECON_OK;
+}
+
+void refresh_bf16(recon_initnet *net) {
+    int64_t tot = net->off.total;
+    k_to_bf16<<<(unsigned)((tot + 255) / 256), 256, 0, net->stream>>>(net->params, net->pbf, tot);
+}
+
+}  // namespace
+
+namespace nn {
+// forward pass on another stream (the tracker's), output to `out` [n][6]
+int forward_on(recon_initnet *net, const uint16_t *in_bf16, int n, float *out, cudaStream_t s) {
+    int rc = check_batch(net, n);
+    if (rc) return rc;
+    cudaStream_t keep = net->stream;
+    net->stream = s;
+    rc = forward(net, reinterpret_cast<const __nv_bfloat16 *>(in_bf16), n);
+    if (!rc && cudaMemcpyAsync(out, net->y, (int64_t)n * kOut * 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        rc = net_fail(RECON_ERR_CUDA, "initnet output copy");
+    net->stream = keep;
+    return rc;
+}
+const float *scale_dev(recon_initnet *net) { return net->params + net->off.scale; }
+}  // namespace nn
+
+extern "C" {
+
+int64_t recon_initnet_param_count(void) { return offsets().total; }
+
+int recon_initnet_create(int32_t max_batch, void *stream, recon_initnet **out) {
+    if (!out || max_batch <= 0) return net_fail(RECON_ERR_INVALID_ARG, "bad argument");
+    *out = nullptr;
+    recon_initnet *net = new recon_initnet();
+    net->max_batch = max_batch;
+    net->off = offsets();
+    net->stream = (cudaStream_t)stream;  // NULL: the legacy default stream
+    int64_t P = net->off.total;
+    int64_t part = 0;
+    for (int l = 0; l < kLayers; l++) {
+        int64_t s = (int64_t)nsplit_for(l, max_batch) * kCout[l] * (kpad(kCin[l]) + 1);
+        if (s > part) part = s;
+    }
+    net->partial_floats = part;
+    bool ok = cudaMalloc(&net->params, P * 4) == cudaSuccess && cudaMalloc(&net->grad, P * 4) == cudaSuccess &&
+              cudaMalloc(&net->m, P * 4) == cudaSuccess && cudaMalloc(&net->v, P * 4) == cudaSuccess &&
+              cudaMalloc(&net->pbf, P * 2) == cudaSuccess &&
+              cudaMalloc(&net->feat, (int64_t)max_batch * kFeat * 4) == cudaSuccess &&
+              cudaMalloc(&net->y, (int64_t)max_batch * kOut * 4) == cudaSuccess &&
+              cudaMalloc(&net->partial, part * 4) == cudaSuccess && cudaMalloc(&net->loss, 16) == cudaSuccess;
+    for (int l = 0; ok && l < kLayers; l++) {
+        ok = cudaMalloc(&net->act[l], act_count(l, max_batch) * 2) == cudaSuccess &&
+             cudaMalloc(&net->dz[l], act_count(l, max_batch) * 4) == cudaSuccess;
+    }
+    if (!ok) {
+        recon_initnet_destroy(net);
+        return net_fail(RECON_ERR_CUDA, "cudaMalloc(initnet)");
+    }
+    cudaMemsetAsync(net->params, 0, P * 4, net->stream);
+    cudaMemsetAsync(net->m, 0, P * 4, net->stream);
+    cudaMemsetAsync(net->v, 0, P * 4, net->stream);
+    cudaMemsetAsync(net->grad, 0, P * 4, net->stream);
+    refresh_bf16(net);
+    if (cudaStreamSynchronize(net->stream) != cudaSuccess) {
+        recon_initnet_destroy(net);
+        return net_fail(RECON_ERR_CUDA, "initnet set-up");
+    }
+    *out = net;
+    return RECON_OK;
+}
+
+int recon_initnet_destroy(recon_initnet *net) {
+    if (!net) return RECON_OK;
+    if (net->stream) cudaStreamSynchronize(net->stream);
+    cudaFree(net->params);
+    cudaFree(net->grad);
+    cudaFree(net->m);
+    cudaFree(net->v);
+    cudaFree(net->pbf);
+    cudaFree(net->feat);
+    cudaFree(net->y);
+    cudaFree(net->partial);
+    cudaFree(net->loss);
+    for (int l = 0; l < kLayers; l++) {
+        cudaFree(net->act[l]);
+        cudaFree(net->dz[l]);
+    }
+    if (net->own_stream) cudaStreamDestroy(net->stream);
+    delete net;
+    return RECON_OK;
+}
+
+int recon_initnet_set_params(recon_initnet *net, const float *params, int32_t on_device) {
+    if (!net || !params) return net_fail(RECON_ERR_INVALID_ARG, "null argument");
+    (void)cudaGetLastError();
+    NCK(cudaMemcpyAsync(net->params, params, net->off.total * 4,
+                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, net->stream));
+    NCK(cudaMemsetAsync(net->m, 0, net->off.total * 4, net->stream));
+    NCK(cudaMemsetAsync(net->v, 0, net->off.total * 4, net->stream));
+    net->step = 0;
+    refresh_bf16(net);
+    NCK(cudaStreamSynchronize(net->stream));
+    return RECON_OK;
+}
+
+int recon_initnet_get_params(recon_initnet *net, float *params_host) {
+    if (!net || !params_host) return net_fail(RECON_ERR_INVALID_ARG, "null argument");
+    (void)cudaGetLastError();
+    NCK(cudaMemcpyAsync(params_host, net->params, net->off.total * 4, cudaMemcpyDeviceToHost, net->stream));
+    NCK(cudaStreamSynchronize(net->stream));
+    return RECON_OK;
+}
+
+int recon_initnet_forward(recon_initnet *net, const uint16_t *in_bf16, int32_t n, float *out) {
+    int rc = check_batch(net, n);
+    if (rc) return rc;
+    if (!in_bf16 || !out) return net_fail(RECON_ERR_INVALID_ARG, "null argument");
+    (void)cudaGetLastError();
+    rc = forward(net, reinterpret_cast<const __nv_bfloat16 *>(in_bf16), n);
+    if (rc) return rc;
+    NCK(cudaMemcpyAsync(out, net->y, (int64_t)n * kOut * 4, cudaMemcpyDeviceToDevice, net->stream));
+    return RECON_OK;
+}
+
+int recon_initnet_gradient(recon_initnet *net, const uint16_t *in_bf16, const float *target, int32_t n, float *grad,
+                           float *loss_dev) {
+    int rc = check_batch(net, n);
+    if (rc) return rc;
+    if (!in_bf16 || !target || !grad || !loss_dev) return net_fail(RECON_ERR_INVALID_ARG, "null argument");
+    (void)cudaGetLastError();
+    const __nv_bfloat16 *in = reinterpret_cast<const __nv_bfloat16 *>(in_bf16);
+    rc = forward(net, in, n);
+    if (rc) return rc;
+    return backward(net, in, target, n, grad, loss_dev);
+}
+
+int recon_initnet_train_step(recon_initnet *net, const uint16_t *in_bf16, const float *target, int32_t n, float lr,
+                             float *loss_dev) {
+    int rc = check_batch(net, n);
+    if (rc) return rc;
+    if (!in_bf16 || !target || !loss_dev) return net_fail(RECON_ERR_INVALID_ARG, "null argument");
+    (void)cudaGetLastError();
+    const __nv_bfloat16 *in = reinterpret_cast<const __nv_bfloat16 *>(in_bf16);
+    rc = forward(net, in, n);
+    if (rc) return rc;
+    rc = backward(net, in, target, n, net->grad, loss_dev);
+    if (rc) return rc;
+    net->step++;
+    float bc1 = 1.0f - powf(0.9f, (float)net->step), bc2 = 1.0f - powf(0.999f, (float)net->step);
+    int64_t ntrain = net->off.scale;  // the output scale is not trained
+    k_adam<<<(unsigned)((ntrain + 255) / 256), 256, 0, net->stream>>>(net->params, net->grad, net->m, net->v, ntrain,
+                                                                      lr, bc1, bc2);
+    refresh_bf16(net);
+    NCK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int recon_initnet_coarse(const uint8_t *gray, const uint16_t *depth, int32_t n, int32_t width, int32_t height,
+                         uint16_t *out_bf16, void *stream) {
+    if (!gray || !depth || !out_bf16 || n <= 0) return net_fail(RECON_ERR_INVALID_ARG, "null argument");
+    if (width < RECON_NET_W || height < RECON_NET_H || width % RECON_NET_W || height % RECON_NET_H)
+        return net_fail(RECON_ERR_INVALID_ARG, "frame size must be a multiple of 80 x 60");
+    (void)cudaGetLastError();
+    int tot = n * RECON_NET_W * RECON_NET_H;
+    k_coarse<<<(tot + 255) / 256, 256, 0, (cudaStream_t)stream>>>(gray, depth, n, width, height,
+                                                                  reinterpret_cast<__nv_bfloat16 *>(out_bf16));
+    NCK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int recon_initnet_pair(const uint16_t *prev_coarse, const uint16_t *cur_coarse, int32_t n, uint16_t *in_bf16,
+                       void *stream) {
+    if (!prev_coarse || !cur_coarse || !in_bf16 || n <= 0) return net_fail(RECON_ERR_INVALID_ARG, "null argument");
+    (void)cudaGetLastError();
+    int tot = n * RECON_NET_W * RECON_NET_H;
+    k_pair<<<(tot + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const __nv_bfloat16 *>(prev_coarse), reinterpret_cast<const __nv_bfloat16 *>(cur_coarse), n,
+        reinterpret_cast<__nv_bfloat16 *>(in_bf16));
+    NCK(cudaGetLastError());
+    return RECON_OK;
+}
+
+}  // extern "C"

@@ -4,6 +4,7 @@
 // operation in the reference's source order, so the results reproduce the
 // reference semantics (and the CPU oracle) bit for bit.  One launch serves all
 // tracker instances of a batch (blockIdx.y = instance).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -1227,6 +1228,98 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int 
     __shared__ SolveShared sh;
     if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
     finalize_iter(d, sh, level, it, use_ph, use_icp, nsel);
+}
+
+// ------------------------------------------------------------------
+// learned initialisation: network inputs and the start-pose gate
+// ------------------------------------------------------------------
+
+// Coarse network image ([60][80][2] BF16: gray, depth in metres / 4) of each
+// instance's uint8 / uint16 input frame, from the input pointer table
+// (gray pointers, then depth pointers); the formula of recon_initnet_coarse.
+__global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
+                             __nv_bfloat16 *out) {
+    const InstDesc &d = D[blockIdx.y];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= kNetW * kNetH) return;
+    const uint8_t *g = in_gray[blockIdx.y];
+    const uint16_t *dp = in_depth[blockIdx.y];
+    if (!g || !dp) return;
+    int W = d.W, bx = d.W / kNetW, by = d.H / kNetH;
+    int ox = p % kNetW, oy = p / kNetW;
+    int gs = 0, cnt = 0;
+    long long ds = 0;
+    for (int y = 0; y < by; y++)
+        for (int x = 0; x < bx; x++) {
+            long long o = (long long)(oy * by + y) * W + ox * bx + x;
+            gs += g[o];
+            int dv = dp[o];
+            if (dv) {
+                ds += dv;
+                cnt++;
+            }
+        }
+    float gv = (float)gs / (255.0f * (float)(bx * by));
+    float dv = cnt ? ((float)ds / (float)cnt) / 4000.0f : 0.0f;
+    __nv_bfloat16 *o = out + ((long long)blockIdx.y * kNetW * kNetH + p) * 2;
+    o[0] = __float2bfloat16_rn(gv);
+    o[1] = __float2bfloat16_rn(dv);
+}
+
+// Integer start-pose cost: sum over the selected points of min(|r| * 1024, 1024)
+// (truncated) of the photometric residual at the coarsest level.
+__device__ __forceinline__ long long gate_cost(const InstDesc &d, const float *T, int level) {
+    int P = d.P, w = d.W >> level, h = d.H >> level;
+    float a = 1.0f / (float)(1 << level);
+    float b = 0.5f * (a - 1.0f);
+    long long c = 0;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        float r, zw;
+        photo_residual(d.calib, T, a, b, d.sel_xyz[i], d.sel_xyz[P + i], d.sel_xyz[2 * P + i], d.sel_I[level][i],
+                       d.cur_gray[level], w, h, d.cur_z, d.W, d.H, r, zw);
+        float u = fabsf(r) * 1024.0f;
+        c += (u >= 1024.0f || !(u == u)) ? 1024 : (long long)u;
+    }
+    return c;
+}
+
+// The learned start pose of each instance: the network's frame-to-frame twist
+// x = net_out * scale gives D = exp(A(x)) (the pose update's exponential,
+// applied to the identity) and the candidate D * T_prev; it replaces T_prev
+// when its gate cost is strictly lower.  choice[i] records the decision.
+__global__ void __launch_bounds__(256) k_init_gate(const InstDesc *D, const float *net_out, const float *scale,
+                                                   int *choice) {
+    const InstDesc &d = D[blockIdx.x];
+    __shared__ float Tp[16], Tc[16], Dm[16];
+    __shared__ SolveScratch S;
+    __shared__ long long cost[2];
+    int t = threadIdx.x;
+    if (t < 16) {
+        Tp[t] = d.T[t];
+        Dm[t] = (t % 5 == 0) ? 1.0f : 0.0f;
+    }
+    if (t < 2) cost[t] = 0;
+    __syncthreads();
+    if (t < 32) {
+        double x[6];
+        for (int k = 0; k < 6; k++) x[k] = (double)(net_out[blockIdx.x * 6 + k] * scale[k]);
+        wexpm_update(S, x, Dm, (double)d.opt_out, t);
+    }
+    __syncthreads();
+    if (t < 16) {
+        int r = t >> 2, c = t & 3;
+        Tc[t] = Dm[r * 4 + 0] * Tp[0 * 4 + c] + Dm[r * 4 + 1] * Tp[1 * 4 + c] + Dm[r * 4 + 2] * Tp[2 * 4 + c] +
+                Dm[r * 4 + 3] * Tp[3 * 4 + c];
+    }
+    __syncthreads();
+    int level = d.L - 1;
+    long long c0 = gate_cost(d, Tp, level), c1 = gate_cost(d, Tc, level);
+    atomicAdd(reinterpret_cast<unsigned long long *>(&cost[0]), (unsigned long long)c0);
+    atomicAdd(reinterpret_cast<unsigned long long *>(&cost[1]), (unsigned long long)c1);
+    __syncthreads();
+    bool take = cost[1] < cost[0];
+    if (t < 16 && take) d.T[t] = Tc[t];
+    if (t == 0 && choice) choice[blockIdx.x] = take ? 1 : 0;
 }
 
 // ------------------------------------------------------------------

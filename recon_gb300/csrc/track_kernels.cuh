@@ -18,6 +18,7 @@ constexpr int kIterBlock = 256;  // threads of a GN iteration CTA
 constexpr int kIterCtaSlots = 4 * 152;  // GN iteration CTAs resident on a 152-SM GB300
 constexpr int kSolveThreads = 64;        // threads of the per-instance solve CTA
 constexpr int kFxLimbs = 4;      // limbs of a fixed-point sum (fx.cuh)
+constexpr int kNetW = 80, kNetH = 60;  // coarse image of the learned initialisation
 
 enum StatSlot { ST_ITERS = 0, ST_SOLVES, ST_NONSPD, ST_STATUS, ST_MEDIAN, ST_ICPSEL0, ST_COUNT = 16 };
 

@@ -45,7 +45,7 @@ class OrcIterTrace(ctypes.Structure):
 
 
 def _build() -> None:
-    src = [os.path.join(ORACLE_DIR, f) for f in ("oracle.c", "oracle.h")]
+    src = [os.path.join(ORACLE_DIR, f) for f in ("oracle.c", "oracle.h", "initnet_oracle.c", "Makefile")]
     src.append(os.path.join(ROOT, "recon_gb300", "csrc", "scene.h"))
     if os.path.exists(LIB_PATH) and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in src):
         return
@@ -84,6 +84,11 @@ def lib() -> ctypes.CDLL:
             L.orc_fx27_clear.argtypes = [vp]
             L.orc_reduce27_fx.argtypes = [vp, vp, i32, vp]
             L.orc_fx27_value.argtypes = [vp, vp, vp]
+            L.orc_net_param_count.restype = ctypes.c_int64
+            L.orc_net_coarse.argtypes = [vp, vp, i32, i32, i32, vp]
+            L.orc_net_forward.argtypes = [vp, vp, i32, i32, vp]
+            L.orc_net_loss_grad.argtypes = [vp, vp, vp, i32, i32, vp]
+            L.orc_net_loss_grad.restype = ctypes.c_double
             L.orc_generate_weights.argtypes = [vp, vp, i32, i32, vp, vp, vp]
             L.orc_student_t.argtypes = [vp, i32, vp]
             L.orc_filter_indices.argtypes = [vp, i32, vp, i32, i32, vp]
@@ -111,6 +116,10 @@ def lib() -> ctypes.CDLL:
             L.orc_convert_depth.argtypes = [vp, i32, vp]
             L.orc_rgbd_float4_to_gray_z.argtypes = [vp, i32, i32, vp, vp, vp]
             L.orc_fuse_keyframe.argtypes = [vp, i32, vp, vp, f32]
+            L.orc_init_gate.argtypes = [vp, vp, vp]
+            L.orc_init_gate.restype = i32
+            L.orc_set_pose.argtypes = [vp, vp]
+            L.orc_get_pose.argtypes = [vp, vp]
             L.orc_num_threads.restype = i32
             L.orc_set_threads.argtypes = [i32]
             _lib = L
@@ -182,6 +191,17 @@ class OracleTracker:
         if n < 0:
             raise RuntimeError("oracle track failed")
         return Tin.reshape(4, 4), list(trace)[:min(n, max_trace)]
+
+    def pose(self) -> np.ndarray:
+        T = np.zeros(16, np.float32)
+        self.L.orc_get_pose(self.h, ptr(T))
+        return T.reshape(4, 4)
+
+    def init_gate(self, net_out: np.ndarray, scale: np.ndarray) -> int:
+        """The learned start-pose gate (orc_init_gate) with the network output of the GPU."""
+        y = np.ascontiguousarray(net_out, np.float32)
+        sc = np.ascontiguousarray(scale, np.float32)
+        return int(self.L.orc_init_gate(self.h, ptr(y), ptr(sc)))
 
     def fuse_keyframe(self, depths, Ts, gate: float = 30.0):
         ds = [np.ascontiguousarray(d, np.uint16) for d in depths]
