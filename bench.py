@@ -38,10 +38,17 @@ ITERS = (1, 3, 10, 5)
 LAMBDA = 0.5
 N_SELECT = 8192
 # algorithmic bytes per point and GN iteration (photometric: xyz 12 + I_ref 4 +
-# J 24 + 4 bilinear taps 16 + depth tap 4 + r/zweight written and re-read 16;
-# ICP: point+normal 24 + 4 taps x 12 + mask 4 + weight 4 + index 4)
-B_PHOTO = 76
+# J 24 + 4 bilinear taps 16 + depth tap 4; the fused kernel keeps the residual
+# and depth weight in registers, so the 16 bytes of the reference's separate
+# passes are not counted; ICP: point+normal 24 + 4 taps x 12 + mask 4 + weight 4
+# + index 4)
+B_PHOTO = 60
 B_ICP = 84
+# learned initialisation: trained parameters and the shortened schedule it runs
+LEARNED_WEIGHTS = "initnet_200k.npz"
+LEARNED_ITERS = (1, 2, 4, 2)
+BOUND_MM, BOUND_DEG = 1.0, 0.05
+METRIC = "tracked frames/s at 640x480, pose err <=1mm/0.05deg vs the oracle: learned-init vs plain GPU"
 
 
 def parse():
@@ -53,6 +60,7 @@ def parse():
     ap.add_argument("--frames", type=int, default=N_FRAMES)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plain-only", action="store_true", help="skip the learned-initialisation arm (profiling)")
     return ap.parse_args()
 
 
@@ -252,7 +260,7 @@ def reference_arm(args, rank, world):
             times.append(dt / n)
     fps = 1.0 / float(np.mean(times))
     line = {
-        "impl": "reference", "metric": "tracked frames/s (bi-objective 640x480, 300-frame trajectory)",
+        "impl": "reference", "metric": METRIC,
         "value": fps, "unit": "frames/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * float(np.mean(times)) * frames_per, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -267,6 +275,41 @@ def reference_arm(args, rank, world):
 
 
 # ---------------------------------------------------------------- main
+def load_net_params():
+    """Trained parameters of the learned initialisation (recon_gb300/weights), or None."""
+    path = os.path.join(ROOT, "recon_gb300", "weights", LEARNED_WEIGHTS)
+    if not os.path.exists(path):
+        return None, None
+    z = np.load(path)
+    return z["params"], {"file": os.path.relpath(path, ROOT), "pairs": int(z["pairs"]), "epochs": int(z["epochs"]),
+                         "validation_start_error_median": {"deg": float(z["val_rot_deg_median"]),
+                                                           "mm": float(z["val_trans_mm_median"])}}
+
+
+def pose_errors(a, b, frames):
+    from recon_gb300 import synth
+    return np.array([synth.pose_error(a[f].astype(np.float64), b[f].astype(np.float64)) for f in frames])
+
+
+def error_summary(e):
+    ok = (e[:, 0] <= BOUND_MM) & (e[:, 1] <= BOUND_DEG)
+    return {"within_bound": float(ok.mean()), "median_mm": float(np.median(e[:, 0])), "max_mm": float(e[:, 0].max()),
+            "median_deg": float(np.median(e[:, 1])), "max_deg": float(e[:, 1].max())}, ok
+
+
+def profiled_traffic():
+    """DRAM bytes per average k_iter launch of this workload, from the committed
+    ncu summary (profiles/k_iter_640x480_biobj_30inst.md), or None."""
+    path = os.path.join(ROOT, "profiles", "k_iter_640x480_biobj_30inst.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -282,64 +325,121 @@ def main():
     seed = rank_seed(rank)
     cal, scene, poses = make_workload(seed, args.frames)
     segs = segments(args.frames)
+    frames = [f for _, fr in segs for f in fr]
     gray, depth = render_frames_gpu(cal, scene, poses, seed, torch)
     stream = torch.cuda.Stream()
     batch = make_batch(cal, len(segs), stream.cuda_stream)
-    poses_out = np.zeros((args.frames + 1, 4, 4), np.float32)
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
 
-    # -------- device-resident timed region
-    for _ in range(args.warmup):
-        run_step(batch, segs, gray, depth, poses_out)
-    batch.enable_timing(True)
-    batch.work(reset=True)
-    launches0 = rg.launch_count()
-    barrier()
-    with ClockSampler(local) as clk:
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(src_g, src_d, out):
+        """W warm-up steps, then K steps between a barrier + synchronize on both
+        sides; (device ms, wall ms), slowest rank."""
+        for _ in range(args.warmup):
+            run_step(batch, segs, src_g, src_d, out)
+        barrier()
+        t0 = time.perf_counter()
         e0.record(stream)
         for _ in range(args.steps):
-            run_step(batch, segs, gray, depth, poses_out)
+            run_step(batch, segs, src_g, src_d, out)
         e1.record(stream)
         barrier()
-    ms = e0.elapsed_time(e1)
-    launches = rg.launch_count() - launches0
+        wall = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1)
+        return max_over_ranks(ms, world, "cuda"), max_over_ranks(1000.0 * wall, world, "cuda")
+
+    # -------- plain GPU tracker (the reference's schedule, bit-identical to the oracle)
+    poses_plain = np.zeros((args.frames + 1, 4, 4), np.float32)
+    clk = ClockSampler(local)  # samples clocks over every timed region below
+    clk.__enter__()
+    launches0 = rg.launch_count()
+    ms_plain, _ = timed(gray, depth, poses_plain)
+    launches_plain = (rg.launch_count() - launches0) / (args.warmup + args.steps)
+    plain_value = job_throughput(world, args.frames, args.steps, ms_plain)
+
+    # -------- per-kernel event timing of the same K steps (a separate pass: the
+    # events make every launch direct instead of graph-replayed)
+    batch.enable_timing(True)
+    batch.work(reset=True)
+    batch.timing(reset=True)
+    for _ in range(args.steps):
+        run_step(batch, segs, gray, depth, poses_plain)
+    torch.cuda.synchronize()
     timing = batch.timing(reset=True)
     work = batch.work(reset=True).astype(np.float64)
     batch.enable_timing(False)
-    ms = max_over_ranks(ms, world, "cuda")
-    frames_per_step = args.frames
-    value = job_throughput(world, frames_per_step, args.steps, ms)
-
-    # -------- roofline of the dominant kernel (the GN iteration kernel)
     it_ms, it_launches = timing["gn_iteration"]
     bytes_iter = float(work[:, 0].sum() * B_PHOTO + work[:, 1].sum() * B_ICP)
     per_launch_bytes = bytes_iter / max(it_launches, 1)
     per_launch_s = it_ms / 1000.0 / max(it_launches, 1)
     achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
     peak, peak_kind = load_peaks()
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_iter_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_launch_scaled")
-        except Exception:
-            traffic = None
+    traffic = profiled_traffic()
 
-    # -------- pose error against ground truth (all tracked frames)
-    errs = []
+    gt = np.zeros_like(poses_plain, dtype=np.float64)
     for k, fr in segs:
         for f in fr:
-            gt = synth.relative_pose(poses[k], poses[f])
-            errs.append(synth.pose_error(gt, poses_out[f].astype(np.float64)))
-    errs = np.array(errs)
+            gt[f] = synth.relative_pose(poses[k], poses[f])
+    plain_vs_gt, _ = error_summary(pose_errors(poses_plain, gt, frames))
 
-    # -------- e2e through the C ABI from pinned host memory
+    # -------- learned initialisation + shortened schedule
+    params, net_info = load_net_params() if not args.plain_only else (None, None)
+    learned = None
+    net = None
+    if params is not None:
+        import recon_gb300.initnet as IN
+        net = IN.InitNet(max_batch=len(segs), stream=stream.cuda_stream)
+        net.set_params(params)
+        batch.set_init_net(net, LEARNED_ITERS)
+        poses_learned = np.zeros_like(poses_plain)
+        launches0 = rg.launch_count()
+        ms_learned, _ = timed(gray, depth, poses_learned)
+        launches_learned = (rg.launch_count() - launches0) / (args.warmup + args.steps)
+        vs_oracle, ok = error_summary(pose_errors(poses_learned, poses_plain, frames))
+        vs_gt, _ = error_summary(pose_errors(poses_learned, gt, frames))
+        # share of frames whose start pose came from the network
+        batch.set_reference([gray[k] for k, _ in segs], [depth[k] for k, _ in segs])
+        acc = []
+        for s in range(max(len(fr) for _, fr in segs)):
+            idx = [fr[min(s, len(fr) - 1)] for _, fr in segs]
+            batch.set_current([gray[i] for i in idx], [depth[i] for i in idx])
+            batch.track()
+            acc.append(float(batch.init_choice()[0].mean()))
+        raw = job_throughput(world, args.frames, args.steps, ms_learned)
+        learned = {"schedule": list(LEARNED_ITERS), "raw_frames_per_s": raw, "ms_per_step": ms_learned / args.steps,
+                   "tracked_frames_per_s": raw * vs_oracle["within_bound"], "vs_oracle": vs_oracle,
+                   "vs_ground_truth": vs_gt, "learned_start_taken": float(np.mean(acc)), "network": net_info,
+                   "gpu_launches_per_step": launches_learned}
+        # the same shortened schedule from the plain start pose (the ablation)
+        batch.set_init_net(None)
+        for i in range(batch.n):
+            batch.set_iterations(i, LEARNED_ITERS)
+        poses_short = np.zeros_like(poses_plain)
+        ms_short, _ = timed(gray, depth, poses_short)
+        short_vs_oracle, _ = error_summary(pose_errors(poses_short, poses_plain, frames))
+        short_raw = job_throughput(world, args.frames, args.steps, ms_short)
+        learned["ablation_plain_start_same_schedule"] = {
+            "raw_frames_per_s": short_raw, "tracked_frames_per_s": short_raw * short_vs_oracle["within_bound"],
+            "vs_oracle": short_vs_oracle}
+        for i in range(batch.n):
+            batch.set_iterations(i, ITERS)
+        batch.set_init_net(net, LEARNED_ITERS)
+
+    # headline: frames tracked within the pose-error bound of the oracle, per second
+    if learned is not None:
+        value = learned["tracked_frames_per_s"]
+        ms_head = learned["ms_per_step"] * args.steps
+        head_launches = learned["gpu_launches_per_step"]
+    else:
+        value, ms_head, head_launches = plain_value, ms_plain, launches_plain
+
+    # -------- e2e through the C ABI from pinned host memory (the headline arm)
     e2e = None
     if not args.no_e2e:
         g_host = torch.empty(gray.shape, dtype=torch.uint8, pin_memory=True)
@@ -348,24 +448,19 @@ def main():
         d_host.copy_(depth)
         g_np = g_host.numpy()
         d_np = d_host.numpy().view(np.uint16)
-        for _ in range(max(1, args.warmup)):
-            run_step(batch, segs, g_np, d_np, poses_out)
-        barrier()
-        t0 = time.perf_counter()
-        e0.record(stream)
-        for _ in range(args.steps):
-            run_step(batch, segs, g_np, d_np, poses_out)
-        e1.record(stream)
-        barrier()
-        wall = time.perf_counter() - t0
-        ms_e2e = max(e0.elapsed_time(e1), 1000.0 * wall)
-        ms_e2e = max_over_ranks(ms_e2e, world, "cuda")
+        out = np.zeros_like(poses_plain)
+        ms_dev, ms_wall = timed(g_np, d_np, out)
+        ms_e2e = max(ms_dev, ms_wall)
+        frac = error_summary(pose_errors(out, poses_plain, frames))[0]["within_bound"] if learned is not None else 1.0
         n_ref = len(segs)
-        n_cur = sum(1 for _ in range(max(len(fr) for _, fr in segs))) * len(segs)
+        n_cur = max(len(fr) for _, fr in segs) * len(segs)
         h2d = (n_ref + n_cur) * W * H * 3
         d2h = max(len(fr) for _, fr in segs) * len(segs) * (64 + 64)
-        e2e = {"value": job_throughput(world, frames_per_step, args.steps, ms_e2e), "unit": "frames/s",
+        e2e = {"value": job_throughput(world, args.frames, args.steps, ms_e2e) * frac, "unit": "frames/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    clk.__exit__(None, None, None)
+    if net is not None:
+        batch.set_init_net(None)
 
     # -------- CPU baseline: the oracle on a bounded sample, and its pose agreement
     cpu = None
@@ -383,38 +478,42 @@ def main():
                          f"{dt:.1f} s"}
         d_t, d_r = [], []
         for f, To in oposes.items():
-            et, er = synth.pose_error(To.astype(np.float64), poses_out[f].astype(np.float64))
+            et, er = synth.pose_error(To.astype(np.float64), poses_plain[f].astype(np.float64))
             d_t.append(et)
             d_r.append(er)
         oracle_err = {"frames": len(d_t), "max_mm": float(max(d_t)), "max_deg": float(max(d_r)),
                       "bit_identical": bool(all(np.array_equal(oposes[f].view(np.uint32),
-                                                               poses_out[f].view(np.uint32)) for f in oposes))}
+                                                               poses_plain[f].view(np.uint32)) for f in oposes))}
 
     if rank == 0:
         clocks = clk.summary()
         line = {
-            "metric": "tracked frames/s (bi-objective 640x480, 300-frame trajectory)",
+            "metric": METRIC,
             "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": ms_head / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32", "data": "synthetic (seeded procedural scene ray-cast on the GPU)",
-            "config": {"workload": "bi-objective lambda=0.5, 640x480, 4 levels, iterations 1/3/10/5, 8192 "
-                                   "photometric points, 300-frame smooth trajectory, keyframe every 10 frames, "
-                                   "30 keyframe segments batched",
+            "config": {"workload": "bi-objective lambda=0.5, 640x480, 4 levels, 8192 photometric points, 300-frame "
+                                   "smooth trajectory, keyframe every 10 frames, 30 keyframe segments batched",
+                       "plain_schedule": list(ITERS),
+                       "learned_schedule": list(LEARNED_ITERS) if learned is not None else None,
+                       "bound": {"mm": BOUND_MM, "deg": BOUND_DEG,
+                                 "against": "plain GPU poses (bit-identical to the oracle)"},
                        "l2": "inputs larger than L2 (301 frames, 277 MB; ~1.2 GB working set)",
                        "parallelism": f"replicas x{world}"},
+            "plain": {"frames_per_s": plain_value, "ms_per_step": ms_plain / args.steps,
+                      "vs_ground_truth": plain_vs_gt, "gpu_launches_per_step": launches_plain},
+            "learned": learned,
+            "speedup_vs_plain": value / plain_value,
             "e2e": e2e,
-            "gpu_launches": int(launches),
+            "gpu_launches": int(round(head_launches * args.steps)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": "k_iter",
                          "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": per_launch_bytes,
-                         "avg_launch_ms": per_launch_s * 1000.0},
+                         "avg_launch_ms": per_launch_s * 1000.0,
+                         "timing": "per-launch CUDA events on the batch stream, separate K-step pass of the plain arm"},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "pose_error_vs_ground_truth": {"median_mm": float(np.median(errs[:, 0])),
-                                           "max_mm": float(errs[:, 0].max()),
-                                           "median_deg": float(np.median(errs[:, 1])),
-                                           "max_deg": float(errs[:, 1].max())},
             "pose_error_vs_oracle": oracle_err,
             "kernel_ms": {k: v[0] for k, v in timing.items()},
             "kernel_launches": {k: v[1] for k, v in timing.items()},

@@ -46,7 +46,10 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
 __global__ void k_ref_from_z(const InstDesc *D, const int *active);
 __global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
                              __nv_bfloat16 *out);
-__global__ void k_init_gate(const InstDesc *D, const float *net_out, const float *scale, int *choice);
+__global__ void k_gate_candidate(const InstDesc *D, const float *net_out, const float *scale, float *cand,
+                                 long long *cost);
+__global__ void k_gate_cost(const InstDesc *D, const float *cand, long long *cost);
+__global__ void k_gate_pick(const InstDesc *D, const float *cand, const long long *cost, int *choice);
 }  // namespace rt
 
 namespace nn {
@@ -165,6 +168,8 @@ struct recon_batch {
     uint16_t *d_netin = nullptr;  // [n][60][80][4]
     float *d_netout = nullptr;    // [n][6]
     int *d_choice = nullptr;      // [n]: 1 where the learned start pose was taken
+    float *d_cand = nullptr;      // [n][16]: candidate start poses
+    long long *d_cost = nullptr;  // [n][2]: gate costs of the current pose and the candidate
     std::vector<std::vector<int>> plain_iters;  // schedules restored when the network is detached
 };
 
@@ -516,8 +521,10 @@ int learned_start(recon_batch *b, const void **row) {
     rc = nn::forward_on(b->net, b->d_netin, n, b->d_netout, b->stream);
     if (rc) return rc;
     g_launches += 8;  // six convolutions, pooling + linear layer, output copy
-    k_init_gate<<<n, 256, 0, b->stream>>>(b->d_desc, b->d_netout, nn::scale_dev(b->net), b->d_choice);
-    g_launches += 1;
+    k_gate_candidate<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_netout, nn::scale_dev(b->net), b->d_cand, b->d_cost);
+    k_gate_cost<<<dim3((b->max_P + 1023) / 1024, n), 256, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost);
+    k_gate_pick<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost, b->d_choice);
+    g_launches += 3;
     b->coarse_prev = cur;
     CK(cudaGetLastError());
     return RECON_OK;
@@ -756,6 +763,8 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->d_netin) cudaFree(b->d_netin);
     if (b->d_netout) cudaFree(b->d_netout);
     if (b->d_choice) cudaFree(b->d_choice);
+    if (b->d_cand) cudaFree(b->d_cand);
+    if (b->d_cost) cudaFree(b->d_cost);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RECON_OK;
@@ -1112,13 +1121,14 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         }
         int rc = prepare_current(b, row, b->d_ones);
         if (rc) return rc;
-        if (!on_device) CK(cudaEventRecord(b->ev_free[f & 1], b->stream));
         k_begin_track<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, 0);
         g_launches += 1;
         if (b->net) {
             rc = learned_start(b, row);
             if (rc) return rc;
         }
+        // every reader of this frame's staged inputs has been issued
+        if (!on_device) CK(cudaEventRecord(b->ev_free[f & 1], b->stream));
         rc = run_schedule(b);
         if (rc) return rc;
         k_store_pose<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tseq + (size_t)f * n * 16);
@@ -1163,6 +1173,8 @@ int recon_batch_set_init_net(recon_batch *b, recon_initnet *net, const int32_t i
         CK(cudaMalloc(&b->d_netin, px * 4 * sizeof(uint16_t)));
         CK(cudaMalloc(&b->d_netout, (size_t)n * 6 * sizeof(float)));
         CK(cudaMalloc(&b->d_choice, (size_t)n * sizeof(int)));
+        CK(cudaMalloc(&b->d_cand, (size_t)n * 16 * sizeof(float)));
+        CK(cudaMalloc(&b->d_cost, (size_t)n * 2 * sizeof(long long)));
         CK(cudaMemsetAsync(b->d_coarse[0], 0, px * 2 * sizeof(uint16_t), b->stream));
         CK(cudaMemsetAsync(b->d_coarse[1], 0, px * 2 * sizeof(uint16_t), b->stream));
     }

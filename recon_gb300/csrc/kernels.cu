@@ -1266,59 +1266,77 @@ __global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, c
     o[1] = __float2bfloat16_rn(dv);
 }
 
-// Integer start-pose cost: sum over the selected points of min(|r| * 1024, 1024)
-// (truncated) of the photometric residual at the coarsest level.
-__device__ __forceinline__ long long gate_cost(const InstDesc &d, const float *T, int level) {
+// Integer start-pose cost of one point: min(trunc(|r| * 1024), 1024) of its
+// photometric residual at `level`.
+__device__ __forceinline__ long long gate_cost_point(const InstDesc &d, const float *T, int level, int i) {
     int P = d.P, w = d.W >> level, h = d.H >> level;
     float a = 1.0f / (float)(1 << level);
     float b = 0.5f * (a - 1.0f);
-    long long c = 0;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        float r, zw;
-        photo_residual(d.calib, T, a, b, d.sel_xyz[i], d.sel_xyz[P + i], d.sel_xyz[2 * P + i], d.sel_I[level][i],
-                       d.cur_gray[level], w, h, d.cur_z, d.W, d.H, r, zw);
-        float u = fabsf(r) * 1024.0f;
-        c += (u >= 1024.0f || !(u == u)) ? 1024 : (long long)u;
-    }
-    return c;
+    float r, zw;
+    photo_residual(d.calib, T, a, b, __ldg(d.sel_xyz + i), __ldg(d.sel_xyz + P + i), __ldg(d.sel_xyz + 2 * P + i),
+                   __ldg(d.sel_I[level] + i), d.cur_gray[level], w, h, d.cur_z, d.W, d.H, r, zw);
+    float u = fabsf(r) * 1024.0f;
+    return (u >= 1024.0f || !(u == u)) ? 1024 : (long long)u;
 }
 
-// The learned start pose of each instance: the network's frame-to-frame twist
-// x = net_out * scale gives D = exp(A(x)) (the pose update's exponential,
-// applied to the identity) and the candidate D * T_prev; it replaces T_prev
-// when its gate cost is strictly lower.  choice[i] records the decision.
-__global__ void __launch_bounds__(256) k_init_gate(const InstDesc *D, const float *net_out, const float *scale,
-                                                   int *choice) {
+// The learned start pose, step 1 (one warp per instance): the network's
+// frame-to-frame twist x = net_out * scale gives D = exp(A(x)) (the pose
+// update's exponential applied to the identity) and the candidate D * T;
+// the two gate costs of the instance are reset.
+__global__ void __launch_bounds__(32) k_gate_candidate(const InstDesc *D, const float *net_out, const float *scale,
+                                                       float *cand, long long *cost) {
     const InstDesc &d = D[blockIdx.x];
-    __shared__ float Tp[16], Tc[16], Dm[16];
+    __shared__ float Tp[16], Dm[16];
     __shared__ SolveScratch S;
-    __shared__ long long cost[2];
     int t = threadIdx.x;
     if (t < 16) {
         Tp[t] = d.T[t];
         Dm[t] = (t % 5 == 0) ? 1.0f : 0.0f;
     }
-    if (t < 2) cost[t] = 0;
-    __syncthreads();
-    if (t < 32) {
-        double x[6];
-        for (int k = 0; k < 6; k++) x[k] = (double)(net_out[blockIdx.x * 6 + k] * scale[k]);
-        wexpm_update(S, x, Dm, (double)d.opt_out, t);
-    }
-    __syncthreads();
+    if (t < 2) cost[2 * blockIdx.x + t] = 0;
+    __syncwarp();
+    double x[6];
+    for (int k = 0; k < 6; k++) x[k] = (double)(net_out[blockIdx.x * 6 + k] * scale[k]);
+    wexpm_update(S, x, Dm, (double)d.opt_out, t);
     if (t < 16) {
         int r = t >> 2, c = t & 3;
-        Tc[t] = Dm[r * 4 + 0] * Tp[0 * 4 + c] + Dm[r * 4 + 1] * Tp[1 * 4 + c] + Dm[r * 4 + 2] * Tp[2 * 4 + c] +
-                Dm[r * 4 + 3] * Tp[3 * 4 + c];
+        cand[16 * blockIdx.x + t] = Dm[r * 4 + 0] * Tp[0 * 4 + c] + Dm[r * 4 + 1] * Tp[1 * 4 + c] +
+                                    Dm[r * 4 + 2] * Tp[2 * 4 + c] + Dm[r * 4 + 3] * Tp[3 * 4 + c];
     }
+}
+
+// Step 2 (grid: point blocks x instances): the integer costs of the current
+// pose and of the candidate at the coarsest level, summed with atomics (exact,
+// so the sum does not depend on the order).
+__global__ void __launch_bounds__(256) k_gate_cost(const InstDesc *D, const float *cand, long long *cost) {
+    const InstDesc &d = D[blockIdx.y];
+    __shared__ float Tp[16], Tc[16];
+    __shared__ long long part[2];
+    int t = threadIdx.x;
+    if (t < 16) {
+        Tp[t] = d.T[t];
+        Tc[t] = cand[16 * blockIdx.y + t];
+    }
+    if (t < 2) part[t] = 0;
     __syncthreads();
     int level = d.L - 1;
-    long long c0 = gate_cost(d, Tp, level), c1 = gate_cost(d, Tc, level);
-    atomicAdd(reinterpret_cast<unsigned long long *>(&cost[0]), (unsigned long long)c0);
-    atomicAdd(reinterpret_cast<unsigned long long *>(&cost[1]), (unsigned long long)c1);
+    long long c0 = 0, c1 = 0;
+    for (int i = blockIdx.x * blockDim.x + t; i < d.P; i += gridDim.x * blockDim.x) {
+        c0 += gate_cost_point(d, Tp, level, i);
+        c1 += gate_cost_point(d, Tc, level, i);
+    }
+    atomicAdd(reinterpret_cast<unsigned long long *>(&part[0]), (unsigned long long)c0);
+    atomicAdd(reinterpret_cast<unsigned long long *>(&part[1]), (unsigned long long)c1);
     __syncthreads();
-    bool take = cost[1] < cost[0];
-    if (t < 16 && take) d.T[t] = Tc[t];
+    if (t < 2) atomicAdd(reinterpret_cast<unsigned long long *>(cost + 2 * blockIdx.y + t), (unsigned long long)part[t]);
+}
+
+// Step 3: the candidate replaces the pose when its cost is strictly lower.
+__global__ void k_gate_pick(const InstDesc *D, const float *cand, const long long *cost, int *choice) {
+    const InstDesc &d = D[blockIdx.x];
+    int t = threadIdx.x;
+    bool take = cost[2 * blockIdx.x + 1] < cost[2 * blockIdx.x];
+    if (t < 16 && take) d.T[t] = cand[16 * blockIdx.x + t];
     if (t == 0 && choice) choice[blockIdx.x] = take ? 1 : 0;
 }
 
