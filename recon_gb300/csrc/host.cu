@@ -522,7 +522,7 @@ int learned_start(recon_batch *b, const void **row) {
     if (rc) return rc;
     g_launches += 8;  // six convolutions, pooling + linear layer, output copy
     k_gate_candidate<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_netout, nn::scale_dev(b->net), b->d_cand, b->d_cost);
-    k_gate_cost<<<dim3((b->max_P + 1023) / 1024, n), 256, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost);
+    k_gate_cost<<<dim3((b->max_P + 255) / 256, n), 256, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost);
     k_gate_pick<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost, b->d_choice);
     g_launches += 3;
     b->coarse_prev = cur;

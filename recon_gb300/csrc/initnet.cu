@@ -4,8 +4,8 @@
 //
 // Every kernel reduces in a fixed order (no floating-point atomics), so a
 // training run is deterministic.  The shapes are small (about 10 MFLOP per
-// sample): one warp computes a 16-pixel by Cout output tile directly from the
-// NHWC input (implicit GEMM, no im2col buffer).
+// sample): a CTA computes a 16-pixel by Cout output tile directly from the NHWC
+// input (implicit GEMM, no im2col buffer).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -60,16 +60,25 @@ Offsets offsets() {
 __device__ __forceinline__ float bf(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
 
 // out[m][co] = relu(bias[co] + sum_k A[m][k] W[co][k]) with A the 3x3 / stride 2
-// / pad 1 patches of `in` (k = tap * Cin + c); one warp per 16 output pixels.
+// / pad 1 patches of `in` (k = tap * Cin + c).  One CTA of 16 warps per 16
+// output pixels: warp w takes output-channel group w % NG and the K steps
+// j = w / NG, w / NG + KS, ...; the KS partial tiles are added in ascending
+// order in shared memory, so the result does not depend on scheduling.
+constexpr int kConvWarps = 16;
+
 template <int COUT>
-__global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16 *in, int N, int H, int W, int Cin, int Kp,
-                                                  const __nv_bfloat16 *w, const float *bias, __nv_bfloat16 *out,
-                                                  int Ho, int Wo) {
-    int lane = threadIdx.x & 31;
-    long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(kConvWarps * 32) k_conv_fwd(const __nv_bfloat16 *in, int N, int H, int W, int Cin,
+                                                              int Kp, const __nv_bfloat16 *w, const float *bias,
+                                                              __nv_bfloat16 *out, int Ho, int Wo) {
+    constexpr int NF = COUT / 8;             // 8-column fragments
+    constexpr int NG = NF < 8 ? NF : 8;      // warps across the columns
+    constexpr int FPW = NF / NG;             // fragments per warp
+    constexpr int KS = kConvWarps / NG;      // warps across K
+    __shared__ float red[KS][16][COUT];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int ng = warp % NG, ks = warp / NG;
     long long M = (long long)N * Ho * Wo;
-    long long m0 = warp * 16;
-    if (m0 >= M) return;
+    long long m0 = (long long)blockIdx.x * 16;
     int g = lane >> 2, tig = lane & 3;
     long long rr[2] = {m0 + g, m0 + g + 8};
     bool rv[2];
@@ -82,11 +91,13 @@ __global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16 *in, int N
         ry[h] = (int)((mm / Wo) % Ho);
         rn[h] = (int)(mm / ((long long)Wo * Ho));
     }
-    float acc[COUT / 8][4];
+    float acc[FPW][4];
 #pragma unroll
-    for (int f = 0; f < COUT / 8; f++) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
-    int K = 9 * Cin;
-    for (int kb = 0; kb < Kp; kb += 16) {
+    for (int f = 0; f < FPW; f++) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
+    int K = 9 * Cin, nk = Kp / 16;
+#pragma unroll 2
+    for (int j = ks; j < nk; j += KS) {
+        int kb = 16 * j;
         // A fragment: a0 (row g, k 2t..2t+1), a1 (row g+8), a2 (row g, k+8), a3 (row g+8, k+8)
         uint32_t a[4];
 #pragma unroll
@@ -104,9 +115,9 @@ __global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16 *in, int N
             a[q] = v;
         }
 #pragma unroll
-        for (int f = 0; f < COUT / 8; f++) {
+        for (int f = 0; f < FPW; f++) {
             // B fragment: b0 (k 2t..2t+1, n g), b1 (k + 8)
-            const __nv_bfloat16 *wr = w + (long long)(f * 8 + g) * Kp + kb + 2 * tig;
+            const __nv_bfloat16 *wr = w + (long long)((ng * FPW + f) * 8 + g) * Kp + kb + 2 * tig;
             uint32_t b0 = *reinterpret_cast<const uint32_t *>(wr);
             uint32_t b1 = *reinterpret_cast<const uint32_t *>(wr + 8);
             asm volatile(
@@ -118,17 +129,29 @@ __global__ void __launch_bounds__(128) k_conv_fwd(const __nv_bfloat16 *in, int N
     }
     // C fragment: c0 c1 (row g, cols 2t, 2t+1), c2 c3 (row g+8)
 #pragma unroll
-    for (int f = 0; f < COUT / 8; f++) {
-        int col = f * 8 + 2 * tig;
+    for (int f = 0; f < FPW; f++) {
+        int col = (ng * FPW + f) * 8 + 2 * tig;
+        red[ks][g][col] = acc[f][0];
+        red[ks][g][col + 1] = acc[f][1];
+        red[ks][g + 8][col] = acc[f][2];
+        red[ks][g + 8][col + 1] = acc[f][3];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 16 * COUT / 2; e += blockDim.x) {
+        int row = e / (COUT / 2), col = 2 * (e % (COUT / 2));
+        long long m = m0 + row;
+        if (m >= M) continue;
+        float v0 = 0.0f, v1 = 0.0f;
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            if (!rv[h]) continue;
-            float v0 = acc[f][2 * h] + bias[col], v1 = acc[f][2 * h + 1] + bias[col + 1];
-            v0 = v0 > 0.0f ? v0 : 0.0f;
-            v1 = v1 > 0.0f ? v1 : 0.0f;
-            __nv_bfloat162 pr = __floats2bfloat162_rn(v0, v1);
-            *reinterpret_cast<__nv_bfloat162 *>(out + rr[h] * COUT + col) = pr;
+        for (int q = 0; q < KS; q++) {
+            v0 += red[q][row][col];
+            v1 += red[q][row][col + 1];
         }
+        v0 = v0 + bias[col];
+        v1 = v1 + bias[col + 1];
+        v0 = v0 > 0.0f ? v0 : 0.0f;
+        v1 = v1 > 0.0f ? v1 : 0.0f;
+        *reinterpret_cast<__nv_bfloat162 *>(out + m * COUT + col) = __floats2bfloat162_rn(v0, v1);
     }
 }
 
@@ -359,16 +382,16 @@ int nsplit_for(int l, int n) {
 int conv_forward(recon_initnet *net, int l, const __nv_bfloat16 *in, int n) {
     int Cin = kCin[l], Cout = kCout[l], Kp = kpad(Cin);
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
-    int warps = (int)((M + 15) / 16);
-    dim3 grid((warps * 32 + 127) / 128);
+    dim3 grid((unsigned)((M + 15) / 16));
+    const int block = kConvWarps * 32;
     const __nv_bfloat16 *w = net->pbf + net->off.w[l];
     const float *b = net->params + net->off.b[l];
     int H = kHt[l], W = kWd[l], Ho = kHt[l + 1], Wo = kWd[l + 1];
     switch (Cout) {
-        case 16: k_conv_fwd<16><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
-        case 32: k_conv_fwd<32><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
-        case 64: k_conv_fwd<64><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
-        default: k_conv_fwd<128><<<grid, 128, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+        case 16: k_conv_fwd<16><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+        case 32: k_conv_fwd<32><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+        case 64: k_conv_fwd<64><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+        default: k_conv_fwd<128><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
     }
     return RECON_OK;
 }
