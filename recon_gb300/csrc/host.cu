@@ -31,7 +31,7 @@ __global__ void k_seg_scatter(const InstDesc *D, const int *active);
 __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
 __global__ void k_icp_compact(const InstDesc *D, int level);
-__global__ void k_icp_student(const InstDesc *D, int level, int pass);
+__global__ void k_icp_student3(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
 __global__ void k_solve(const InstDesc *D, int level, int it);
 __global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
@@ -437,11 +437,11 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
                 TimedScope ts(b, s, TK_ICP_COMPACT, in_graph);
                 k_icp_compact<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
             }
-            for (int pass = 1; pass <= 3; pass++) {
+            {
                 TimedScope ts(b, s, TK_ICP_STUDENT, in_graph);
-                k_icp_student<<<grid_pix(maxpix, n), 256, 0, s>>>(D, level, pass);
+                k_icp_student3<<<dim3(kIterCluster, n), 1024, 0, s>>>(D, level);
             }
-            b->graph_kernels += 5;
+            b->graph_kernels += 3;
         }
         // ICP chunks per CTA: enough CTAs for about four waves of the batch's
         // chunks, at most 8 chunks each (the result does not depend on it)

@@ -650,29 +650,6 @@ __global__ void k_icp_compact(const InstDesc *D, int level) {
     block_add_ll(&d.icp_var[0], vsum);
 }
 
-// updateWeightsKernel / clampWeightsKernel (rgb2gray.cu:549-569) with the
-// variance of the previous pass; the final pass clamps at 1.  Only the final
-// pass's weights are used, so passes 1 and 2 produce just their variance sums.
-__global__ void k_icp_student(const InstDesc *D, int level, int pass) {
-    INST_DESC;
-    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
-    if (d.iters[d.L - 1 - level] <= 0) return;
-    int nsel = d.icp_nsel[level];
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    long long vsum = 0;
-    if (i < nsel) {
-        float Sf = (float)(long long)d.icp_var[pass - 1];
-        float minVal = (float)nsel;
-        float var = (nsel <= 1024) ? Sf : (Sf < minVal ? minVal : Sf);
-        float sigma2 = var / (float)nsel;
-        float r2 = d.icp_r2[i];
-        float wv = 6 / (5 + r2 / sigma2);
-        if (pass == 3) d.icp_w[i] = fminf(wv, 1.0f);
-        else vsum = trunc_prod(r2, wv);
-    }
-    if (pass < 3) block_add_ll(&d.icp_var[pass], vsum);
-}
-
 // ------------------------------------------------------------------
 // one Gauss-Newton iteration for every instance
 // ------------------------------------------------------------------
@@ -1228,6 +1205,64 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int 
     __shared__ SolveShared sh;
     if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
     finalize_iter(d, sh, level, it, use_ph, use_icp, nsel);
+}
+
+// The three Student-t passes of a level in one launch (updateWeightsKernel /
+// clampWeightsKernel, rgb2gray.cu:549-569): each pass weighs every
+// correspondence with the variance of the previous pass; the final pass clamps
+// at 1 and writes the weights, the first two produce only their variance sums
+// (exact int64 sums of truncated products).  An 8-CTA cluster per instance
+// (blockIdx.y) splits the correspondences and exchanges the CTAs' sums through
+// distributed shared memory, so no pass waits for a separate launch.
+constexpr int kStudentThreads = 1024;
+
+__global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads)
+    k_icp_student3(const InstDesc *D, int level) {
+    __shared__ InstDesc sd;
+    __shared__ long long part[2];
+    __shared__ long long warp_sum[kStudentThreads / 32];
+    load_desc(sd, D + blockIdx.y);
+    __syncthreads();
+    const InstDesc &d = sd;
+    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
+    if (d.iters[d.L - 1 - level] <= 0) return;  // uniform over the cluster
+    int nsel = __ldcg(d.icp_nsel + level);
+    int rank = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    int stride = kIterCluster * kStudentThreads;
+    long long var = (long long)__ldcg(d.icp_var + 0);
+    for (int pass = 1; pass <= 3; pass++) {
+        float Sf = (float)var;
+        float minVal = (float)nsel;
+        float vv = (nsel <= 1024) ? Sf : (Sf < minVal ? minVal : Sf);
+        float sigma2 = vv / (float)nsel;
+        long long vsum = 0;
+        for (int i = rank * kStudentThreads + t; i < nsel; i += stride) {
+            float r2 = __ldg(d.icp_r2 + i);
+            float wv = 6 / (5 + r2 / sigma2);
+            if (pass == 3) d.icp_w[i] = fminf(wv, 1.0f);
+            else vsum += trunc_prod(r2, wv);
+        }
+        if (pass == 3) break;
+        for (int o = 16; o > 0; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
+        if (lane == 0) warp_sum[wid] = vsum;
+        __syncthreads();
+        if (t == 0) {
+            long long sum = 0;
+            for (int w = 0; w < kStudentThreads / 32; w++) sum += warp_sum[w];
+            part[pass - 1] = sum;
+        }
+        cluster_arrive();
+        cluster_wait();  // every CTA's sum of this pass is in its shared memory
+        long long tot = 0;
+#pragma unroll
+        for (int r = 0; r < kIterCluster; r++) tot += *cluster_peer(&part[pass - 1], r);
+        var = tot;
+        if (rank == 0 && t == 0) d.icp_var[pass] = (unsigned long long)tot;
+        __syncthreads();  // warp_sum is rewritten by the next pass
+    }
+    // no CTA leaves while another may still read its sums
+    cluster_arrive();
+    cluster_wait();
 }
 
 // ------------------------------------------------------------------
