@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="skip the learned-initialisation arm (profiling)")
+    ap.add_argument("--no-tune", action="store_true", help="built-in tile shapes instead of the autotuner's")
     return ap.parse_args()
 
 
@@ -329,6 +330,16 @@ def main():
     gray, depth = render_frames_gpu(cal, scene, poses, seed, torch)
     stream = torch.cuda.Stream()
     batch = make_batch(cal, len(segs), stream.cuda_stream)
+    tile = None
+    if not args.no_tune:
+        # tile shape of the linearisation kernel, timed on the first frame of
+        # every segment before any timed region (poses do not depend on it)
+        from recon_gb300.tune import autotune_icp_chunks
+        batch.set_reference([gray[k] for k, _ in segs], [depth[k] for k, _ in segs])
+        batch.set_current([gray[fr[0]] for _, fr in segs], [depth[fr[0]] for _, fr in segs])
+        chosen, table = autotune_icp_chunks(batch)
+        tile = {"icp_chunks_per_cta": chosen[:4],
+                "candidates_ms": {str(l): {str(c): round(v, 3) for c, v in t.items()} for l, t in table.items()}}
 
     def barrier():
         torch.cuda.synchronize()
@@ -499,7 +510,8 @@ def main():
                        "bound": {"mm": BOUND_MM, "deg": BOUND_DEG,
                                  "against": "plain GPU poses (bit-identical to the oracle)"},
                        "l2": "inputs larger than L2 (301 frames, 277 MB; ~1.2 GB working set)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "tile": tile or {"icp_chunks_per_cta": batch.icp_chunks_per_cta(), "autotuned": False}},
             "plain": {"frames_per_s": plain_value, "ms_per_step": ms_plain / args.steps,
                       "vs_ground_truth": plain_vs_gt, "gpu_launches_per_step": launches_plain},
             "learned": learned,

@@ -168,6 +168,15 @@ int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *c
 int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters[RECON_MAX_LEVELS]);
 int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambda);
 
+/* Tile shape of the linearisation kernel at each pyramid level: ICP chunks of
+ * 1024 pixels per CTA, 1..64, or 0 for the built-in choice.  Poses and sums do
+ * not depend on it (the normal equations are exact integer sums); only the
+ * speed does.  recon_gb300.tune.autotune_icp_chunks picks it by timing.  No
+ * reference counterpart: the reference launches fixed 1024-thread blocks. */
+int recon_batch_set_icp_chunks_per_cta(recon_batch *b, const int32_t per_level[RECON_MAX_LEVELS]);
+/* The values in effect (the built-in choice resolved), 0 for unused levels. */
+int recon_batch_get_icp_chunks_per_cta(recon_batch *b, int32_t per_level[RECON_MAX_LEVELS]);
+
 /* Per-iteration trace of instance `inst` (enabled with max_iters > 0). */
 int recon_batch_enable_trace(recon_batch *b, int32_t max_iters);
 int recon_batch_get_trace(recon_batch *b, int32_t inst, recon_iter_trace *out, int32_t max);
@@ -188,7 +197,10 @@ int64_t recon_launch_count(void);         /* kernels launched by the library so 
 
 /* Copies an internal device array of instance `inst` to host memory (tests).
  * Names: ref_gray, cur_gray, ref_z, cur_z, ref_pts, ref_nrm, cur_pts, sel_idx,
- * sel_xyz, sel_I, sel_J, vtx, icp_select, icp_w, grad_hist.  Returns bytes. */
+ * sel_xyz, sel_I, sel_J, vtx, grad_hist, icp_nsel, and icp_mask (uint8) /
+ * icp_w (float) per pixel of the last level the ICP term prepared (`level`
+ * gives its size; icp_w is 0 where the pixel is not a correspondence).
+ * Returns bytes. */
 int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, int32_t level, void *host_dst,
                               int64_t nbytes);
 

@@ -952,6 +952,8 @@ void orc_icp_residual_jacobian(const float *ref6, const int32_t *select, int nse
         res[idx] = 0.0f;
         for (int c = 0; c < 6; c++) J[idx + npadded * c] = 0.0f;
         if (idx >= nsel) continue;
+        /* a weight that is not positive gives zeros below; skip the work */
+        if (!(weights[idx] > 0.0f)) continue;
         const float *p = &ref6[select[idx] * 6];
         float p3[3] = {p[0], p[1], p[2]}, rn[3] = {p[3], p[4], p[5]};
         float q3[3], cn[3];
@@ -1336,6 +1338,8 @@ struct orc_tracker {
     float *full_res;
     int32_t *rmask, *select;
     float *icp_r, *icp_r2, *icp_w, *icp_J, *icp_res;
+    float *icp_wpx;    /* the level's Student-t weights per pixel, 0 where not selected */
+    int32_t *all_px;   /* 0, 1, 2, ...: every pixel of the level in order */
     int32_t nsel[ORC_MAX_LEVELS];
     int has_ref, has_cur;
     float T[16];
@@ -1387,6 +1391,9 @@ orc_tracker *orc_create(const orc_config *cfg, const float *calib) {
     t->icp_w = (float *)xmalloc(npmax * sizeof(float));
     t->icp_res = (float *)xmalloc(npmax * sizeof(float));
     t->icp_J = (float *)xmalloc(6 * (size_t)npmax * sizeof(float));
+    t->icp_wpx = (float *)xmalloc(npmax * sizeof(float));
+    t->all_px = (int32_t *)xmalloc(W * H * sizeof(int32_t));
+    for (int i = 0; i < W * H; i++) t->all_px[i] = i;
     for (int i = 0; i < 16; i++) t->T[i] = (i % 5 == 0) ? 1.0f : 0.0f;
     return t;
 }
@@ -1402,6 +1409,7 @@ void orc_destroy(orc_tracker *t) {
     for (int c = 0; c < 6; c++) free(t->Jw[c]);
     free(t->full_res); free(t->rmask); free(t->select);
     free(t->icp_r); free(t->icp_r2); free(t->icp_w); free(t->icp_res); free(t->icp_J);
+    free(t->icp_wpx); free(t->all_px);
     free(t);
 }
 
@@ -1581,14 +1589,19 @@ int orc_track(orc_tracker *t, float *Tio, orc_iter_trace *trace, int max_trace) 
                         }
                         orc_student_t(t->icp_r2, t->nsel[layer], t->icp_w);
                     }
+                    memset(t->icp_wpx, 0, (size_t)wl * hl * sizeof(float));
+                    for (int k = 0; k < t->nsel[layer]; k++) t->icp_wpx[t->select[k]] = t->icp_w[k];
                 }
                 int ns = t->nsel[layer];
                 if (ns <= 0) {
                     ok = 0;
                 } else {
-                    int np = padded_len(ns);
-                    orc_icp_residual_jacobian(t->ref6[layer], t->select, ns, wl, hl, layer, t->T, t->calib,
-                                              t->cur6[layer], t->curmask[layer], np, t->icp_res, t->icp_J, t->icp_w,
+                    /* The canonical FP32 stage of the ICP sums runs over the
+                     * level's pixel grid in 1024-pixel chunks; a pixel that was
+                     * not selected has weight 0 and contributes exact zeros. */
+                    int npx = wl * hl, np = padded_len(npx);
+                    orc_icp_residual_jacobian(t->ref6[layer], t->all_px, npx, wl, hl, layer, t->T, t->calib,
+                                              t->cur6[layer], t->curmask[layer], np, t->icp_res, t->icp_J, t->icp_wpx,
                                               t->cfg.opt_scale_in);
                     const float *J6[6];
                     for (int c = 0; c < 6; c++) J6[c] = t->icp_J + (size_t)c * np;
@@ -1671,6 +1684,7 @@ int orc_get_array(orc_tracker *t, const char *name, int level, void *dst, int64_
     else if (!strcmp(name, "T")) { src = t->T; n = 64; }
     else if (!strcmp(name, "icp_w")) { src = t->icp_w; n = (int64_t)t->nsel[level] * 4; }
     else if (!strcmp(name, "icp_select")) { src = t->select; n = (int64_t)t->nsel[level] * 4; }
+    else if (!strcmp(name, "icp_w_px")) { src = t->icp_wpx; n = (int64_t)W * H * 4; }
     else return -1;
     if (n > nbytes) return -2;
     memcpy(dst, src, (size_t)n);

@@ -112,6 +112,8 @@ def lib() -> ctypes.CDLL:
             L.recon_batch_get_poses.argtypes = [vp, vp, vp]
             L.recon_batch_set_iterations.argtypes = [vp, i32, vp]
             L.recon_batch_set_mode.argtypes = [vp, i32, i32, f32]
+            L.recon_batch_set_icp_chunks_per_cta.argtypes = [vp, vp]
+            L.recon_batch_get_icp_chunks_per_cta.argtypes = [vp, vp]
             L.recon_batch_enable_trace.argtypes = [vp, i32]
             L.recon_batch_get_trace.argtypes = [vp, i32, vp, i32]
             L.recon_batch_get_array.argtypes = [vp, i32, ctypes.c_char_p, i32, vp, i64]
@@ -317,6 +319,16 @@ class Batch:
     def set_mode(self, inst: int, mode: int, lam: float):
         check(lib().recon_batch_set_mode(self.h, inst, mode, lam))
 
+    def set_icp_chunks_per_cta(self, per_level):
+        """ICP chunks of 1024 pixels per linearisation CTA at each level (0: built-in)."""
+        v = (ctypes.c_int32 * 4)(*(list(per_level) + [0] * 4)[:4])
+        check(lib().recon_batch_set_icp_chunks_per_cta(self.h, ctypes.cast(v, ctypes.c_void_p)))
+
+    def icp_chunks_per_cta(self):
+        v = (ctypes.c_int32 * 4)()
+        check(lib().recon_batch_get_icp_chunks_per_cta(self.h, ctypes.cast(v, ctypes.c_void_p)))
+        return list(v)
+
     def enable_trace(self, max_iters: int):
         check(lib().recon_batch_enable_trace(self.h, max_iters))
 
@@ -349,8 +361,7 @@ class Batch:
         return out[: n // out.itemsize]
 
 
-TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_compact", "icp_student_t", "prep_current", "prep_reference",
-                "gn_solve"]
+TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_student_t", "prep_current", "prep_reference", "gn_solve"]
 
 
 def launch_count() -> int:

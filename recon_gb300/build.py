@@ -53,6 +53,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
     flags = [ARCH, "-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
              "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-diag-suppress", "550"]
+    # extra nvcc options (e.g. -DRECON_ITER_MIN_BLOCKS=3) for tuning builds
+    flags += os.environ.get("RECON_NVCC_EXTRA", "").split()
 
     def compile_unit(u):
         obj = os.path.join(BUILD, u.replace(".cu", ".o"))

@@ -30,7 +30,6 @@ __global__ void k_seg_scan(const InstDesc *D, const int *active);
 __global__ void k_seg_scatter(const InstDesc *D, const int *active);
 __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
-__global__ void k_icp_compact(const InstDesc *D, int level);
 __global__ void k_icp_student3(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
 __global__ void k_solve(const InstDesc *D, int level, int it);
@@ -132,6 +131,8 @@ struct recon_batch {
     bool graph_dirty = true;
     int max_pix = 0, max_L = 0, max_P = 0;
     long long graph_kernels = 0;
+    // ICP chunks of 1024 pixels per k_iter CTA at each level (0: built-in choice)
+    int icp_cpc[kMaxLevels] = {0, 0, 0, 0};
     // optional per-launch CUDA-event timing (kinds: see TimingKind)
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> graph_events, direct_events;
@@ -225,15 +226,12 @@ size_t layout(InstDesc &d, char *base) {
     d.ph_r = a.take<float>(P);
     d.ph_zw = a.take<float>(P);
     d.ph_hist = a.take<int>(1024);
-    d.icp_res = a.take<float>(n);
     d.icp_mask = a.take<uint8_t>(n);
-    int nblk = (n + kChunk - 1) / kChunk;
-    d.icp_blkcnt = a.take<int>(nblk);
-    d.icp_select = a.take<int>(n);
     d.icp_r2 = a.take<float>(n);
     d.icp_w = a.take<float>(n);
-    d.icp_pk_pts = a.take<float4>(n);
-    d.icp_pk_nrm = a.take<float4>(n);
+    int nblk = (n + kChunk - 1) / kChunk;
+    d.icp_blkcnt = a.take<int>(nblk);
+    d.icp_blkvar = a.take<long long>(nblk);
     d.icp_var = a.take<unsigned long long>(4);
     d.icp_nsel = a.take<int>(kMaxLevels);
     d.fuse_c2 = a.take<double>(kMaxLevels);
@@ -309,7 +307,7 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
 
 dim3 grid_pix(int pix, int n, int block = 256) { return dim3((pix + block - 1) / block, n, 1); }
 
-enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_COMPACT, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_COUNT };
+enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_COUNT };
 
 // brackets one launch with a pair of events when timing is enabled; events
 // recorded during stream capture become graph nodes and are re-recorded by
@@ -410,6 +408,15 @@ int prepare_current(recon_batch *b, const void **in = nullptr, const int *active
     return RECON_OK;
 }
 
+// ICP chunks per k_iter CTA at `level` for a level whose largest instance has
+// `nchunk` chunks: the tuned value, else about five waves of CTAs over the
+// batch's chunks, at most 8 chunks each.  The result does not depend on it.
+int icp_per_cta(const recon_batch *b, int level, int nchunk) {
+    if (b->icp_cpc[level] > 0) return b->icp_cpc[level];
+    int waves = 5 * kIterCtaSlots;
+    return std::min(8, std::max(1, (b->n * nchunk + waves / 2) / waves));
+}
+
 // the per-frame Gauss-Newton schedule (gpuEstimateIncrement, phototracker.cpp:666-689)
 int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
     int n = b->n;
@@ -434,18 +441,12 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
                 k_icp_mask<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
             }
             {
-                TimedScope ts(b, s, TK_ICP_COMPACT, in_graph);
-                k_icp_compact<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
-            }
-            {
                 TimedScope ts(b, s, TK_ICP_STUDENT, in_graph);
                 k_icp_student3<<<dim3(kIterCluster, n), 1024, 0, s>>>(D, level);
             }
-            b->graph_kernels += 3;
+            b->graph_kernels += 2;
         }
-        // ICP chunks per CTA: enough CTAs for about four waves of the batch's
-        // chunks, at most 8 chunks each (the result does not depend on it)
-        int per_cta = std::min(8, std::max(1, (n * nchunk) / (8 * kIterCtaSlots)));
+        int per_cta = icp_per_cta(b, level, nchunk);
         int ncta = (nchunk + per_cta - 1) / per_cta;
         // the photometric cluster, then the ICP CTAs rounded up to whole clusters
         int gx = kIterCluster + (any_icp ? (ncta + kIterCluster - 1) / kIterCluster * kIterCluster : 0);
@@ -895,6 +896,31 @@ int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters
     return upload_desc(b);
 }
 
+int recon_batch_set_icp_chunks_per_cta(recon_batch *b, const int32_t per_level[RECON_MAX_LEVELS]) {
+    clear_stale_error();
+    if (!b || !per_level) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    for (int l = 0; l < kMaxLevels; l++)
+        if (per_level[l] < 0 || per_level[l] > 64) return fail(RECON_ERR_INVALID_ARG, "chunks per CTA out of [0, 64]");
+    CK(cudaStreamSynchronize(b->stream));
+    for (int l = 0; l < kMaxLevels; l++) b->icp_cpc[l] = per_level[l];
+    b->graph_dirty = true;
+    return RECON_OK;
+}
+
+int recon_batch_get_icp_chunks_per_cta(recon_batch *b, int32_t per_level[RECON_MAX_LEVELS]) {
+    clear_stale_error();
+    if (!b || !per_level) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    for (int l = 0; l < kMaxLevels; l++) {
+        int maxpix = 0;
+        for (int i = 0; i < b->n; i++) {
+            const recon_config &c = b->cfg[i];
+            if (l < c.levels) maxpix = std::max(maxpix, (c.width >> l) * (c.height >> l));
+        }
+        per_level[l] = maxpix ? icp_per_cta(b, l, (maxpix + kChunk - 1) / kChunk) : 0;
+    }
+    return RECON_OK;
+}
+
 int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambda) {
     clear_stale_error();
     if (!b || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
@@ -972,12 +998,9 @@ int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, in
     else if (nm == "grad_hist") { src = d.grad_hist; sz = (int64_t)d.select_bins * 4; }
     else if (nm == "T") { src = d.T; sz = 64; }
     else if (nm == "icp_nsel") { src = d.icp_nsel; sz = 16; }
-    else if (nm == "icp_select" || nm == "icp_w") {
-        int nsel = 0;
-        CK(cudaMemcpy(&nsel, d.icp_nsel + level, 4, cudaMemcpyDeviceToHost));
-        src = (nm == "icp_select") ? (const void *)d.icp_select : (const void *)d.icp_w;
-        sz = (int64_t)nsel * 4;
-    } else return fail(RECON_ERR_INVALID_ARG, "unknown array");
+    else if (nm == "icp_mask") { src = d.icp_mask; sz = (int64_t)W * H; }
+    else if (nm == "icp_w") { src = d.icp_w; sz = (int64_t)W * H * 4; }
+    else return fail(RECON_ERR_INVALID_ARG, "unknown array");
     if (sz > nbytes) return fail(RECON_ERR_INVALID_ARG, "destination too small");
     CK(cudaStreamSynchronize(b->stream));
     CK(cudaMemcpy(host_dst, src, sz, cudaMemcpyDeviceToHost));

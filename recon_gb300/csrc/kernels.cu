@@ -522,28 +522,49 @@ __global__ void k_attr_jac(const InstDesc *D, const int *active) {
 // ICP: correspondence mask, compaction, Student-t weights
 // ------------------------------------------------------------------
 
-// icpResidualKernel2, rgb2gray.cu:223-260: full-grid residual and mask at a
-// level; per-block (1024 pixels) valid counts for the stable compaction.
+// (long long)x for 0 <= x < 2^63 (or x = -0) from the bits of x with integer
+// operations: the float -> int64 conversion instruction issues on the FP64
+// pipe, which is narrow on this GPU.
+__device__ __forceinline__ long long trunc_f32_nonneg(float x) {
+    uint32_t bits = __float_as_uint(x) & 0x7fffffffu;
+    int E = (int)(bits >> 23);
+    if (E < 127) return 0;  // x < 1
+    uint64_t m = (uint64_t)((bits & 0x7fffffu) | 0x800000u);
+    int sh = E - 150;
+    return (long long)(sh >= 0 ? (m << sh) : (m >> -sh));
+}
+
+// the reference's int truncation of r^2 w (estimateVariance1024, rgb2gray.cu:519-521)
+__device__ __forceinline__ long long trunc_prod(float r2, float w) {
+    float prod = r2 * w;
+    return (prod >= 0.0f && prod < 9.0e18f) ? trunc_f32_nonneg(prod) : (prod >= 9.0e18f ? 9000000000000000000LL : 0);
+}
+
+// icpResidualKernel2 (rgb2gray.cu:223-260) with initWeightsKernel's first
+// Student-t weight (rgb2gray.cu:827-850): per pixel of the level, whether it is
+// a correspondence at the level's start pose and its squared residual; per
+// block of 1024 pixels the number of correspondences and the exact int64 sum
+// of the truncated r^2 w0 products (the first variance sum).  The ICP sums of
+// the iterations run over the pixel grid, so no compacted list is built.
 __global__ void k_icp_mask(const InstDesc *D, int level) {
     INST_DESC;
     if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
     if (d.iters[d.L - 1 - level] <= 0) return;
     int w = d.W >> level, h = d.H >> level, n = w * h;
-    __shared__ int s_cnt;
-    if (threadIdx.x == 0) s_cnt = 0;
-    if (blockIdx.x == 0 && threadIdx.x < 4) d.icp_var[threadIdx.x] = 0ull;
+    __shared__ int s_cnt[kLanes / 32];
+    __shared__ long long s_var[kLanes / 32];
     if (blockIdx.x == 0 && threadIdx.x == 0) d.work[2] += (unsigned long long)n;
-    __syncthreads();
     const float *T = d.T;
     const float *K = d.calib + RC_KL;
     float a = 1.0f / (float)(1 << level);
     float b = 0.5f * (a - 1.0f);
     int cnt = 0;
+    long long vsum = 0;
     for (int m = 0; m < 4; m++) {
         int i = blockIdx.x * kChunk + threadIdx.x + kLanes * m;
         if (i >= n) break;
         uint8_t ok = 0;
-        float res = 0.0f;
+        float r2 = 0.0f;
         float4 p = d.ref_pts[level][i];
         if (p.w != 0.0f) {
             float4 rn = d.ref_nrm[level][i];
@@ -561,93 +582,36 @@ __global__ void k_icp_mask(const InstDesc *D, int level) {
                 bilin_pts(d.cur_pts[level], off2, w, fx, fy, cx, cy, cz, m0, m1, m2, m3);
                 if (m0 != 0.0f && m1 != 0.0f && m2 != 0.0f && m3 != 0.0f) {
                     float dx = cx - qx, dy = cy - qy, dz = cz - qz;
-                    res = dx * cnx + dy * cny + dz * cnz;
+                    float res = dx * cnx + dy * cny + dz * cnz;
+                    r2 = res * res;
+                    float w0 = 6 / (5 + r2 / 100.0f);
+                    vsum += trunc_prod(r2, w0);
                     ok = 1;
                 }
             }
         }
-        d.icp_res[i] = res;
+        d.icp_r2[i] = r2;
         d.icp_mask[i] = ok;
         cnt += ok;
     }
     cnt = __reduce_add_sync(0xffffffffu, cnt);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&s_cnt, cnt);
+    for (int o = 16; o > 0; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
+    int wid = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_cnt[wid] = cnt;
+        s_var[wid] = vsum;
+    }
     __syncthreads();
-    if (threadIdx.x == 0) d.icp_blkcnt[blockIdx.x] = s_cnt;
-}
-
-__device__ __forceinline__ long long trunc_prod(float r2, float w) {
-    float prod = r2 * w;
-    return (prod >= 0.0f && prod < 9.0e18f) ? (long long)prod : (prod >= 9.0e18f ? 9000000000000000000LL : 0);
-}
-
-__device__ __forceinline__ void block_add_ll(unsigned long long *dst, long long v) {
-    __shared__ long long s_acc;
-    if (threadIdx.x == 0) s_acc = 0;
-    __syncthreads();
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd((unsigned long long *)&s_acc, (unsigned long long)v);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_acc != 0) atomicAdd(dst, (unsigned long long)s_acc);
-}
-
-// selectValidIndex + packIndex + initWeightsKernel (rgb2gray.cu:395-475,
-// 827-850): stable compaction in pixel order, r^2, first Student-t weight and
-// the first variance sum (exact int64 sum of truncated products).
-__global__ void k_icp_compact(const InstDesc *D, int level) {
-    INST_DESC;
-    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
-    if (d.iters[d.L - 1 - level] <= 0) return;
-    int w = d.W >> level, h = d.H >> level, n = w * h;
-    int nblk = (n + kChunk - 1) / kChunk;
-    if ((int)blockIdx.x >= nblk) return;
-    __shared__ int s_base, s_tot;
-    __shared__ int s_warp[8];
-    if (threadIdx.x < 32) {
-        int pre = 0, tot = 0;
-        for (int k = threadIdx.x; k < nblk; k += 32) {
-            int c = d.icp_blkcnt[k];
-            tot += c;
-            if (k < (int)blockIdx.x) pre += c;
+    if (threadIdx.x == 0) {
+        int c = 0;
+        long long v = 0;
+        for (int k = 0; k < kLanes / 32; k++) {
+            c += s_cnt[k];
+            v += s_var[k];
         }
-        pre = __reduce_add_sync(0xffffffffu, pre);
-        tot = __reduce_add_sync(0xffffffffu, tot);
-        if (threadIdx.x == 0) { s_base = pre; s_tot = tot; }
+        d.icp_blkcnt[blockIdx.x] = c;
+        d.icp_blkvar[blockIdx.x] = v;
     }
-    __syncthreads();
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        d.icp_nsel[level] = s_tot;
-        // ICP weight of the fused system, kept off the iteration's critical path
-        d.fuse_c2[level] = (double)d.lambda / (double)s_tot;
-    }
-    int base = s_base;
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    long long vsum = 0;
-    for (int m = 0; m < 4; m++) {
-        int i = blockIdx.x * kChunk + threadIdx.x + kLanes * m;
-        int f = (i < n) ? d.icp_mask[i] : 0;
-        unsigned int bal = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) s_warp[wid] = __popc(bal);
-        __syncthreads();
-        int wbase = 0;
-        for (int k = 0; k < wid; k++) wbase += s_warp[k];
-        int tot = 0;
-        for (int k = 0; k < 8; k++) tot += s_warp[k];
-        if (f) {
-            int pos = base + wbase + __popc(bal & ((1u << lane) - 1u));
-            float r = d.icp_res[i];
-            float r2 = r * r;
-            float w0 = 6 / (5 + r2 / 100.0f);
-            d.icp_select[pos] = i;
-            d.icp_r2[pos] = r2;
-            d.icp_pk_pts[pos] = d.ref_pts[level][i];
-            d.icp_pk_nrm[pos] = d.ref_nrm[level][i];
-            vsum += trunc_prod(r2, w0);
-        }
-        base += tot;
-        __syncthreads();
-    }
-    block_add_ll(&d.icp_var[0], vsum);
 }
 
 // ------------------------------------------------------------------
@@ -856,22 +820,32 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
     }
 }
 
-// icpResidualIndexKernel2, rgb2gray.cu:323-390, for one point.  The selected
-// reference point and normal were packed in selection order by k_icp_compact;
-// the Student-t weight is the last pass's.
-__device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int level, int idx, int nsel, float *j,
-                                          float &res) {
+// The inputs of ICP pixel `idx` of the level: its last Student-t weight and
+// its reference point and normal (weight 0 past the end of the grid).
+__device__ __forceinline__ void icp_load(const InstDesc &d, int level, int idx, int npix, float &weight, float4 &p,
+                                         float4 &rn) {
+    weight = 0.0f;
+    p = rn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (idx < npix) {
+        weight = __ldg(d.icp_w + idx);
+        p = __ldg(d.ref_pts[level] + idx);
+        rn = __ldg(d.ref_nrm[level] + idx);
+    }
+}
+
+// icpResidualIndexKernel2, rgb2gray.cu:323-390, for one pixel of the level.  A
+// pixel that is not a correspondence has weight 0, and the reference's test
+// `weight > 0` then gives zeros.
+__device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int level, float weight, float4 p,
+                                          float4 rn, float *j, float &res) {
     res = 0.0f;
 #pragma unroll
     for (int c = 0; c < 6; c++) j[c] = 0.0f;
-    if (idx >= nsel) return;
+    if (!(weight > 0.0f)) return;
     int w = d.W >> level, h = d.H >> level;
     const float *K = d.calib + RC_KL;
     float a = 1.0f / (float)(1 << level);
     float b = 0.5f * (a - 1.0f);
-    float4 p = __ldg(d.icp_pk_pts + idx);
-    float4 rn = __ldg(d.icp_pk_nrm + idx);
-    float weight = __ldg(d.icp_w + idx);
     float qx, qy, qz, cnx, cny, cnz;
     mul4(T, p.x, p.y, p.z, qx, qy, qz);
     rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
@@ -884,7 +858,7 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     int off2 = xdi + ydi * w;
     float cx, cy, cz, m0, m1, m2, m3;
     bilin_pts(d.cur_pts[level], off2, w, fx, fy, cx, cy, cz, m0, m1, m2, m3);
-    if (!(m0 != 0.0f && weight > 0.0f && fabsf(cz - qz) < 300.0f)) return;
+    if (!(m0 != 0.0f && fabsf(cz - qz) < 300.0f)) return;
     float optScaleIn = d.opt_in;
     float rvx = cx - qx, rvy = cy - qy, rvz = cz - qz;
     res = optScaleIn * weight * (rvx * cnx + rvy * cny + rvz * cnz);
@@ -1019,10 +993,10 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
     return rank < nph;
 }
 
-// ICP chunks [c0, c1) of an instance: lane t evaluates points t + 256m of each
-// chunk (icpResidualIndexKernel2 and the reference's per-point Jacobian), the
-// warp totals of each chunk go into the CTA's fixed-point sums.
-__device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0, int c1, int nsel) {
+// ICP chunks [c0, c1) of 1024 pixels of the level: lane t evaluates pixels
+// t + 256m of each chunk (icpResidualIndexKernel2 and the reference's per-point
+// Jacobian), the warp totals of each chunk go into the CTA's fixed-point sums.
+__device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0, int c1, int npix) {
     int t = threadIdx.x, lane = t & 31;
     for (int c = c0; c < c1; c++) {
         float acc[27];
@@ -1031,9 +1005,14 @@ __device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0,
 #pragma unroll
         for (int g = 0; g < 2; g++) {
             int i = c * kChunk + t + kLanes * (2 * g);
+            // both pixels' loads are in flight before either is evaluated
+            float wa, wb;
+            float4 pa, na, pb, nb;
+            icp_load(d, level, i, npix, wa, pa, na);
+            icp_load(d, level, i + kLanes, npix, wb, pb, nb);
             float ja[6], ra, jb[6], rb;
-            icp_point(d, sh.T, level, i, nsel, ja, ra);
-            icp_point(d, sh.T, level, i + kLanes, nsel, jb, rb);
+            icp_point(d, sh.T, level, wa, pa, na, ja, ra);
+            icp_point(d, sh.T, level, wb, pb, nb, jb, rb);
             acc27(acc, ja, ra);
             acc27(acc, jb, rb);
         }
@@ -1144,7 +1123,7 @@ __device__ __forceinline__ void load_desc(InstDesc &sd, const InstDesc *src_desc
 // The linearisation of one GN iteration at `level`, iteration `it`, for every
 // instance (blockIdx.y).  blockIdx.x 0..7: the photometric cluster of the
 // instance (updateLinearSystem, phototracker.cpp:505-511); blockIdx.x = 8 + j:
-// ICP chunks [j K, (j+1) K) of 1024 correspondences, K = icp_per_cta
+// ICP chunks [j K, (j+1) K) of 1024 pixels, K = icp_per_cta
 // (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).  Every CTA adds
 // its fixed-point sums to the instance's with integer atomics, so the result
 // does not depend on K or on the order in which CTAs finish; k_solve then
@@ -1163,8 +1142,9 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
     int nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
-    int nchunks = (nsel + kChunk - 1) / kChunk;
-    int nicp = (nchunks + icp_per_cta - 1) / icp_per_cta;
+    int npix = (d.W >> level) * (d.H >> level);
+    int nchunks = (npix + kChunk - 1) / kChunk;
+    int nicp = nsel > 0 ? (nchunks + icp_per_cta - 1) / icp_per_cta : 0;
     int role = blockIdx.x;
     int set;  // which sums this CTA adds to: 0 photometric, 1 ICP
     if (role < kCluster) {
@@ -1182,7 +1162,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
         if (!photo_cluster(d, sh, level, role)) return;
     } else {
         int c0 = (role - kCluster) * icp_per_cta;
-        icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), nsel);
+        icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), npix);
     }
     __syncthreads();
     fx_flush(sh, d.fx + set * kFxTerms, d.fx_bad + set);
@@ -1208,39 +1188,96 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int 
 }
 
 // The three Student-t passes of a level in one launch (updateWeightsKernel /
-// clampWeightsKernel, rgb2gray.cu:549-569): each pass weighs every
-// correspondence with the variance of the previous pass; the final pass clamps
-// at 1 and writes the weights, the first two produce only their variance sums
-// (exact int64 sums of truncated products).  An 8-CTA cluster per instance
-// (blockIdx.y) splits the correspondences and exchanges the CTAs' sums through
-// distributed shared memory, so no pass waits for a separate launch.
+// clampWeightsKernel, rgb2gray.cu:549-569) over the level's pixel grid: each
+// pass weighs every correspondence with the variance of the previous pass; the
+// final pass clamps at 1 and writes every pixel's weight (0 where the pixel is
+// not a correspondence), the first two produce only their variance sums (exact
+// int64 sums of truncated products).  An 8-CTA cluster per instance
+// (blockIdx.y) splits the pixels and exchanges the CTAs' sums through
+// distributed shared memory, so no pass waits for a separate launch.  Two
+// CTAs fit on an SM, so a batch of up to 38 instances runs in one wave.  The
+// correspondence count and the first sum are k_icp_mask's block totals.
 constexpr int kStudentThreads = 1024;
 
-__global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads)
+__device__ __forceinline__ float student_w(float r2, float sigma2) { return 6 / (5 + r2 / sigma2); }
+
+__global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads, 2)
     k_icp_student3(const InstDesc *D, int level) {
     __shared__ InstDesc sd;
     __shared__ long long part[2];
     __shared__ long long warp_sum[kStudentThreads / 32];
+    __shared__ int warp_cnt[kStudentThreads / 32];
+    __shared__ long long s_var0;
+    __shared__ int s_nsel;
     load_desc(sd, D + blockIdx.y);
     __syncthreads();
     const InstDesc &d = sd;
     if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
     if (d.iters[d.L - 1 - level] <= 0) return;  // uniform over the cluster
-    int nsel = __ldcg(d.icp_nsel + level);
+    int n = (d.W >> level) * (d.H >> level);
+    int nblk = (n + kChunk - 1) / kChunk;
     int rank = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    {
+        int c = 0;
+        long long v = 0;
+        for (int k = t; k < nblk; k += kStudentThreads) {
+            c += __ldcg(d.icp_blkcnt + k);
+            v += __ldcg(d.icp_blkvar + k);
+        }
+        c = __reduce_add_sync(0xffffffffu, c);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) {
+            warp_cnt[wid] = c;
+            warp_sum[wid] = v;
+        }
+        __syncthreads();
+        if (t == 0) {
+            int cs = 0;
+            long long vs = 0;
+            for (int w = 0; w < kStudentThreads / 32; w++) {
+                cs += warp_cnt[w];
+                vs += warp_sum[w];
+            }
+            s_nsel = cs;
+            s_var0 = vs;
+        }
+        __syncthreads();
+    }
+    int nsel = s_nsel;
+    long long var = s_var0;
+    if (rank == 0 && t == 0) {
+        d.icp_nsel[level] = nsel;
+        // ICP weight of the fused system, kept off the iteration's critical path
+        d.fuse_c2[level] = (double)d.lambda / (double)nsel;
+        d.icp_var[0] = (unsigned long long)var;
+    }
     int stride = kIterCluster * kStudentThreads;
-    long long var = (long long)__ldcg(d.icp_var + 0);
     for (int pass = 1; pass <= 3; pass++) {
         float Sf = (float)var;
         float minVal = (float)nsel;
         float vv = (nsel <= 1024) ? Sf : (Sf < minVal ? minVal : Sf);
         float sigma2 = vv / (float)nsel;
         long long vsum = 0;
-        for (int i = rank * kStudentThreads + t; i < nsel; i += stride) {
-            float r2 = __ldg(d.icp_r2 + i);
-            float wv = 6 / (5 + r2 / sigma2);
-            if (pass == 3) d.icp_w[i] = fminf(wv, 1.0f);
-            else vsum += trunc_prod(r2, wv);
+        int i = rank * kStudentThreads + t;
+        float r_next = 0.0f;
+        uint8_t m_next = 0;
+        if (i < n) {
+            r_next = __ldg(d.icp_r2 + i);
+            m_next = __ldg(d.icp_mask + i);
+        }
+        for (; i < n; i += stride) {
+            // the next pixel's loads are in flight while this one is weighed
+            float r = r_next;
+            uint8_t mk = m_next;
+            if (i + stride < n) {
+                r_next = __ldg(d.icp_r2 + i + stride);
+                m_next = __ldg(d.icp_mask + i + stride);
+            }
+            if (pass == 3) {
+                d.icp_w[i] = mk ? fminf(student_w(r, sigma2), 1.0f) : 0.0f;
+            } else if (mk) {
+                vsum += trunc_prod(r, student_w(r, sigma2));
+            }
         }
         if (pass == 3) break;
         for (int o = 16; o > 0; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
@@ -1311,7 +1348,7 @@ __device__ __forceinline__ long long gate_cost_point(const InstDesc &d, const fl
     photo_residual(d.calib, T, a, b, __ldg(d.sel_xyz + i), __ldg(d.sel_xyz + P + i), __ldg(d.sel_xyz + 2 * P + i),
                    __ldg(d.sel_I[level] + i), d.cur_gray[level], w, h, d.cur_z, d.W, d.H, r, zw);
     float u = fabsf(r) * 1024.0f;
-    return (u >= 1024.0f || !(u == u)) ? 1024 : (long long)u;
+    return (u >= 1024.0f || !(u == u)) ? 1024 : (long long)(int)u;  // 0 <= u < 1024: a 32-bit conversion
 }
 
 // The learned start pose, step 1 (one warp per instance): the network's

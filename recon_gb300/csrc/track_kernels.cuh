@@ -50,14 +50,12 @@ struct InstDesc {
     float *ph_r, *ph_zw;
     int *ph_hist;     // [256,512) the last histogram (for the trace), [512] its median bin
     // ICP scratch
-    float *icp_res;          // W*H full-grid residual
-    uint8_t *icp_mask;       // W*H
-    int *icp_blkcnt;         // blocks of 1024 pixels
-    int *icp_select;         // W*H
-    float *icp_r2, *icp_w;   // W*H
-    float4 *icp_pk_pts;      // W*H: selected reference points in selection order (x y z mask)
-    float4 *icp_pk_nrm;      // W*H: their normals
-    unsigned long long *icp_var;  // 4
+    uint8_t *icp_mask;       // W*H: the pixel is a correspondence of the level
+    float *icp_r2;           // W*H: its squared residual at the level's start pose
+    float *icp_w;            // W*H: its Student-t weight, 0 where not selected
+    int *icp_blkcnt;         // per 1024-pixel block: correspondences
+    long long *icp_blkvar;   // per 1024-pixel block: first variance sum
+    unsigned long long *icp_var;  // 4: the variance sums of the passes
     int *icp_nsel;           // kMaxLevels
     double *fuse_c2;         // kMaxLevels: lambda / (ICP correspondences) of the level
     // fixed-point sums of the current iteration: [0,108) photometric, [108,216) ICP

@@ -146,6 +146,20 @@ def test_tracking_trace_matches_oracle(pair, mode):
     assert st.iterations == len(tro)
 
 
+def test_icp_correspondences_and_student_t_weights(pair):
+    """The finest level's correspondence mask (icpResidualKernel2) and the final
+    Student-t weights of every pixel (generateStudentTWeights), 0 where the pixel
+    is not a correspondence."""
+    trk, orc, T, st, To, tro = run_pair(pair, rg.BIOBJECTIVE)
+    n = pair.W * pair.H
+    mask = trk.get_array(0, "icp_mask", 0, np.uint8, n)
+    sel = orc.get("icp_select", 0, n, np.int32)
+    assert np.array_equal(np.flatnonzero(mask), sel), "correspondence mask"
+    assert st.icp_selected[0] == sel.size
+    assert_bitexact(trk.get_array(0, "icp_w", 0, np.float32, n), orc.get("icp_w_px", 0, n, np.float32),
+                    "Student-t weights per pixel")
+
+
 def test_cg_solver_matches_oracle():
     p = frame_pair(320, 240, seed=21)
     trk, orc, T, st, To, tro = run_pair(p, rg.BIOBJECTIVE, solver=rg.SOLVER_CG, iters=(10, 10, 10))
