@@ -408,6 +408,24 @@ int prepare_current(recon_batch *b, const void **in = nullptr, const int *active
     return RECON_OK;
 }
 
+// Launches a kernel of the per-frame schedule as a programmatic dependent of
+// the previous kernel in the stream (a programmatic edge inside a graph): it
+// may start while that kernel finishes and waits for it with pdl_wait.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // ICP chunks per k_iter CTA at `level` for a level whose largest instance has
 // `nchunk` chunks: the tuned value, else about five waves of CTAs over the
 // batch's chunks, at most 8 chunks each.  The result does not depend on it.
@@ -438,11 +456,11 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
         if (any_icp) {
             {
                 TimedScope ts(b, s, TK_ICP_MASK, in_graph);
-                k_icp_mask<<<dim3(nchunk, n), kLanes, 0, s>>>(D, level);
+                CK(launch_pdl(k_icp_mask, dim3(nchunk, n), dim3(kLanes), s, D, level));
             }
             {
                 TimedScope ts(b, s, TK_ICP_STUDENT, in_graph);
-                k_icp_student3<<<dim3(kIterCluster, n), 1024, 0, s>>>(D, level);
+                CK(launch_pdl(k_icp_student3, dim3(kIterCluster, n), dim3(1024), s, D, level));
             }
             b->graph_kernels += 2;
         }
@@ -453,11 +471,11 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
         for (int it = 0; it < maxit; it++) {
             {
                 TimedScope ts(b, s, TK_ITER, in_graph);
-                k_iter<<<dim3(gx, n), kIterBlock, 0, s>>>(D, level, it, per_cta);
+                CK(launch_pdl(k_iter, dim3(gx, n), dim3(kIterBlock), s, D, level, it, per_cta));
             }
             {
                 TimedScope ts(b, s, TK_SOLVE, in_graph);
-                k_solve<<<n, kSolveThreads, 0, s>>>(D, level, it);
+                CK(launch_pdl(k_solve, dim3(n), dim3(kSolveThreads), s, D, level, it));
             }
             b->graph_kernels += 2;
         }

@@ -547,12 +547,14 @@ __device__ __forceinline__ long long trunc_prod(float r2, float w) {
 // of the truncated r^2 w0 products (the first variance sum).  The ICP sums of
 // the iterations run over the pixel grid, so no compacted list is built.
 __global__ void k_icp_mask(const InstDesc *D, int level) {
+    pdl_trigger();
     INST_DESC;
     if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
     if (d.iters[d.L - 1 - level] <= 0) return;
     int w = d.W >> level, h = d.H >> level, n = w * h;
     __shared__ int s_cnt[kLanes / 32];
     __shared__ long long s_var[kLanes / 32];
+    pdl_wait();
     if (blockIdx.x == 0 && threadIdx.x == 0) d.work[2] += (unsigned long long)n;
     const float *T = d.T;
     const float *K = d.calib + RC_KL;
@@ -1133,12 +1135,14 @@ __device__ __forceinline__ void load_desc(InstDesc &sd, const InstDesc *src_desc
 #endif
 __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads, RECON_ITER_MIN_BLOCKS)
     k_iter(const InstDesc *D, int level, int it, int icp_per_cta) {
+    pdl_trigger();
     __shared__ InstDesc sd;
     load_desc(sd, D + blockIdx.y);
     __syncthreads();
     const InstDesc &d = sd;
     if (level >= d.L) return;
     if (it >= d.iters[d.L - 1 - level]) return;
+    pdl_wait();
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
     int nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
@@ -1173,12 +1177,14 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
 // (estimateIncrement, phototracker.cpp:646-664; linearFuse,
 // shapetracker.cpp:392-394).
 __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int level, int it) {
+    pdl_trigger();
     __shared__ InstDesc sd;
     load_desc(sd, D + blockIdx.x);
     __syncthreads();
     const InstDesc &d = sd;
     if (level >= d.L) return;
     if (it >= d.iters[d.L - 1 - level]) return;
+    pdl_wait();
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
     int nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
@@ -1203,6 +1209,7 @@ __device__ __forceinline__ float student_w(float r2, float sigma2) { return 6 / 
 
 __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads, 2)
     k_icp_student3(const InstDesc *D, int level) {
+    pdl_trigger();
     __shared__ InstDesc sd;
     __shared__ long long part[2];
     __shared__ long long warp_sum[kStudentThreads / 32];
@@ -1214,6 +1221,7 @@ __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentT
     const InstDesc &d = sd;
     if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
     if (d.iters[d.L - 1 - level] <= 0) return;  // uniform over the cluster
+    pdl_wait();
     int n = (d.W >> level) * (d.H >> level);
     int nblk = (n + kChunk - 1) / kChunk;
     int rank = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5;

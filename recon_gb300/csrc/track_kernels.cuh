@@ -70,6 +70,15 @@ struct InstDesc {
     int *trace_count;
 };
 
+// Programmatic dependent launch.  The kernels of the per-frame schedule are
+// launched so that the next kernel may start while this one finishes:
+// pdl_trigger lets it be scheduled, and pdl_wait (griddepcontrol.wait) returns
+// once every earlier kernel of the stream has completed and its writes are
+// visible.  Before pdl_wait a kernel reads only the instance descriptors (not
+// written by any kernel of the schedule) and writes nothing.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 // k_iter copies a descriptor into shared memory as 32-bit words
 static_assert(sizeof(InstDesc) % sizeof(int) == 0, "InstDesc must be a whole number of words");
 
