@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="skip the learned-initialisation arm (profiling)")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile shapes instead of the autotuner's")
+    ap.add_argument("--tile", default=None, help="ICP chunks per CTA per level, e.g. 3,2,2,1 (no tuning)")
     return ap.parse_args()
 
 
@@ -331,7 +332,10 @@ def main():
     stream = torch.cuda.Stream()
     batch = make_batch(cal, len(segs), stream.cuda_stream)
     tile = None
-    if not args.no_tune:
+    if args.tile:
+        batch.set_icp_chunks_per_cta([int(v) for v in args.tile.split(",")])
+        tile = {"icp_chunks_per_cta": batch.icp_chunks_per_cta(), "autotuned": False}
+    elif not args.no_tune:
         # tile shape of the linearisation kernel, timed on the first frame of
         # every segment before any timed region (poses do not depend on it)
         from recon_gb300.tune import autotune_icp_chunks

@@ -5,7 +5,8 @@
  * function restates one reference kernel or host routine of ttykkala/recon and
  * cites the file:line it follows.  FP32 expressions are written in the
  * reference's source order; the library is compiled with -ffp-contract=off so
- * that no multiply-add is fused.  Reductions follow the canonical chunked tree
+ * that no multiply-add is fused implicitly (the canonical lane sums below call
+ * fmaf explicitly).  Reductions follow the canonical chunked tree
  * described at orc_reduce27; the tracker folds its FP32 warp values exactly in
  * fixed point (orc_reduce27_fx), the reference-named shim in FP64 order
  * (orc_reduce27).  The reference's own order is available as
@@ -580,7 +581,8 @@ int orc_generate_weights(const float *r, const float *zw, int N, int nbins, int3
  *
  * Order (identical in the CUDA kernels): N is split into chunks of 1024 points;
  * in chunk k, lane t (0..255) sums the products of points k*1024 + t + 256*m for
- * m = 0..3 in FP32; each warp of 32 lanes combines its lanes with an xor
+ * m = 0..3 in FP32, each product added with one fused multiply-add (fmaf, one
+ * rounding, identical on every IEEE platform); each warp of 32 lanes combines its lanes with an xor
  * butterfly (offsets 16, 8, 4, 2, 1) in FP32; the 8 warp values are converted to
  * FP64 and summed in warp order; chunk values are summed in chunk order in FP64.
  * Term order: the 21 upper-triangle JtJ terms (j <= i, row-major over j), then
@@ -600,8 +602,8 @@ static void chunk_warp_values(const float *const *J6, const float *r, int k, flo
                 for (int c = 0; c < 6; c++) jv[c] = J6[c][i];
                 int q = 0;
                 for (int j = 0; j < 6; j++)
-                    for (int ii = j; ii < 6; ii++) s[q++] += jv[j] * jv[ii];
-                for (int c = 0; c < 6; c++) s[q++] += jv[c] * r[i];
+                    for (int ii = j; ii < 6; ii++, q++) s[q] = fmaf(jv[j], jv[ii], s[q]);
+                for (int c = 0; c < 6; c++, q++) s[q] = fmaf(jv[c], r[i], s[q]);
             }
             for (int q = 0; q < 27; q++) lane[l][q] = s[q];
         }

@@ -630,7 +630,10 @@ struct __align__(16) IterShared {
     long long fx[27][kFxLimbs];  // this CTA's fixed-point sums of its warp totals
     int fx_bad;
     double A_ph[27];    // the allocation-free entry point's photometric terms
-    __align__(16) float J[6][kChunk];  // the photometric Jacobian of this CTA's first chunk
+    // photometric CTAs: the Jacobian of the CTA's first chunk; ICP CTAs: the
+    // Jacobians of the chunk being reduced (with R, its residuals)
+    __align__(16) float J[6][kChunk];
+    float R[kChunk];
     int hist[256];      // this CTA's photometric histogram (read by its cluster)
     int hist_all[256];  // the instance's histogram
     int median;
@@ -644,6 +647,10 @@ struct SolveShared {
     float T[16];
     double A_ph[27], A_icp[27];
     SolveScratch S;
+    // scalars loaded with the sums
+    double fuse_c2;
+    unsigned long long work0, work1;
+    int nsel, median, st_iters, st_solves, st_nonspd, trace_slot;
 };
 
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory"); }
@@ -681,15 +688,16 @@ __device__ __forceinline__ void fx_flush(const IterShared &sh, unsigned long lon
     if (threadIdx.x == 0 && sh.fx_bad) atomicOr(dst_bad, 1);
 }
 
-// canonical per-lane accumulation of the 27 normal-equation terms
+// canonical per-lane accumulation of the 27 normal-equation terms, one fused
+// multiply-add per product (the oracle's fmaf)
 __device__ __forceinline__ void acc27(float *s, const float *j, float r) {
     int q = 0;
 #pragma unroll
     for (int a = 0; a < 6; a++)
 #pragma unroll
-        for (int c = a; c < 6; c++) s[q++] += j[a] * j[c];
+        for (int c = a; c < 6; c++, q++) s[q] = __fmaf_rn(j[a], j[c], s[q]);
 #pragma unroll
-    for (int c = 0; c < 6; c++) s[q++] += j[c] * r;
+    for (int c = 0; c < 6; c++, q++) s[q] = __fmaf_rn(j[c], r, s[q]);
 }
 
 // Warp totals of the 27 terms by recursive halving: at the step with offset o
@@ -1001,22 +1009,36 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
 __device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0, int c1, int npix) {
     int t = threadIdx.x, lane = t & 31;
     for (int c = c0; c < c1; c++) {
+        // Phase 1: the lane's four pixels with no accumulators live; each
+        // result goes to the lane's own shared slots.
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            // two pixels at a time: both loads in flight, then both evaluated
+            float w[2];
+            float4 p[2], n[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) icp_load(d, level, c * kChunk + t + kLanes * (2 * g + u), npix, w[u], p[u], n[u]);
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                int m = 2 * g + u;
+                float j[6], r;
+                icp_point(d, sh.T, level, w[u], p[u], n[u], j, r);
+#pragma unroll
+                for (int k = 0; k < 6; k++) sh.J[k][t + kLanes * m] = j[k];
+                sh.R[t + kLanes * m] = r;
+            }
+        }
+        // Phase 2: the canonical per-lane sums in point order, from the slots
+        // this thread wrote (no barrier needed).
         float acc[27];
 #pragma unroll
         for (int q = 0; q < 27; q++) acc[q] = 0.0f;
 #pragma unroll
-        for (int g = 0; g < 2; g++) {
-            int i = c * kChunk + t + kLanes * (2 * g);
-            // both pixels' loads are in flight before either is evaluated
-            float wa, wb;
-            float4 pa, na, pb, nb;
-            icp_load(d, level, i, npix, wa, pa, na);
-            icp_load(d, level, i + kLanes, npix, wb, pb, nb);
-            float ja[6], ra, jb[6], rb;
-            icp_point(d, sh.T, level, wa, pa, na, ja, ra);
-            icp_point(d, sh.T, level, wb, pb, nb, jb, rb);
-            acc27(acc, ja, ra);
-            acc27(acc, jb, rb);
+        for (int m = 0; m < 4; m++) {
+            float j[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) j[k] = sh.J[k][t + kLanes * m];
+            acc27(acc, j, sh.R[t + kLanes * m]);
         }
         float v = warp_terms(acc);
         if (lane < 27) fx_add_term(sh, lane, v);
@@ -1032,27 +1054,50 @@ __device__ __forceinline__ int packed_index(int r, int c) {
 // for the next iteration), the system of the mode (fused in FP64 for
 // BIOBJECTIVE with weights precomputed off this path, linearFuseKernel
 // warp.cu:918-924), the solve and SE(3) update (warp 0), the statistics and
-// the optional trace.
+// the optional trace.  Every global value it reads is loaded in one round trip
+// at the start (threads 54..63 fetch the scalars), since the FP64 solve that
+// follows is a long serial chain.
 __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh, int level, int it, bool use_ph,
-                                              bool use_icp, int nsel) {
+                                              bool use_icp) {
     int t = threadIdx.x;
     SolveScratch &S = sh.S;
+    long long L[kFxLimbs];
+    int bad = 0;
+    unsigned long long *src = nullptr;
     if (t < 54) {
         int set = t / 27, q = t % 27;
-        unsigned long long *src = d.fx + set * kFxTerms + q * kFxLimbs;
-        long long L[kFxLimbs];
+        src = d.fx + set * kFxTerms + q * kFxLimbs;
 #pragma unroll
         for (int k = 0; k < kFxLimbs; k++) L[k] = (long long)__ldcg(src + k);
-        int bad = __ldcg(d.fx_bad + set);
+        bad = __ldcg(d.fx_bad + set);
+    } else if (t == 54) {
+        sh.nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
+    } else if (t == 55) {
+        sh.fuse_c2 = __ldcg(d.fuse_c2 + level);
+    } else if (t == 56) {
+        sh.median = use_ph ? __ldcg(d.ph_hist + 512) : -1;
+    } else if (t == 57) {
+        sh.st_iters = __ldcg(d.stats + ST_ITERS);
+        sh.st_solves = __ldcg(d.stats + ST_SOLVES);
+        sh.st_nonspd = __ldcg(d.stats + ST_NONSPD);
+    } else if (t == 58) {
+        sh.work0 = __ldcg(d.work + 0);
+        sh.work1 = __ldcg(d.work + 1);
+    } else if (t == 59) {
+        sh.trace_slot = d.trace ? __ldcg(d.trace_count) : 0;
+    }
+    if (t < 16) sh.T[t] = __ldcg(d.T + t);
+    if (t < 54) {
         double v = bad ? __longlong_as_double(0x7ff8000000000000LL) : fx_to_double(L);
-        (set ? sh.A_icp : sh.A_ph)[q] = v;
+        (t >= 27 ? sh.A_icp : sh.A_ph)[t % 27] = v;
 #pragma unroll
         for (int k = 0; k < kFxLimbs; k++) src[k] = 0ull;
     }
     __syncthreads();
     if (t < 2) d.fx_bad[t] = 0;
+    int nsel = sh.nsel;
     bool ok = !(use_icp && nsel <= 0);  // ShapeTracker "not enough points": no solve
-    int slot = d.trace ? *d.trace_count : 0;
+    int slot = sh.trace_slot;
     bool tr_on = d.trace && slot < d.trace_max;
     recon_iter_trace *tr = tr_on ? d.trace + slot : nullptr;
     if (t < 42) {
@@ -1061,7 +1106,7 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
         double v;
         if (d.mode == RECON_PHOTOMETRIC) v = aph;
         else if (d.mode == RECON_GEOMETRIC) v = aic;
-        else v = ok ? d.fuse_c1 * aph + d.fuse_c2[level] * aic : aph;  // (1-lambda)/P * photo + lambda/N * icp
+        else v = ok ? d.fuse_c1 * aph + sh.fuse_c2 * aic : aph;  // (1-lambda)/P * photo + lambda/N * icp
         if (t < 36) S.A[t] = v;
         else S.b[t - 36] = v;
         if (tr) {
@@ -1076,7 +1121,7 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
             }
         }
     }
-    int median = use_ph ? __ldcg(d.ph_hist + 512) : -1;
+    int median = sh.median;
     if (tr) {
         for (int k = t; k < 256; k += blockDim.x)
             tr->hist[k] = (use_ph && k < d.hist_bins) ? __ldcg(d.ph_hist + 256 + k) : 0;
@@ -1089,17 +1134,14 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
     if (lane < 16) d.T[lane] = sh.T[lane];
     if (tr && lane < 16) tr->T[lane] = sh.T[lane];
     if (lane == 0) {
-        // loads first, then stores: the counters are independent
         int *stt = d.stats;
         unsigned long long *wk = d.work;
-        int s_it = stt[ST_ITERS], s_so = stt[ST_SOLVES], s_ns = stt[ST_NONSPD];
-        unsigned long long w0 = wk[0], w1 = wk[1];
-        stt[ST_ITERS] = s_it + 1;
-        if (ok) stt[ST_SOLVES] = s_so + 1;
-        if (st != 0) stt[ST_NONSPD] = s_ns + 1;
+        stt[ST_ITERS] = sh.st_iters + 1;
+        if (ok) stt[ST_SOLVES] = sh.st_solves + 1;
+        if (st != 0) stt[ST_NONSPD] = sh.st_nonspd + 1;
         if (use_ph) stt[ST_MEDIAN] = median;
-        if (use_ph) wk[0] = w0 + (unsigned long long)d.P;
-        if (use_icp) wk[1] = w1 + (unsigned long long)nsel;
+        if (use_ph) wk[0] = sh.work0 + (unsigned long long)d.P;
+        if (use_icp) wk[1] = sh.work1 + (unsigned long long)nsel;
         if (use_icp) stt[ST_ICPSEL0 + level] = nsel;
         if (tr) {
             tr->level = level;
@@ -1187,10 +1229,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int 
     pdl_wait();
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
-    int nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
     __shared__ SolveShared sh;
-    if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
-    finalize_iter(d, sh, level, it, use_ph, use_icp, nsel);
+    finalize_iter(d, sh, level, it, use_ph, use_icp);
 }
 
 // The three Student-t passes of a level in one launch (updateWeightsKernel /

@@ -356,8 +356,8 @@ __global__ void __launch_bounds__(256) k_reduce27(const float *J, const float *r
         float rv = r ? r[i] : 0.0f;
         int q = 0;
         for (int aa = 0; aa < 6; aa++)
-            for (int cc = aa; cc < 6; cc++) acc[q++] += j[aa] * j[cc];
-        for (int cc = 0; cc < 6; cc++) acc[q++] += j[cc] * rv;
+            for (int cc = aa; cc < 6; cc++, q++) acc[q] = __fmaf_rn(j[aa], j[cc], acc[q]);
+        for (int cc = 0; cc < 6; cc++, q++) acc[q] = __fmaf_rn(j[cc], rv, acc[q]);
     }
     for (int q = 0; q < 27; q++) {
         float v = acc[q];
