@@ -21,6 +21,14 @@ namespace rt {
 
 #define INST_DESC const InstDesc &d = D[blockIdx.y]
 
+// Copies an instance descriptor (pointers, sizes, calibration) into shared
+// memory with one parallel load instead of a chain of dependent global loads.
+__device__ __forceinline__ void load_desc(InstDesc &sd, const InstDesc *src_desc) {
+    const int *src = reinterpret_cast<const int *>(src_desc);
+    int *dst = reinterpret_cast<int *>(&sd);
+    for (int k = threadIdx.x; k < (int)(sizeof(InstDesc) / sizeof(int)); k += blockDim.x) dst[k] = __ldg(src + k);
+}
+
 // ------------------------------------------------------------------
 // input conversion and pyramids
 // ------------------------------------------------------------------
@@ -540,61 +548,87 @@ __device__ __forceinline__ long long trunc_prod(float r2, float w) {
     return (prod >= 0.0f && prod < 9.0e18f) ? trunc_f32_nonneg(prod) : (prod >= 9.0e18f ? 9000000000000000000LL : 0);
 }
 
+// The residual and mask of pixel i of the level (icpResidualKernel2) from its
+// loaded reference point p and normal rn; returns the mask, sets r2.
+__device__ __forceinline__ uint8_t icp_mask_pixel(const InstDesc &d, const float *T, int level, float4 p, float4 rn,
+                                                  float &r2) {
+    r2 = 0.0f;
+    if (p.w == 0.0f) return 0;
+    int w = d.W >> level, h = d.H >> level;
+    const float *K = d.calib + RC_KL;
+    float a = 1.0f / (float)(1 << level);
+    float b = 0.5f * (a - 1.0f);
+    float qx, qy, qz, cnx, cny, cnz;
+    mul4(T, p.x, p.y, p.z, qx, qy, qz);
+    rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
+    float q2x = qx / qz, q2y = qy / qz;
+    float p2x = a * (K[0] * q2x + K[2]) + b;
+    float p2y = a * (K[4] * q2y + K[5]) + b;
+    if (!(p2x >= 0 && p2x < (w - 1) && p2y >= 0 && p2y < (h - 1))) return 0;
+    int xdi = ftoi(p2x), ydi = ftoi(p2y);
+    int off2 = xdi + ydi * w;
+    float fx = p2x - xdi, fy = p2y - ydi;
+    float cx, cy, cz, m0, m1, m2, m3;
+    bilin_pts(d.cur_pts[level], off2, w, fx, fy, cx, cy, cz, m0, m1, m2, m3);
+    if (!(m0 != 0.0f && m1 != 0.0f && m2 != 0.0f && m3 != 0.0f)) return 0;
+    float dx = cx - qx, dy = cy - qy, dz = cz - qz;
+    float res = dx * cnx + dy * cny + dz * cnz;
+    r2 = res * res;
+    return 1;
+}
+
 // icpResidualKernel2 (rgb2gray.cu:223-260) with initWeightsKernel's first
 // Student-t weight (rgb2gray.cu:827-850): per pixel of the level, whether it is
 // a correspondence at the level's start pose and its squared residual; per
 // block of 1024 pixels the number of correspondences and the exact int64 sum
 // of the truncated r^2 w0 products (the first variance sum).  The ICP sums of
 // the iterations run over the pixel grid, so no compacted list is built.
-__global__ void k_icp_mask(const InstDesc *D, int level) {
+__global__ void __launch_bounds__(kLanes) k_icp_mask(const InstDesc *D, int level) {
     pdl_trigger();
-    INST_DESC;
-    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
-    if (d.iters[d.L - 1 - level] <= 0) return;
-    int w = d.W >> level, h = d.H >> level, n = w * h;
+    __shared__ InstDesc sd;
+    __shared__ float sT[16];
     __shared__ int s_cnt[kLanes / 32];
     __shared__ long long s_var[kLanes / 32];
+    load_desc(sd, D + blockIdx.y);
+    __syncthreads();
+    const InstDesc &d = sd;
+    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
+    if (d.iters[d.L - 1 - level] <= 0) return;
+    int n = (d.W >> level) * (d.H >> level);
     pdl_wait();
+    if (threadIdx.x < 16) sT[threadIdx.x] = __ldcg(d.T + threadIdx.x);
     if (blockIdx.x == 0 && threadIdx.x == 0) d.work[2] += (unsigned long long)n;
-    const float *T = d.T;
-    const float *K = d.calib + RC_KL;
-    float a = 1.0f / (float)(1 << level);
-    float b = 0.5f * (a - 1.0f);
+    __syncthreads();
     int cnt = 0;
     long long vsum = 0;
-    for (int m = 0; m < 4; m++) {
-        int i = blockIdx.x * kChunk + threadIdx.x + kLanes * m;
-        if (i >= n) break;
-        uint8_t ok = 0;
-        float r2 = 0.0f;
-        float4 p = d.ref_pts[level][i];
-        if (p.w != 0.0f) {
-            float4 rn = d.ref_nrm[level][i];
-            float qx, qy, qz, cnx, cny, cnz;
-            mul4(T, p.x, p.y, p.z, qx, qy, qz);
-            rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
-            float q2x = qx / qz, q2y = qy / qz;
-            float p2x = a * (K[0] * q2x + K[2]) + b;
-            float p2y = a * (K[4] * q2y + K[5]) + b;
-            if (p2x >= 0 && p2x < (w - 1) && p2y >= 0 && p2y < (h - 1)) {
-                int xdi = ftoi(p2x), ydi = ftoi(p2y);
-                int off2 = xdi + ydi * w;
-                float fx = p2x - xdi, fy = p2y - ydi;
-                float cx, cy, cz, m0, m1, m2, m3;
-                bilin_pts(d.cur_pts[level], off2, w, fx, fy, cx, cy, cz, m0, m1, m2, m3);
-                if (m0 != 0.0f && m1 != 0.0f && m2 != 0.0f && m3 != 0.0f) {
-                    float dx = cx - qx, dy = cy - qy, dz = cz - qz;
-                    float res = dx * cnx + dy * cny + dz * cnz;
-                    r2 = res * res;
-                    float w0 = 6 / (5 + r2 / 100.0f);
-                    vsum += trunc_prod(r2, w0);
-                    ok = 1;
-                }
+#pragma unroll
+    for (int g = 0; g < 2; g++) {
+        // two pixels at a time: point and normal loads in flight together
+        int i0 = blockIdx.x * kChunk + threadIdx.x + kLanes * (2 * g);
+        float4 p[2], rn[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            int i = i0 + kLanes * u;
+            p[u] = rn[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (i < n) {
+                p[u] = __ldg(d.ref_pts[level] + i);
+                rn[u] = __ldg(d.ref_nrm[level] + i);
             }
         }
-        d.icp_r2[i] = r2;
-        d.icp_mask[i] = ok;
-        cnt += ok;
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            int i = i0 + kLanes * u;
+            if (i >= n) continue;
+            float r2;
+            uint8_t ok = icp_mask_pixel(d, sT, level, p[u], rn[u], r2);
+            if (ok) {
+                float w0 = 6 / (5 + r2 / 100.0f);
+                vsum += trunc_prod(r2, w0);
+            }
+            d.icp_r2[i] = r2;
+            d.icp_mask[i] = ok;
+            cnt += ok;
+        }
     }
     cnt = __reduce_add_sync(0xffffffffu, cnt);
     for (int o = 16; o > 0; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
@@ -1156,13 +1190,6 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
     }
 }
 
-// Copies an instance descriptor (pointers, sizes, calibration) into shared
-// memory with one parallel load instead of a chain of dependent global loads.
-__device__ __forceinline__ void load_desc(InstDesc &sd, const InstDesc *src_desc) {
-    const int *src = reinterpret_cast<const int *>(src_desc);
-    int *dst = reinterpret_cast<int *>(&sd);
-    for (int k = threadIdx.x; k < (int)(sizeof(InstDesc) / sizeof(int)); k += blockDim.x) dst[k] = __ldg(src + k);
-}
 
 // The linearisation of one GN iteration at `level`, iteration `it`, for every
 // instance (blockIdx.y).  blockIdx.x 0..7: the photometric cluster of the
