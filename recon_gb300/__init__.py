@@ -361,7 +361,8 @@ class Batch:
         return out[: n // out.itemsize]
 
 
-TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_student_t", "prep_current", "prep_reference", "gn_solve"]
+TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_student_t", "prep_current", "prep_reference", "gn_solve",
+                "icp_prepare"]
 
 
 def launch_count() -> int:

@@ -31,6 +31,7 @@ __global__ void k_seg_scatter(const InstDesc *D, const int *active);
 __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
 __global__ void k_icp_student3(const InstDesc *D, int level);
+__global__ void k_icp_prepare(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
 __global__ void k_solve(const InstDesc *D, int level, int it);
 __global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
@@ -307,7 +308,7 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
 
 dim3 grid_pix(int pix, int n, int block = 256) { return dim3((pix + block - 1) / block, n, 1); }
 
-enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_COUNT };
+enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_ICP_PREP, TK_COUNT };
 
 // brackets one launch with a pair of events when timing is enabled; events
 // recorded during stream capture become graph nodes and are re-recorded by
@@ -408,6 +409,11 @@ int prepare_current(recon_batch *b, const void **in = nullptr, const int *active
     return RECON_OK;
 }
 
+// Levels with at most this many pixels per instance prepare their ICP
+// correspondences and weights in one cluster launch (k_icp_prepare, at most
+// 16 pixels per thread); larger ones use the wide mask grid + k_icp_student3.
+constexpr int kPrepareFusedMaxPix = 16 * 8 * 1024;
+
 // Launches a kernel of the per-frame schedule as a programmatic dependent of
 // the previous kernel in the stream (a programmatic edge inside a graph): it
 // may start while that kernel finishes and waits for it with pdl_wait.
@@ -453,7 +459,12 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
         }
         if (maxit == 0) continue;
         int nchunk = (maxpix + kChunk - 1) / kChunk;
-        if (any_icp) {
+        if (any_icp && maxpix <= kPrepareFusedMaxPix) {
+            // small grid: mask and Student-t passes in one cluster launch
+            TimedScope ts(b, s, TK_ICP_PREP, in_graph);
+            CK(launch_pdl(k_icp_prepare, dim3(kIterCluster, n), dim3(1024), s, D, level));
+            b->graph_kernels += 1;
+        } else if (any_icp) {
             {
                 TimedScope ts(b, s, TK_ICP_MASK, in_graph);
                 CK(launch_pdl(k_icp_mask, dim3(nchunk, n), dim3(kLanes), s, D, level));

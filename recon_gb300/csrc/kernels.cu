@@ -1274,11 +1274,17 @@ constexpr int kStudentThreads = 1024;
 
 __device__ __forceinline__ float student_w(float r2, float sigma2) { return 6 / (5 + r2 / sigma2); }
 
-__global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads, 2)
-    k_icp_student3(const InstDesc *D, int level) {
-    pdl_trigger();
+// The body of the Student-t kernels.  With kMask the cluster first evaluates
+// the level's correspondences itself (k_icp_mask's per-pixel work, over the
+// same pixel-to-thread mapping as the passes, so every thread reads back only
+// what it wrote) and exchanges the count and first variance sum; without it
+// those come from k_icp_mask's block totals.
+template <bool kMask>
+__device__ __forceinline__ void student_body(const InstDesc *D, int level) {
     __shared__ InstDesc sd;
-    __shared__ long long part[2];
+    __shared__ float sT[16];
+    __shared__ long long part[3];
+    __shared__ int part_cnt;
     __shared__ long long warp_sum[kStudentThreads / 32];
     __shared__ int warp_cnt[kStudentThreads / 32];
     __shared__ long long s_var0;
@@ -1290,34 +1296,80 @@ __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentT
     if (d.iters[d.L - 1 - level] <= 0) return;  // uniform over the cluster
     pdl_wait();
     int n = (d.W >> level) * (d.H >> level);
-    int nblk = (n + kChunk - 1) / kChunk;
     int rank = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    {
-        int c = 0;
-        long long v = 0;
+    int stride = kIterCluster * kStudentThreads;
+    int c = 0;
+    long long v = 0;
+    if (kMask) {
+        if (t < 16) sT[t] = __ldcg(d.T + t);
+        if (rank == 0 && t == 0) d.work[2] += (unsigned long long)n;
+        __syncthreads();
+        for (int i0 = rank * kStudentThreads + t; i0 < n; i0 += 2 * stride) {
+            // two pixels at a time: point and normal loads in flight together
+            float4 p[2], rn[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                int i = i0 + u * stride;
+                p[u] = rn[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (i < n) {
+                    p[u] = __ldg(d.ref_pts[level] + i);
+                    rn[u] = __ldg(d.ref_nrm[level] + i);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                int i = i0 + u * stride;
+                if (i >= n) continue;
+                float r2;
+                uint8_t ok = icp_mask_pixel(d, sT, level, p[u], rn[u], r2);
+                if (ok) v += trunc_prod(r2, 6 / (5 + r2 / 100.0f));
+                d.icp_r2[i] = r2;
+                d.icp_mask[i] = ok;
+                c += ok;
+            }
+        }
+    } else {
+        int nblk = (n + kChunk - 1) / kChunk;
         for (int k = t; k < nblk; k += kStudentThreads) {
             c += __ldcg(d.icp_blkcnt + k);
             v += __ldcg(d.icp_blkvar + k);
         }
-        c = __reduce_add_sync(0xffffffffu, c);
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) {
-            warp_cnt[wid] = c;
-            warp_sum[wid] = v;
+    }
+    c = __reduce_add_sync(0xffffffffu, c);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+        warp_cnt[wid] = c;
+        warp_sum[wid] = v;
+    }
+    __syncthreads();
+    if (t == 0) {
+        int cs = 0;
+        long long vs = 0;
+        for (int w = 0; w < kStudentThreads / 32; w++) {
+            cs += warp_cnt[w];
+            vs += warp_sum[w];
         }
-        __syncthreads();
+        s_nsel = cs;
+        s_var0 = vs;
+        part[2] = vs;
+        part_cnt = cs;
+    }
+    if (kMask) {
+        cluster_arrive();
+        cluster_wait();  // every CTA's count and first sum are in its shared memory
         if (t == 0) {
             int cs = 0;
             long long vs = 0;
-            for (int w = 0; w < kStudentThreads / 32; w++) {
-                cs += warp_cnt[w];
-                vs += warp_sum[w];
+#pragma unroll
+            for (int r = 0; r < kIterCluster; r++) {
+                cs += *cluster_peer(&part_cnt, r);
+                vs += *cluster_peer(&part[2], r);
             }
             s_nsel = cs;
             s_var0 = vs;
         }
-        __syncthreads();
     }
+    __syncthreads();
     int nsel = s_nsel;
     long long var = s_var0;
     if (rank == 0 && t == 0) {
@@ -1326,7 +1378,6 @@ __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentT
         d.fuse_c2[level] = (double)d.lambda / (double)nsel;
         d.icp_var[0] = (unsigned long long)var;
     }
-    int stride = kIterCluster * kStudentThreads;
     for (int pass = 1; pass <= 3; pass++) {
         float Sf = (float)var;
         float minVal = (float)nsel;
@@ -1375,6 +1426,23 @@ __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentT
     // no CTA leaves while another may still read its sums
     cluster_arrive();
     cluster_wait();
+}
+
+__global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads, 2)
+    k_icp_student3(const InstDesc *D, int level) {
+    pdl_trigger();
+    student_body<false>(D, level);
+}
+
+// The whole ICP preparation of a level in one launch (mask, count, first sum,
+// three Student-t passes): for the coarser levels, where the grid is small
+// enough for one cluster per instance to evaluate it.  Two CTAs per SM, as for
+// k_icp_student3 (a few registers spill in the mask phase; measured faster
+// than one CTA per SM at 30 instances).
+__global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads, 2)
+    k_icp_prepare(const InstDesc *D, int level) {
+    pdl_trigger();
+    student_body<true>(D, level);
 }
 
 // ------------------------------------------------------------------
