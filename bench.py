@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="skip the learned-initialisation arm (profiling)")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile shapes instead of the autotuner's")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance mixed-resolution workload")
     ap.add_argument("--tile", default=None, help="ICP chunks per CTA per level, e.g. 3,2,2,1 (no tuning)")
     return ap.parse_args()
 
@@ -299,6 +300,133 @@ def error_summary(e):
             "median_deg": float(np.median(e[:, 1])), "max_deg": float(e[:, 1].max())}, ok
 
 
+# ---------------------------------------------------------------- batched workload
+BATCH_N = 256
+BATCH_RES = [(80, 60), (160, 120), (320, 240), (640, 480)]
+
+
+def batch_workload(seed: int, torch):
+    """The batched-tracking workload: 256 instances whose resolutions are drawn
+    uniformly from 80x60 / 160x120 / 320x240 / 640x480 (4 levels at 640, else 3),
+    each a seeded scene rendered at the identity and at a start offset of
+    0.5-4 deg about a random axis and 0.5-50 mm along a random direction,
+    4-12 Gauss-Newton iterations per level drawn per instance, and
+    N_sel = min(8192, floor(W*H/2/1024)*1024)."""
+    import recon_gb300 as rg
+    from recon_gb300 import synth
+    rng = np.random.default_rng(seed)
+    cals = {r: synth.make_calibration(*r) for r in BATCH_RES}
+    inst = []
+    for i in range(BATCH_N):
+        Wi, Hi = BATCH_RES[int(rng.integers(len(BATCH_RES)))]
+        L = 4 if Wi == 640 else 3
+        iters = tuple(int(v) for v in rng.integers(4, 13, size=L))
+        P = int(min(8192, (Wi * Hi // 2 // 1024) * 1024))
+        deg, mm = float(rng.uniform(0.5, 4.0)), float(rng.uniform(0.5, 50.0))
+        Tcur = synth.offset_pose(int(rng.integers(1 << 30)), deg, mm)
+        scene = synth.make_scene(int(rng.integers(1 << 30)))
+        cal = cals[(Wi, Hi)]
+        g = torch.empty((2, Hi, Wi), dtype=torch.uint8, device="cuda")
+        d = torch.empty((2, Hi, Wi), dtype=torch.int16, device="cuda")
+        for f, T in enumerate((np.eye(4), Tcur)):
+            rg.render_depth(scene, synth.camera_struct(cal, "L", T), 0.01, seed + 1, f, d[f])
+            rg.render_gray(scene, synth.camera_struct(cal, "R", T), g[f])
+        inst.append({"W": Wi, "H": Hi, "L": L, "iters": iters, "P": P, "cal": cal, "scene": scene, "Tcur": Tcur,
+                     "gt": synth.relative_pose(np.eye(4), Tcur), "g": g, "d": d,
+                     "cfg": rg.make_config(Wi, Hi, L, mode=rg.BIOBJECTIVE, iters=iters, n_select=P, lam=LAMBDA)})
+    torch.cuda.synchronize()
+    return inst
+
+
+def batch_arm(args, torch, world, rank, seed):
+    """Tracks the batched workload: one step tracks all 256 instances from the
+    identity (one graph replay of the whole per-level schedule).  Returns the
+    throughput, accuracy against the rendering poses, the per-kernel times and
+    the linearisation kernel's roofline."""
+    import recon_gb300 as rg
+    from recon_gb300 import synth
+    from recon_gb300.tune import autotune_icp_chunks
+    inst = batch_workload(seed, torch)
+    stream = torch.cuda.Stream()
+    b = rg.Batch([x["cfg"] for x in inst], [x["cal"].calib for x in inst], stream=stream.cuda_stream)
+    b.set_reference([x["g"][0] for x in inst], [x["d"][0] for x in inst])
+    b.set_current([x["g"][1] for x in inst], [x["d"][1] for x in inst])
+    T0 = np.tile(np.eye(4, dtype=np.float32), (BATCH_N, 1, 1))
+    chosen, _ = autotune_icp_chunks(b, T_init=T0)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        b.track_async(T0)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.track_async(T0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+    T, stats = b.poses()
+    err = np.array([synth.pose_error(T[i].astype(np.float64), inst[i]["gt"]) for i in range(BATCH_N)])
+    # per-kernel event timing and the work counters over the same K steps
+    b.enable_timing(True)
+    b.work(reset=True)
+    b.timing(reset=True)
+    for _ in range(args.steps):
+        b.track_async(T0)
+    torch.cuda.synchronize()
+    timing = b.timing(reset=True)
+    work = b.work(reset=True).astype(np.float64)
+    b.enable_timing(False)
+    it_ms, it_launches = timing["gn_iteration"]
+    bytes_iter = float(work[:, 0].sum() * B_PHOTO + work[:, 1].sum() * B_ICP)
+    peak, peak_kind = load_peaks()
+    achieved = bytes_iter / (it_ms / 1000.0) / 1e9 if it_ms > 0 else 0.0
+    pix = sum(x["W"] * x["H"] for x in inst)
+    out = {"workload": "256 instances, resolutions uniform over 80x60/160x120/320x240/640x480, bi-objective "
+                       "lambda=0.5, start offsets 0.5-4 deg / 0.5-50 mm, 4-12 iterations per level, "
+                       "N_sel=min(8192, floor(W*H/2/1024)*1024)",
+           "resolution_counts": {f"{w}x{h}": sum(1 for x in inst if x["W"] == w) for w, h in BATCH_RES},
+           "level0_pixels": pix, "gn_iterations": int(sum(sum(x["iters"]) for x in inst)),
+           "tracked_frames_per_s": world * BATCH_N * args.steps / (ms / 1000.0), "ms_per_step": ms / args.steps,
+           "tile": chosen[:4],
+           "vs_ground_truth": {"median_mm": float(np.median(err[:, 0])), "median_deg": float(np.median(err[:, 1])),
+                               "within_5mm_0.5deg": float(np.mean((err[:, 0] <= 5.0) & (err[:, 1] <= 0.5)))},
+           "kernel_ms_per_step": {k: v[0] / args.steps for k, v in timing.items() if v[1]},
+           "roofline_k_iter": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                               "peak_source": peak_kind, "launches_per_step": it_launches / args.steps}}
+    if rank == 0 and not args.no_cpu:
+        out["pose_error_vs_oracle"] = batch_oracle_check(inst, T)
+    b.close()
+    return out
+
+
+def batch_oracle_check(inst, T):
+    """One instance of each resolution tracked by the oracle from CPU-rendered
+    copies of the same frames; returns the largest pose difference."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    worst, checked = 0.0, []
+    for w, h in BATCH_RES:
+        i = next((k for k, x in enumerate(inst) if x["W"] == w), None)
+        if i is None:
+            continue
+        x = inst[i]
+        g0, d0 = x["g"][0].cpu().numpy(), x["d"][0].cpu().numpy()
+        g1, d1 = x["g"][1].cpu().numpy(), x["d"][1].cpu().numpy()
+        orc = O.OracleTracker(O.make_config(w, h, x["L"], mode=O.BIOBJECTIVE, iters=x["iters"], n_select=x["P"],
+                                            lam=LAMBDA), x["cal"].calib)
+        orc.set_reference(g0, d0.view(np.uint16))
+        orc.set_current(g1, d1.view(np.uint16))
+        To, _ = orc.track()
+        orc.close()
+        worst = max(worst, float(np.abs(To - T[i]).max()))
+        checked.append(i)
+    return {"instances": checked, "max_abs_pose_diff": worst, "bit_identical": worst == 0.0}
+
+
 def profiled_traffic():
     """DRAM bytes per average k_iter launch of this workload, from the committed
     ncu summary (profiles/k_iter_640x480_biobj_30inst.md), or None."""
@@ -473,6 +601,11 @@ def main():
         d2h = max(len(fr) for _, fr in segs) * len(segs) * (64 + 64)
         e2e = {"value": job_throughput(world, args.frames, args.steps, ms_e2e) * frac, "unit": "frames/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    # -------- the batched workload (256 mixed-resolution instances): a reported
+    # measurement beside the headline, with its own roofline
+    batched = None
+    if not args.no_batch:
+        batched = batch_arm(args, torch, world, rank, 5000 + 7919 * rank)
     clk.__exit__(None, None, None)
     if net is not None:
         batch.set_init_net(None)
@@ -533,6 +666,7 @@ def main():
             "pose_error_vs_oracle": oracle_err,
             "kernel_ms": {k: v[0] for k, v in timing.items()},
             "kernel_launches": {k: v[1] for k, v in timing.items()},
+            "batch256": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

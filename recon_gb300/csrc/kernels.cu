@@ -595,6 +595,9 @@ __global__ void __launch_bounds__(kLanes) k_icp_mask(const InstDesc *D, int leve
     if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
     if (d.iters[d.L - 1 - level] <= 0) return;
     int n = (d.W >> level) * (d.H >> level);
+    // the grid covers the batch's largest level; this instance has fewer blocks
+    // (its per-block arrays hold exactly that many entries)
+    if ((int)blockIdx.x >= (n + kChunk - 1) / kChunk) return;
     pdl_wait();
     if (threadIdx.x < 16) sT[threadIdx.x] = __ldcg(d.T + threadIdx.x);
     if (blockIdx.x == 0 && threadIdx.x == 0) d.work[2] += (unsigned long long)n;

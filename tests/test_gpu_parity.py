@@ -281,3 +281,29 @@ def test_keyframe_fusion_matches_oracle():
         orc.set_current(g[f], d[f])
         To, _ = orc.track(To)
         assert_bitexact(T6[f - 6, 0], To, f"frame {f} after fusion")
+
+
+def test_batch_with_uneven_resolutions_matches_oracle_per_iteration():
+    """A batch whose launches are sized by its largest instance: every smaller
+    instance must still match the oracle at every iteration (per-instance
+    arrays indexed by block must not be touched by the extra blocks)."""
+    specs = [(640, 480, 71), (320, 240, 72), (160, 120, 73), (80, 60, 74), (320, 240, 75), (160, 120, 76),
+             (80, 60, 77), (320, 240, 78)]
+    pairs = [frame_pair(w, h, seed=s, deg=3.0, mm=30.0) for w, h, s in specs]
+    iters = [(4, 5, 6, 3), (5, 7, 4), (6, 4, 5), (7, 3, 6), (3, 6, 5), (4, 4, 4), (5, 5, 5), (6, 6, 2)]
+    cfgs = [rg.make_config(p.W, p.H, p.L, mode=rg.BIOBJECTIVE, iters=it, n_select=n_select_for(p.W, p.H))
+            for p, it in zip(pairs, iters)]
+    b = rg.Batch(cfgs, [p.cal.calib for p in pairs])
+    b.enable_trace(64)
+    b.set_reference([p.g0 for p in pairs], [p.d0 for p in pairs])
+    b.set_current([p.g1 for p in pairs], [p.d1 for p in pairs])
+    for rep in range(2):
+        T, _ = b.track(np.tile(np.eye(4, dtype=np.float32), (len(pairs), 1, 1)))
+        for i, (p, it) in enumerate(zip(pairs, iters)):
+            ocfg = O.make_config(p.W, p.H, p.L, mode=rg.BIOBJECTIVE, iters=it, n_select=n_select_for(p.W, p.H))
+            orc = O.OracleTracker(ocfg, p.cal.calib)
+            orc.set_reference(p.g0, p.d0)
+            orc.set_current(p.g1, p.d1)
+            To, tro = orc.track()
+            compare_traces(b.trace(i), tro)
+            assert_bitexact(T[i], To, f"instance {i} ({p.W}x{p.H}), run {rep}")
