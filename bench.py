@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--plain-only", action="store_true", help="skip the learned-initialisation arm (profiling)")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile shapes instead of the autotuner's")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance mixed-resolution workload")
+    ap.add_argument("--batch-only", action="store_true", help="only the 256-instance workload (profiling)")
     ap.add_argument("--tile", default=None, help="ICP chunks per CTA per level, e.g. 3,2,2,1 (no tuning)")
     return ap.parse_args()
 
@@ -352,7 +353,11 @@ def batch_arm(args, torch, world, rank, seed):
     b.set_reference([x["g"][0] for x in inst], [x["d"][0] for x in inst])
     b.set_current([x["g"][1] for x in inst], [x["d"][1] for x in inst])
     T0 = np.tile(np.eye(4, dtype=np.float32), (BATCH_N, 1, 1))
-    chosen, _ = autotune_icp_chunks(b, T_init=T0)
+    if args.tile:
+        b.set_icp_chunks_per_cta([int(v) for v in args.tile.split(",")])
+        chosen = b.icp_chunks_per_cta()
+    else:
+        chosen, _ = autotune_icp_chunks(b, T_init=T0)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     for _ in range(args.warmup):
@@ -453,6 +458,15 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     seed = rank_seed(rank)
+    if args.batch_only:
+        out = batch_arm(args, torch, world, rank, 5000 + 7919 * rank)
+        if rank == 0:
+            print(json.dumps({"metric": "tracked frames/s, 256-instance mixed-resolution batch", "unit": "frames/s",
+                              "value": out["tracked_frames_per_s"], "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "batch256": out}), flush=True)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
     cal, scene, poses = make_workload(seed, args.frames)
     segs = segments(args.frames)
     frames = [f for _, fr in segs for f in fr]
