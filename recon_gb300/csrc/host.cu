@@ -55,6 +55,7 @@ __global__ void k_gate_pick(const InstDesc *D, const float *cand, const long lon
 namespace nn {
 int forward_on(recon_initnet *net, const uint16_t *in_bf16, int n, float *out, cudaStream_t s);
 const float *scale_dev(recon_initnet *net);
+int forward_kernels(int n);
 }  // namespace nn
 
 using namespace rt;
@@ -550,7 +551,7 @@ int learned_start(recon_batch *b, const void **row) {
     g_launches += 1;
     rc = nn::forward_on(b->net, b->d_netin, n, b->d_netout, b->stream);
     if (rc) return rc;
-    g_launches += 8;  // six convolutions, pooling + linear layer, output copy
+    g_launches += nn::forward_kernels(n);
     k_gate_candidate<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_netout, nn::scale_dev(b->net), b->d_cand, b->d_cost);
     k_gate_cost<<<dim3((b->max_P + 255) / 256, n), 256, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost);
     k_gate_pick<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost, b->d_choice);

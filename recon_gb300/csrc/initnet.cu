@@ -12,6 +12,7 @@
 
 #include <math.h>
 
+#include <algorithm>
 #include <string>
 
 #include "../../include/recon_initnet.h"
@@ -61,15 +62,19 @@ __device__ __forceinline__ float bf(const __nv_bfloat16 *p) { return __bfloat162
 
 // out[m][co] = relu(bias[co] + sum_k A[m][k] W[co][k]) with A the 3x3 / stride 2
 // / pad 1 patches of `in` (k = tap * Cin + c).  One CTA of 16 warps per 16
-// output pixels: warp w takes output-channel group w % NG and the K steps
-// j = w / NG, w / NG + KS, ...; the KS partial tiles are added in ascending
-// order in shared memory, so the result does not depend on scheduling.
+// output pixels and K split (blockIdx.y of gridDim.y): the split covers a
+// contiguous range of 16-wide K steps, warp w takes output-channel group
+// w % NG and the steps j0 + w / NG, + KS, ...; the KS partial tiles are added in
+// ascending order in shared memory.  With one split the CTA adds the bias,
+// applies the ReLU and stores BF16; with several it stores its FP32 tile to
+// `partial` and k_conv_split_finish adds the splits in ascending order.  Every
+// order is fixed, so the result does not depend on scheduling.
 constexpr int kConvWarps = 16;
 
 template <int COUT>
 __global__ void __launch_bounds__(kConvWarps * 32) k_conv_fwd(const __nv_bfloat16 *in, int N, int H, int W, int Cin,
                                                               int Kp, const __nv_bfloat16 *w, const float *bias,
-                                                              __nv_bfloat16 *out, int Ho, int Wo) {
+                                                              __nv_bfloat16 *out, int Ho, int Wo, float *partial) {
     constexpr int NF = COUT / 8;             // 8-column fragments
     constexpr int NG = NF < 8 ? NF : 8;      // warps across the columns
     constexpr int FPW = NF / NG;             // fragments per warp
@@ -95,8 +100,10 @@ __global__ void __launch_bounds__(kConvWarps * 32) k_conv_fwd(const __nv_bfloat1
 #pragma unroll
     for (int f = 0; f < FPW; f++) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
     int K = 9 * Cin, nk = Kp / 16;
+    int S = gridDim.y, per = (nk + S - 1) / S;
+    int j0 = blockIdx.y * per, j1 = min(nk, j0 + per);
 #pragma unroll 2
-    for (int j = ks; j < nk; j += KS) {
+    for (int j = j0 + ks; j < j1; j += KS) {
         int kb = 16 * j;
         // A fragment: a0 (row g, k 2t..2t+1), a1 (row g+8), a2 (row g, k+8), a3 (row g+8, k+8)
         uint32_t a[4];
@@ -147,12 +154,39 @@ __global__ void __launch_bounds__(kConvWarps * 32) k_conv_fwd(const __nv_bfloat1
             v0 += red[q][row][col];
             v1 += red[q][row][col + 1];
         }
+        if (S > 1) {
+            float *pp = partial + ((long long)blockIdx.y * M + m) * COUT + col;
+            pp[0] = v0;
+            pp[1] = v1;
+            continue;
+        }
         v0 = v0 + bias[col];
         v1 = v1 + bias[col + 1];
         v0 = v0 > 0.0f ? v0 : 0.0f;
         v1 = v1 > 0.0f ? v1 : 0.0f;
         *reinterpret_cast<__nv_bfloat162 *>(out + m * COUT + col) = __floats2bfloat162_rn(v0, v1);
     }
+}
+
+// The K splits of a convolution added in ascending order, bias, ReLU, BF16.
+template <int COUT>
+__global__ void k_conv_split_finish(const float *partial, int S, long long M, const float *bias,
+                                    __nv_bfloat16 *out) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M * (COUT / 2)) return;
+    long long m = e / (COUT / 2);
+    int col = 2 * (int)(e % (COUT / 2));
+    float v0 = 0.0f, v1 = 0.0f;
+    for (int q = 0; q < S; q++) {
+        const float *pp = partial + ((long long)q * M + m) * COUT + col;
+        v0 += pp[0];
+        v1 += pp[1];
+    }
+    v0 = v0 + bias[col];
+    v1 = v1 + bias[col + 1];
+    v0 = v0 > 0.0f ? v0 : 0.0f;
+    v1 = v1 > 0.0f ? v1 : 0.0f;
+    *reinterpret_cast<__nv_bfloat162 *>(out + m * COUT + col) = __floats2bfloat162_rn(v0, v1);
 }
 
 // global average pooling of the last activation and the linear layer; one CTA
@@ -354,6 +388,7 @@ struct recon_initnet {
     __nv_bfloat16 *act[kLayers] = {nullptr};
     float *dz[kLayers] = {nullptr};
     float *feat = nullptr, *y = nullptr, *partial = nullptr, *loss = nullptr;
+    float *fpart = nullptr;  // forward K-split tiles
     int64_t partial_floats = 0;
     int64_t step = 0;
 };
@@ -379,19 +414,42 @@ int nsplit_for(int l, int n) {
     return (int)(s < 1 ? 1 : (s > kMaxSplit ? kMaxSplit : s));
 }
 
-int conv_forward(recon_initnet *net, int l, const __nv_bfloat16 *in, int n) {
-    int Cin = kCin[l], Cout = kCout[l], Kp = kpad(Cin);
+// K splits of layer l's forward convolution for a batch of n: enough CTAs for
+// about two per SM when the layer has few output pixels (the deep layers), at
+// least one 16-wide K step per warp and split.
+int fsplit_for(int l, int n) {
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
-    dim3 grid((unsigned)((M + 15) / 16));
-    const int block = kConvWarps * 32;
+    long long ctas = (M + 15) / 16;
+    int NF = kCout[l] / 8, NG = NF < 8 ? NF : 8, KS = kConvWarps / NG;
+    int nk = kpad(kCin[l]) / 16;
+    long long s = (2 * 152) / ctas;
+    if (s > nk / KS) s = nk / KS;
+    return (int)(s < 1 ? 1 : s);
+}
+
+template <int COUT>
+void conv_launch(recon_initnet *net, int l, const __nv_bfloat16 *in, int n) {
+    int Cin = kCin[l], Kp = kpad(Cin);
+    long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
+    int S = fsplit_for(l, n);
+    dim3 grid((unsigned)((M + 15) / 16), (unsigned)S);
     const __nv_bfloat16 *w = net->pbf + net->off.w[l];
     const float *b = net->params + net->off.b[l];
-    int H = kHt[l], W = kWd[l], Ho = kHt[l + 1], Wo = kWd[l + 1];
-    switch (Cout) {
-        case 16: k_conv_fwd<16><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
-        case 32: k_conv_fwd<32><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
-        case 64: k_conv_fwd<64><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
-        default: k_conv_fwd<128><<<grid, block, 0, net->stream>>>(in, n, H, W, Cin, Kp, w, b, net->act[l], Ho, Wo); break;
+    k_conv_fwd<COUT><<<grid, kConvWarps * 32, 0, net->stream>>>(in, n, kHt[l], kWd[l], Cin, Kp, w, b, net->act[l],
+                                                                kHt[l + 1], kWd[l + 1], net->fpart);
+    if (S > 1) {
+        long long pairs = M * (COUT / 2);
+        k_conv_split_finish<COUT><<<(unsigned)((pairs + 255) / 256), 256, 0, net->stream>>>(net->fpart, S, M, b,
+                                                                                           net->act[l]);
+    }
+}
+
+int conv_forward(recon_initnet *net, int l, const __nv_bfloat16 *in, int n) {
+    switch (kCout[l]) {
+        case 16: conv_launch<16>(net, l, in, n); break;
+        case 32: conv_launch<32>(net, l, in, n); break;
+        case 64: conv_launch<64>(net, l, in, n); break;
+        default: conv_launch<128>(net, l, in, n); break;
     }
     return RECON_OK;
 }
@@ -463,6 +521,13 @@ int forward_on(recon_initnet *net, const uint16_t *in_bf16, int n, float *out, c
     return rc;
 }
 const float *scale_dev(recon_initnet *net) { return net->params + net->off.scale; }
+// kernels one forward pass of a batch of n launches: the convolutions, their
+// split-K finishing kernels and the pooling + linear layer
+int forward_kernels(int n) {
+    int k = kLayers + 1;
+    for (int l = 0; l < kLayers; l++) k += fsplit_for(l, n) > 1 ? 1 : 0;
+    return k;
+}
 }  // namespace nn
 
 extern "C" {
@@ -483,12 +548,19 @@ int recon_initnet_create(int32_t max_batch, void *stream, recon_initnet **out) {
         if (s > part) part = s;
     }
     net->partial_floats = part;
+    int64_t fpart = 1;
+    for (int l = 0; l < kLayers; l++)
+        for (int nb = 1; nb <= max_batch; nb++) {
+            int S = fsplit_for(l, nb);
+            if (S > 1) fpart = std::max(fpart, (int64_t)S * nb * kHt[l + 1] * kWd[l + 1] * kCout[l]);
+        }
     bool ok = cudaMalloc(&net->params, P * 4) == cudaSuccess && cudaMalloc(&net->grad, P * 4) == cudaSuccess &&
               cudaMalloc(&net->m, P * 4) == cudaSuccess && cudaMalloc(&net->v, P * 4) == cudaSuccess &&
               cudaMalloc(&net->pbf, P * 2) == cudaSuccess &&
               cudaMalloc(&net->feat, (int64_t)max_batch * kFeat * 4) == cudaSuccess &&
               cudaMalloc(&net->y, (int64_t)max_batch * kOut * 4) == cudaSuccess &&
-              cudaMalloc(&net->partial, part * 4) == cudaSuccess && cudaMalloc(&net->loss, 16) == cudaSuccess;
+              cudaMalloc(&net->partial, part * 4) == cudaSuccess && cudaMalloc(&net->fpart, fpart * 4) == cudaSuccess &&
+              cudaMalloc(&net->loss, 16) == cudaSuccess;
     for (int l = 0; ok && l < kLayers; l++) {
         ok = cudaMalloc(&net->act[l], act_count(l, max_batch) * 2) == cudaSuccess &&
              cudaMalloc(&net->dz[l], act_count(l, max_batch) * 4) == cudaSuccess;
@@ -521,6 +593,7 @@ int recon_initnet_destroy(recon_initnet *net) {
     cudaFree(net->feat);
     cudaFree(net->y);
     cudaFree(net->partial);
+    cudaFree(net->fpart);
     cudaFree(net->loss);
     for (int l = 0; l < kLayers; l++) {
         cudaFree(net->act[l]);

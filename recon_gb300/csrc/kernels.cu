@@ -1527,15 +1527,17 @@ __global__ void __launch_bounds__(32) k_gate_candidate(const InstDesc *D, const 
 // pose and of the candidate at the coarsest level, summed with atomics (exact,
 // so the sum does not depend on the order).
 __global__ void __launch_bounds__(256) k_gate_cost(const InstDesc *D, const float *cand, long long *cost) {
-    const InstDesc &d = D[blockIdx.y];
+    __shared__ InstDesc sd;
     __shared__ float Tp[16], Tc[16];
-    __shared__ long long part[2];
+    __shared__ long long part[2][8];
+    load_desc(sd, D + blockIdx.y);
+    __syncthreads();
+    const InstDesc &d = sd;
     int t = threadIdx.x;
     if (t < 16) {
-        Tp[t] = d.T[t];
-        Tc[t] = cand[16 * blockIdx.y + t];
+        Tp[t] = __ldcg(d.T + t);
+        Tc[t] = __ldcg(cand + 16 * blockIdx.y + t);
     }
-    if (t < 2) part[t] = 0;
     __syncthreads();
     int level = d.L - 1;
     long long c0 = 0, c1 = 0;
@@ -1543,10 +1545,21 @@ __global__ void __launch_bounds__(256) k_gate_cost(const InstDesc *D, const floa
         c0 += gate_cost_point(d, Tp, level, i);
         c1 += gate_cost_point(d, Tc, level, i);
     }
-    atomicAdd(reinterpret_cast<unsigned long long *>(&part[0]), (unsigned long long)c0);
-    atomicAdd(reinterpret_cast<unsigned long long *>(&part[1]), (unsigned long long)c1);
+    // integer sums: any order gives the same totals
+    for (int o = 16; o > 0; o >>= 1) {
+        c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+    }
+    if ((t & 31) == 0) {
+        part[0][t >> 5] = c0;
+        part[1][t >> 5] = c1;
+    }
     __syncthreads();
-    if (t < 2) atomicAdd(reinterpret_cast<unsigned long long *>(cost + 2 * blockIdx.y + t), (unsigned long long)part[t]);
+    if (t < 2) {
+        long long s = 0;
+        for (int w = 0; w < 8; w++) s += part[t][w];
+        atomicAdd(reinterpret_cast<unsigned long long *>(cost + 2 * blockIdx.y + t), (unsigned long long)s);
+    }
 }
 
 // Step 3: the candidate replaces the pose when its cost is strictly lower.
