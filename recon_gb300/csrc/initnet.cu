@@ -168,6 +168,81 @@ __global__ void __launch_bounds__(kConvWarps * 32) k_conv_fwd(const __nv_bfloat1
     }
 }
 
+// The same convolution for the wide, shallow layers (few channels, K of at
+// most a few 16-wide steps): each warp owns a 16-pixel tile and all its
+// columns and runs the whole K loop in ascending order, so no warp idles and
+// no partial tiles are added.  8 warps (128 pixels) per CTA.
+constexpr int kConvPxWarps = 8;
+
+template <int COUT>
+__global__ void __launch_bounds__(kConvPxWarps * 32) k_conv_fwd_px(const __nv_bfloat16 *in, int N, int H, int W,
+                                                                   int Cin, int Kp, const __nv_bfloat16 *w,
+                                                                   const float *bias, __nv_bfloat16 *out, int Ho,
+                                                                   int Wo) {
+    constexpr int NF = COUT / 8;
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    long long M = (long long)N * Ho * Wo;
+    long long m0 = ((long long)blockIdx.x * kConvPxWarps + warp) * 16;
+    if (m0 >= M) return;
+    int g = lane >> 2, tig = lane & 3;
+    long long rr[2] = {m0 + g, m0 + g + 8};
+    bool rv[2];
+    int rn[2], ry[2], rx[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        rv[h] = rr[h] < M;
+        long long mm = rv[h] ? rr[h] : 0;
+        rx[h] = (int)(mm % Wo);
+        ry[h] = (int)((mm / Wo) % Ho);
+        rn[h] = (int)(mm / ((long long)Wo * Ho));
+    }
+    float acc[NF][4];
+#pragma unroll
+    for (int f = 0; f < NF; f++) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
+    int K = 9 * Cin, nk = Kp / 16;
+    for (int j = 0; j < nk; j++) {
+        int kb = 16 * j;
+        uint32_t a[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int h = q & 1;
+            int k = kb + 2 * tig + ((q >> 1) ? 8 : 0);
+            uint32_t v = 0;
+            if (rv[h] && k < K) {
+                int tap = k / Cin, c = k - tap * Cin;
+                int ky = tap / 3, kx = tap - ky * 3;
+                int iy = 2 * ry[h] - 1 + ky, ix = 2 * rx[h] - 1 + kx;
+                if (iy >= 0 && iy < H && ix >= 0 && ix < W)
+                    v = *reinterpret_cast<const uint32_t *>(in + (((long long)rn[h] * H + iy) * W + ix) * Cin + c);
+            }
+            a[q] = v;
+        }
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            const __nv_bfloat16 *wr = w + (long long)(f * 8 + g) * Kp + kb + 2 * tig;
+            uint32_t b0 = *reinterpret_cast<const uint32_t *>(wr);
+            uint32_t b1 = *reinterpret_cast<const uint32_t *>(wr + 8);
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                "{%0,%1,%2,%3};\n"
+                : "+f"(acc[f][0]), "+f"(acc[f][1]), "+f"(acc[f][2]), "+f"(acc[f][3])
+                : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        int col = f * 8 + 2 * tig;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (!rv[h]) continue;
+            float v0 = acc[f][2 * h] + bias[col], v1 = acc[f][2 * h + 1] + bias[col + 1];
+            v0 = v0 > 0.0f ? v0 : 0.0f;
+            v1 = v1 > 0.0f ? v1 : 0.0f;
+            *reinterpret_cast<__nv_bfloat162 *>(out + rr[h] * COUT + col) = __floats2bfloat162_rn(v0, v1);
+        }
+    }
+}
+
 // The K splits of a convolution added in ascending order, bias, ReLU, BF16.
 template <int COUT>
 __global__ void k_conv_split_finish(const float *partial, int S, long long M, const float *bias,
@@ -417,6 +492,7 @@ int nsplit_for(int l, int n) {
 // K splits of layer l's forward convolution for a batch of n: enough CTAs for
 // about two per SM when the layer has few output pixels (the deep layers), at
 // least one 16-wide K step per warp and split.
+bool pixel_parallel(int l);
 int fsplit_for(int l, int n) {
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
     long long ctas = (M + 15) / 16;
@@ -427,10 +503,24 @@ int fsplit_for(int l, int n) {
     return (int)(s < 1 ? 1 : s);
 }
 
+// Layers whose 16 warps would mostly idle in k_conv_fwd (fewer K steps than the
+// warps it spreads over K) run as k_conv_fwd_px.
+bool pixel_parallel(int l) {
+    int NF = kCout[l] / 8, NG = NF < 8 ? NF : 8, KS = kConvWarps / NG;
+    return kpad(kCin[l]) / 16 < KS;
+}
+
 template <int COUT>
 void conv_launch(recon_initnet *net, int l, const __nv_bfloat16 *in, int n) {
     int Cin = kCin[l], Kp = kpad(Cin);
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
+    if (pixel_parallel(l)) {
+        long long tiles = (M + 15) / 16;
+        k_conv_fwd_px<COUT><<<(unsigned)((tiles + kConvPxWarps - 1) / kConvPxWarps), kConvPxWarps * 32, 0,
+                               net->stream>>>(in, n, kHt[l], kWd[l], Cin, Kp, net->pbf + net->off.w[l],
+                                              net->params + net->off.b[l], net->act[l], kHt[l + 1], kWd[l + 1]);
+        return;
+    }
     int S = fsplit_for(l, n);
     dim3 grid((unsigned)((M + 15) / 16), (unsigned)S);
     const __nv_bfloat16 *w = net->pbf + net->off.w[l];
@@ -525,7 +615,7 @@ const float *scale_dev(recon_initnet *net) { return net->params + net->off.scale
 // split-K finishing kernels and the pooling + linear layer
 int forward_kernels(int n) {
     int k = kLayers + 1;
-    for (int l = 0; l < kLayers; l++) k += fsplit_for(l, n) > 1 ? 1 : 0;
+    for (int l = 0; l < kLayers; l++) k += (!pixel_parallel(l) && fsplit_for(l, n) > 1) ? 1 : 0;
     return k;
 }
 }  // namespace nn
