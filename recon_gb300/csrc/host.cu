@@ -30,6 +30,10 @@ __global__ void k_seg_scan(const InstDesc *D, const int *active);
 __global__ void k_seg_scatter(const InstDesc *D, const int *active);
 __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
+constexpr int kPyrTile = 16;
+__global__ void k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *in_gray,
+                                       const uint16_t *const *in_depth, const float *const *in_rgbd, int tiles_x,
+                                       int tiles_y);
 __global__ void k_icp_student3(const InstDesc *D, int level);
 __global__ void k_icp_prepare(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
@@ -148,7 +152,6 @@ struct recon_batch {
     const void **h_seqptr = nullptr;  // pinned
     float *d_Tseq = nullptr;
     size_t Tseq_cap = 0;
-    int *d_ones = nullptr;
     uint8_t *d_slot[2] = {nullptr, nullptr};
     size_t slot_bytes = 0;
     cudaStream_t copy_stream = nullptr;
@@ -395,17 +398,22 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
     return RECON_OK;
 }
 
-int prepare_current(recon_batch *b, const void **in = nullptr, const int *active = nullptr) {
+// the current frame's level-0 conversion and pyramid in one launch
+int prepare_current(recon_batch *b, const void **in = nullptr) {
     TimedScope ts(b, b->stream, TK_PREP_CUR, false);
     int n = b->n;
-    auto D = b->d_desc;
     if (!in) in = b->d_inptr;
-    if (!active) active = b->d_active;
-    k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, b->stream>>>(
-        D, 0, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
-    for (int l = 1; l < b->max_L; l++)
-        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, b->stream>>>(D, l, 0, active);
-    g_launches += 1 + (b->max_L - 1);
+    int maxw = 0, maxh = 0;
+    for (auto &c : b->cfg) {
+        maxw = std::max(maxw, c.width);
+        maxh = std::max(maxh, c.height);
+    }
+    int tx = (maxw + kPyrTile - 1) / kPyrTile, ty = (maxh + kPyrTile - 1) / kPyrTile;
+    // one tile per CTA (measured faster than fewer CTAs walking several tiles)
+    k_prep_current_pyramid<<<dim3(tx * ty, n), kPyrTile * kPyrTile, 0, b->stream>>>(
+        b->d_desc, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n),
+        tx, ty);
+    g_launches += 1;
     CK(cudaGetLastError());
     return RECON_OK;
 }
@@ -771,7 +779,6 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->d_seqptr) cudaFree(b->d_seqptr);
     if (b->h_seqptr) cudaFreeHost(b->h_seqptr);
     if (b->d_Tseq) cudaFree(b->d_Tseq);
-    if (b->d_ones) cudaFree(b->d_ones);
     for (int k = 0; k < 2; k++) {
         if (b->d_slot[k]) cudaFree(b->d_slot[k]);
         if (b->ev_copied[k]) cudaEventDestroy(b->ev_copied[k]);
@@ -1083,11 +1090,6 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     int n = b->n;
     for (size_t k = 0; k < (size_t)nf * n; k++)
         if (!gray[k] || !depth[k]) return fail(RECON_ERR_INVALID_ARG, "null frame pointer");
-    if (!b->d_ones) {
-        std::vector<int> ones(n, 1);
-        CK(cudaMalloc(&b->d_ones, n * sizeof(int)));
-        CK(cudaMemcpy(b->d_ones, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-    }
     size_t rows = on_device ? (size_t)nf : 2;
     size_t need_ptr = rows * 3 * n;
     if (need_ptr > b->seqptr_cap) {
@@ -1172,7 +1174,7 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
             CK(cudaEventRecord(b->ev_copied[k], b->copy_stream));
             CK(cudaStreamWaitEvent(b->stream, b->ev_copied[k], 0));
         }
-        int rc = prepare_current(b, row, b->d_ones);
+        int rc = prepare_current(b, row);
         if (rc) return rc;
         k_begin_track<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, 0);
         g_launches += 1;

@@ -89,6 +89,105 @@ __global__ void k_convert_level0(const InstDesc *D, int is_ref, const uint8_t *c
     }
 }
 
+// The current frame's whole pyramid in one pass: k_convert_level0's
+// conversion of the level-0 pixels and k_downsample's 2x2 reductions for the
+// coarser levels (the same expressions in the same order, so every value is
+// identical), computed per 16x16 tile of level 0 with the intermediate levels
+// in shared memory, so level 0 is not read back from memory.  One thread per
+// level-0 pixel of the tile; grid: tiles of the batch's largest frame x
+// instances.
+constexpr int kPyrTile = 16;
+
+__global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(const InstDesc *D,
+                                                                             const uint8_t *const *in_gray,
+                                                                             const uint16_t *const *in_depth,
+                                                                             const float *const *in_rgbd, int tiles_x,
+                                                                             int tiles_y) {
+    __shared__ InstDesc sd;
+    __shared__ float sg[2][kPyrTile * kPyrTile];   // gray of the current and the next level (ping-pong)
+    __shared__ float4 sp[2][kPyrTile * kPyrTile];  // points (x y z mask)
+    load_desc(sd, D + blockIdx.y);
+    __syncthreads();
+    const InstDesc &d = sd;
+    const uint8_t *gp = in_gray[blockIdx.y];
+    const uint16_t *dp = in_depth[blockIdx.y];
+    const float *fp = in_rgbd[blockIdx.y];
+    if (!fp && (!gp || !dp)) return;  // instance not updated by this call
+    int W = d.W, H = d.H;
+    float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
+    float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
+    float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
+    int lx = threadIdx.x % kPyrTile, ly = threadIdx.x / kPyrTile;
+    // tiles with a grid stride (the launch uses one tile per CTA)
+    for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
+        int tx = tile % tiles_x, ty = tile / tiles_x;
+        if (tx * kPyrTile >= W || ty * kPyrTile >= H) continue;  // uniform over the CTA
+        int xi = tx * kPyrTile + lx, yi = ty * kPyrTile + ly;
+        __syncthreads();  // the previous tile's shared values are consumed
+        // level 0 (k_convert_level0)
+        if (xi < W && yi < H) {
+            int i = xi + yi * W;
+            float g, z;
+            if (fp) {
+                float4 p = __ldg((const float4 *)fp + xi + (H - 1 - yi) * W);
+                g = 0.3f * p.x + 0.59f * p.y + 0.11f * p.z;
+                z = -(p.w * (maxDist - minDist) + minDist);
+            } else {
+                g = (float)__ldg(gp + i) / 255.0f;
+                uint16_t dm = __ldg(dp + i);
+                z = dm ? -(float)dm : 0.0f;
+            }
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (z < 0) {
+                o.x = ((float)xi - cx) * z / fx;
+                o.y = ((float)yi - cy) * z / fy;
+                o.z = z;
+                o.w = 1.0f;
+            }
+            d.cur_gray[0][i] = g;
+            d.cur_z[i] = z;
+            d.cur_pts[0][i] = o;
+            sg[0][threadIdx.x] = g;
+            sp[0][threadIdx.x] = o;
+        }
+        // levels 1.. (k_downsample, is_ref = 0): a tile of side kPyrTile >> l
+        int side = kPyrTile;
+        for (int l = 1; l < d.L; l++) {
+            __syncthreads();
+            int cur = (l - 1) & 1, nxt = l & 1;
+            int hs = side;  // side of the finer tile
+            side >>= 1;
+            int wlo = W >> l, hlo = H >> l;
+            if ((int)threadIdx.x < side * side) {
+                int ox = threadIdx.x % side, oy = threadIdx.x / side;
+                int gx = tx * side + ox, gy = ty * side + oy;
+                if (gx < wlo && gy < hlo) {
+                    int c0 = 2 * ox + 2 * oy * hs;
+                    int offs[4] = {c0, c0 + 1, c0 + hs, c0 + hs + 1};
+                    float gl = (sg[cur][offs[0]] + sg[cur][offs[1]] + sg[cur][offs[2]] + sg[cur][offs[3]]) / 4.0f;
+                    float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, ns = 0.0f;
+                    for (int k = 0; k < 4; k++) {
+                        float4 q = sp[cur][offs[k]];
+                        if (q.w != 0.0f) {
+                            ns++;
+                            p0 += q.x;
+                            p1 += q.y;
+                            p2 += q.z;
+                        }
+                    }
+                    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (ns > 0.0f) o = make_float4(p0 / ns, p1 / ns, p2 / ns, 1.0f);
+                    int i = gx + gy * wlo;
+                    d.cur_gray[l][i] = gl;
+                    d.cur_pts[l][i] = o;
+                    sg[nxt][threadIdx.x] = gl;
+                    sp[nxt][threadIdx.x] = o;
+                }
+            }
+        }
+    }
+}
+
 // fastDownSampleHdrKernel (downSample2Cuda.cu:35-42) for the gray pyramid and
 // downSampleCloud6Kernel (d2z.cu:557-588) for the point pyramid.
 __global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int *active) {
