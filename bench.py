@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--plain-only", action="store_true", help="skip the learned-initialisation arm (profiling)")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile shapes instead of the autotuner's")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance mixed-resolution workload")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision measurement")
     ap.add_argument("--batch-only", action="store_true", help="only the 256-instance workload (profiling)")
     ap.add_argument("--tile", default=None, help="ICP chunks per CTA per level, e.g. 3,2,2,1 (no tuning)")
     return ap.parse_args()
@@ -185,9 +186,10 @@ def segments(n_frames):
     return segs
 
 
-def make_batch(cal, n_inst, stream):
+def make_batch(cal, n_inst, stream, precision=0):
     import recon_gb300 as rg
-    cfg = rg.make_config(W, H, LEVELS, mode=rg.BIOBJECTIVE, iters=ITERS, n_select=N_SELECT, lam=LAMBDA)
+    cfg = rg.make_config(W, H, LEVELS, mode=rg.BIOBJECTIVE, iters=ITERS, n_select=N_SELECT, lam=LAMBDA,
+                         precision=precision)
     return rg.Batch([cfg] * n_inst, [cal.calib] * n_inst, stream=stream)
 
 
@@ -615,6 +617,30 @@ def main():
         d2h = max(len(fr) for _, fr in segs) * len(segs) * (64 + 64)
         e2e = {"value": job_throughput(world, args.frames, args.steps, ms_e2e) * frac, "unit": "frames/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    # -------- mixed precision (FP16 images and intensities, BF16 photometric
+    # Jacobians) on the plain arm's schedule: speed and pose error against the
+    # FP32 poses, which are the oracle's
+    mixed = None
+    if not args.no_mixed:
+        mb = make_batch(cal, len(segs), stream.cuda_stream, precision=rg.PRECISION_MIXED)
+        mb.set_icp_chunks_per_cta(batch.icp_chunks_per_cta())
+        poses_mixed = np.zeros_like(poses_plain)
+        for _ in range(args.warmup):
+            run_step(mb, segs, gray, depth, poses_mixed)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            run_step(mb, segs, gray, depth, poses_mixed)
+        e1.record(stream)
+        barrier()
+        ms_mixed = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
+        m_err, _ = error_summary(pose_errors(poses_mixed, poses_plain, frames))
+        mixed = {"storage": "FP16 current gray pyramid and reference intensities, BF16 photometric Jacobians; "
+                            "FP32 arithmetic, exact fixed-point sums, FP64 solve",
+                 "frames_per_s": job_throughput(world, args.frames, args.steps, ms_mixed),
+                 "vs_fp32": m_err}
+        mb.close()
+
     # -------- the batched workload (256 mixed-resolution instances): a reported
     # measurement beside the headline, with its own roofline
     batched = None
@@ -681,6 +707,7 @@ def main():
             "kernel_ms": {k: v[0] for k, v in timing.items()},
             "kernel_launches": {k: v[1] for k, v in timing.items()},
             "batch256": batched,
+            "mixed_precision": mixed,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -761,6 +761,55 @@ void orc_reduce27_refordered(const float *const *J6, const float *r, int N, floa
 }
 
 /* ------------------------------------------------------------------ */
+/* Mixed-precision storage                                             */
+/* ------------------------------------------------------------------ */
+
+/* IEEE binary16 rounding to nearest even, by integer operations on the float's
+ * bits: 10 fraction bits for normal results (exponent >= -14), a fixed 2^-24
+ * quantum below, overflow to infinity at and above 65520. */
+float orc_f16_round(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
+    if (a >= 0x7f800000u) return x;                  /* Inf, NaN */
+    uint32_t r;
+    if (a >= 0x38800000u) {                          /* |x| >= 2^-14: normal binary16 */
+        r = a + 0xfffu + ((a >> 13) & 1u);
+        r &= ~0x1fffu;
+        if (r >= 0x47800000u) r = 0x7f800000u;       /* rounded up to 2^16: infinity */
+    } else {                                         /* subnormal binary16: multiples of 2^-24 */
+        /* |x| = m * 2^(e - 150) (e >= 1) or m * 2^-149 (e = 0); in units of
+         * 2^-24 that is m >> s with s = 126 - e (125 for e = 0), s >= 14 */
+        int e = (int)(a >> 23);
+        uint64_t m = (a & 0x7fffffu) | (e ? 0x800000u : 0u);
+        int sh = e ? 126 - e : 125;
+        uint64_t q = 0;
+        if (sh < 40) {
+            uint64_t qi = m >> sh, rem = m & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+            q = qi + ((rem > half || (rem == half && (qi & 1))) ? 1 : 0);
+        }
+        float f = (float)q * 5.9604644775390625e-8f; /* q * 2^-24, exact (q <= 1024) */
+        memcpy(&r, &f, 4);
+    }
+    r |= sign;
+    float out;
+    memcpy(&out, &r, 4);
+    return out;
+}
+
+/* bfloat16 (8 fraction bits) rounding to nearest even; NaN and Inf kept. */
+float orc_bf16_round(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return x;
+    u = u + 0x7fffu + ((u >> 16) & 1u);
+    u &= 0xffff0000u;
+    float out;
+    memcpy(&out, &u, 4);
+    return out;
+}
+
+/* ------------------------------------------------------------------ */
 /* ICP                                                                 */
 /* ------------------------------------------------------------------ */
 
@@ -1341,6 +1390,8 @@ struct orc_tracker {
     int32_t *rmask, *select;
     float *icp_r, *icp_r2, *icp_w, *icp_J, *icp_res;
     float *icp_wpx;    /* the level's Student-t weights per pixel, 0 where not selected */
+    /* mixed precision: the stored (rounded) copies the photometric term reads */
+    float *cur_gray_q[ORC_MAX_LEVELS], *sel_I_q[ORC_MAX_LEVELS], *sel_J_q[ORC_MAX_LEVELS];
     int32_t *all_px;   /* 0, 1, 2, ...: every pixel of the level in order */
     int32_t nsel[ORC_MAX_LEVELS];
     int has_ref, has_cur;
@@ -1394,6 +1445,12 @@ orc_tracker *orc_create(const orc_config *cfg, const float *calib) {
     t->icp_res = (float *)xmalloc(npmax * sizeof(float));
     t->icp_J = (float *)xmalloc(6 * (size_t)npmax * sizeof(float));
     t->icp_wpx = (float *)xmalloc(npmax * sizeof(float));
+    if (cfg->precision == 1)
+        for (int l = 0; l < t->L; l++) {
+            t->cur_gray_q[l] = (float *)xmalloc((size_t)(W >> l) * (H >> l) * sizeof(float));
+            t->sel_I_q[l] = (float *)xmalloc(P * sizeof(float));
+            t->sel_J_q[l] = (float *)xmalloc(6 * (size_t)P * sizeof(float));
+        }
     t->all_px = (int32_t *)xmalloc(W * H * sizeof(int32_t));
     for (int i = 0; i < W * H; i++) t->all_px[i] = i;
     for (int i = 0; i < 16; i++) t->T[i] = (i % 5 == 0) ? 1.0f : 0.0f;
@@ -1412,6 +1469,7 @@ void orc_destroy(orc_tracker *t) {
     free(t->full_res); free(t->rmask); free(t->select);
     free(t->icp_r); free(t->icp_r2); free(t->icp_w); free(t->icp_res); free(t->icp_J);
     free(t->icp_wpx); free(t->all_px);
+    for (int l = 0; l < ORC_MAX_LEVELS; l++) { free(t->cur_gray_q[l]); free(t->sel_I_q[l]); free(t->sel_J_q[l]); }
     free(t);
 }
 
@@ -1449,6 +1507,11 @@ static int prepare_reference(orc_tracker *t, const float *gray0, const float *z0
     orc_compute_normals6(t->ref6[0], t->refmask[0], W, H);
     for (int l = 1; l < L; l++)
         orc_downsample_cloud6(t->ref6[l - 1], t->refmask[l - 1], W >> l, H >> l, t->ref6[l], t->refmask[l]);
+    if (t->cfg.precision == 1)
+        for (int l = 0; l < L; l++) {
+            for (int k = 0; k < P; k++) t->sel_I_q[l][k] = orc_f16_round(t->sel_I[l][k]);
+            for (int k = 0; k < 6 * P; k++) t->sel_J_q[l][k] = orc_bf16_round(t->sel_J[l][k]);
+        }
     if (reset_pose)
         for (int i = 0; i < 16; i++) t->T[i] = (i % 5 == 0) ? 1.0f : 0.0f;
     t->has_ref = 1;
@@ -1502,6 +1565,9 @@ int orc_set_current(orc_tracker *t, const uint8_t *gray, const uint16_t *depth) 
     orc_gen_cloud6(t->cur_z, W, H, t->calib, t->cur6[0], t->curmask[0]);
     for (int l = 1; l < L; l++)
         orc_downsample_cloud6(t->cur6[l - 1], t->curmask[l - 1], W >> l, H >> l, t->cur6[l], t->curmask[l]);
+    if (t->cfg.precision == 1)
+        for (int l = 0; l < L; l++)
+            for (int i = 0; i < (W >> l) * (H >> l); i++) t->cur_gray_q[l][i] = orc_f16_round(t->cur_gray[l][i]);
     t->has_cur = 1;
     return 0;
 }
@@ -1566,11 +1632,16 @@ int orc_track(orc_tracker *t, float *Tio, orc_iter_trace *trace, int max_trace) 
             int median = -1;
             int ok = 1;
             if (mode == ORC_PHOTOMETRIC || mode == ORC_BIOBJECTIVE) {
-                orc_interpolate_residual(P, t->sel_xyz, t->sel_I[layer], t->T, t->calib, layer, t->cur_gray[layer],
-                                         wl, hl, t->cur_z, W, H, t->r, t->zw);
+                /* mixed precision reads the rounded copies; the arithmetic is the same */
+                int mixed = t->cfg.precision == 1;
+                const float *selI = mixed ? t->sel_I_q[layer] : t->sel_I[layer];
+                const float *img = mixed ? t->cur_gray_q[layer] : t->cur_gray[layer];
+                const float *selJ = mixed ? t->sel_J_q[layer] : t->sel_J[layer];
+                orc_interpolate_residual(P, t->sel_xyz, selI, t->T, t->calib, layer, img, wl, hl, t->cur_z, W, H, t->r,
+                                         t->zw);
                 median = orc_generate_weights(t->r, t->zw, P, t->cfg.hist_bins, hist, t->w, t->rw);
                 for (int c = 0; c < 6; c++)
-                    for (int i = 0; i < P; i++) t->Jw[c][i] = t->sel_J[layer][c * P + i] * t->w[i];
+                    for (int i = 0; i < P; i++) t->Jw[c][i] = selJ[c * P + i] * t->w[i];
                 const float *J6[6];
                 for (int c = 0; c < 6; c++) J6[c] = t->Jw[c];
                 orc_fx27 acc;

@@ -54,7 +54,14 @@ typedef struct orc_config {
     int32_t iters[ORC_MAX_LEVELS]; /* coarse -> fine, phototracker.cpp:148-149 */
     float opt_scale_in;            /* phototracker.cpp:50 */
     float opt_scale_out;           /* phototracker.cpp:51 */
+    int32_t precision;             /* 0 FP32; 1 mixed: FP16 current images and reference
+                                      intensities, BF16 photometric Jacobians (values rounded
+                                      to nearest even on storage, FP32 arithmetic) */
 } orc_config;
+
+/* float -> nearest binary16 / bfloat16 value (ties to even), widened back to float */
+float orc_f16_round(float x);
+float orc_bf16_round(float x);
 
 typedef struct orc_iter_trace {
     int32_t level, iter, mode, solved, icp_selected, status;

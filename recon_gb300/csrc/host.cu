@@ -203,6 +203,8 @@ int validate(const recon_config &c) {
     for (int l = 0; l < RECON_MAX_LEVELS; l++)
         if (c.iters[l] < 0 || c.iters[l] > 1000) return fail(RECON_ERR_INVALID_ARG, "bad iteration count");
     if (!(c.lambda >= 0.0f && c.lambda <= 1.0f)) return fail(RECON_ERR_INVALID_ARG, "lambda must be in [0,1]");
+    if (c.precision != RECON_PRECISION_FP32 && c.precision != RECON_PRECISION_MIXED)
+        return fail(RECON_ERR_INVALID_ARG, "bad precision");
     return RECON_OK;
 }
 
@@ -220,6 +222,10 @@ size_t layout(InstDesc &d, char *base) {
         d.cur_pts[l] = nl ? a.take<float4>(nl) : nullptr;
         d.sel_I[l] = (l < d.L) ? a.take<float>(P) : nullptr;
         d.sel_J[l] = (l < d.L) ? a.take<float>(6 * (size_t)P) : nullptr;
+        bool mixed = d.precision == RECON_PRECISION_MIXED && l < d.L;
+        d.sel_Ih[l] = mixed ? a.take<__half>(P) : nullptr;
+        d.sel_Jb[l] = mixed ? a.take<__nv_bfloat16>(6 * (size_t)P) : nullptr;
+        d.cur_grayh[l] = mixed ? a.take<__half>(nl) : nullptr;
     }
     d.ref_z = a.take<float>(n);
     d.cur_z = a.take<float>(n);

@@ -145,6 +145,7 @@ __global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(con
                 o.w = 1.0f;
             }
             d.cur_gray[0][i] = g;
+            if (d.cur_grayh[0]) d.cur_grayh[0][i] = __float2half_rn(g);  // mixed precision
             d.cur_z[i] = z;
             d.cur_pts[0][i] = o;
             sg[0][threadIdx.x] = g;
@@ -179,6 +180,7 @@ __global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(con
                     if (ns > 0.0f) o = make_float4(p0 / ns, p1 / ns, p2 / ns, 1.0f);
                     int i = gx + gy * wlo;
                     d.cur_gray[l][i] = gl;
+                    if (d.cur_grayh[l]) d.cur_grayh[l][i] = __float2half_rn(gl);
                     d.cur_pts[l][i] = o;
                     sg[nxt][threadIdx.x] = gl;
                     sp[nxt][threadIdx.x] = o;
@@ -582,7 +584,10 @@ __global__ void k_attr_jac(const InstDesc *D, const int *active) {
     d.sel_xyz[k] = p3x;
     d.sel_xyz[P + k] = p3y;
     d.sel_xyz[2 * P + k] = p3z;
-    for (int l = 0; l < L; l++) d.sel_I[l][k] = col[l];
+    for (int l = 0; l < L; l++) {
+        d.sel_I[l][k] = col[l];
+        if (d.sel_Ih[l]) d.sel_Ih[l][k] = __float2half_rn(col[l]);  // mixed precision
+    }
 
     // precomputeJacobian4Kernel
     float optScaleIn = d.opt_in;
@@ -621,6 +626,7 @@ __global__ void k_attr_jac(const InstDesc *D, const int *active) {
                 val = (dp2x / s) * gx[l] + (dp2y / s) * gy[l];
             }
             d.sel_J[l][c * P + k] = val;
+            if (d.sel_Jb[l]) d.sel_Jb[l][c * P + k] = __float2bfloat16_rn(val);  // mixed precision
         }
     }
 }
@@ -1027,21 +1033,42 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     for (int c = 0; c < 3; c++) j[3 + c] = -weight * (-cnx * T[c] - cny * T[4 + c] - cnz * T[8 + c]);
 }
 
+// The arrays the photometric term reads: FP32, or (mixed precision) the FP16
+// current image and reference intensities and the BF16 Jacobian.  Widening a
+// stored FP16 / BF16 value to FP32 is exact, so the arithmetic that follows is
+// the FP32 path's on rounded inputs.
+template <bool kMixed> struct PhotoArrays;
+template <> struct PhotoArrays<false> {
+    using TI = float;
+    using TJ = float;
+    static __device__ const float *img(const InstDesc &d, int l) { return d.cur_gray[l]; }
+    static __device__ const float *I(const InstDesc &d, int l) { return d.sel_I[l]; }
+    static __device__ const float *J(const InstDesc &d, int l) { return d.sel_J[l]; }
+};
+template <> struct PhotoArrays<true> {
+    using TI = __half;
+    using TJ = __nv_bfloat16;
+    static __device__ const __half *img(const InstDesc &d, int l) { return d.cur_grayh[l]; }
+    static __device__ const __half *I(const InstDesc &d, int l) { return d.sel_Ih[l]; }
+    static __device__ const __nv_bfloat16 *J(const InstDesc &d, int l) { return d.sel_Jb[l]; }
+};
+
 // Photometric residuals of lane t's 4 points of chunk c
 // (interpolateResidualKernel2, warp.cu:269-332).
+template <bool kMixed>
 __device__ __forceinline__ void photo_lane_residuals(const InstDesc &d, const float *T, int level, int c, int t,
                                                      float *r, float *zw) {
     int P = d.P;
     int w = d.W >> level, h = d.H >> level;
     float a = 1.0f / (float)(1 << level);
     float b = 0.5f * (a - 1.0f);
-    const float *img = d.cur_gray[level];
-    const float *I = d.sel_I[level];
+    const auto *img = PhotoArrays<kMixed>::img(d, level);
+    const auto *I = PhotoArrays<kMixed>::I(d, level);
 #pragma unroll
     for (int m = 0; m < 4; m++) {
         int i = c * kChunk + t + kLanes * m;
         photo_residual(d.calib, T, a, b, __ldg(d.sel_xyz + i), __ldg(d.sel_xyz + P + i), __ldg(d.sel_xyz + 2 * P + i),
-                       __ldg(I + i), img, w, h, d.cur_z, d.W, d.H, r[m], zw[m]);
+                       ldf(I + i), img, w, h, d.cur_z, d.W, d.H, r[m], zw[m]);
     }
 }
 
@@ -1051,17 +1078,23 @@ __device__ __forceinline__ void photo_lane_residuals(const InstDesc &d, const fl
 // the median bin (seekThreshold64Kernel, histogram64.cu:48-61) and weighs its
 // own points (generateWeights64Kernel, 79-94) into the CTA's fixed-point sums.
 // Returns whether this CTA had a chunk.
+template <bool kMixed>
 __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int rank) {
+    using TJ = typename PhotoArrays<kMixed>::TJ;
     int P = d.P, nph = P / kChunk, nb = d.hist_bins;
     int t = threadIdx.x, lane = t & 31;
-    const float *J = d.sel_J[level];
+    const TJ *J = PhotoArrays<kMixed>::J(d, level);
+    // the Jacobian tile in shared memory, in its stored type (a BF16 tile uses
+    // the first half of sh.J)
+    TJ(*sJ)[kChunk] = reinterpret_cast<TJ(*)[kChunk]>(&sh.J[0][0]);
+    constexpr int kPer16 = 16 / sizeof(TJ);  // values per 16-byte copy
     // the first chunk's Jacobian does not depend on the pose: copy it to shared
     // memory asynchronously while the residuals are evaluated
     if (rank < nph) {
-        for (int k = t; k < 6 * (kChunk / 4); k += blockDim.x) {
-            int col = k / (kChunk / 4), q4 = k % (kChunk / 4);
-            const float *src = J + (size_t)col * P + rank * kChunk + 4 * q4;
-            unsigned int dst = (unsigned int)__cvta_generic_to_shared(&sh.J[col][4 * q4]);
+        for (int k = t; k < 6 * (kChunk / kPer16); k += blockDim.x) {
+            int col = k / (kChunk / kPer16), q = k % (kChunk / kPer16);
+            const TJ *src = J + (size_t)col * P + rank * kChunk + kPer16 * q;
+            unsigned int dst = (unsigned int)__cvta_generic_to_shared(&sJ[col][kPer16 * q]);
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -1071,7 +1104,7 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
     float r0[4], zw0[4];
     for (int c = rank; c < nph; c += kCluster) {
         float r[4], zw[4];
-        photo_lane_residuals(d, sh.T, level, c, t, r, zw);
+        photo_lane_residuals<kMixed>(d, sh.T, level, c, t, r, zw);
 #pragma unroll
         for (int m = 0; m < 4; m++) {
             // one shared-memory atomic per distinct bin of the warp
@@ -1119,12 +1152,12 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
                 r = r0[m];
                 zw = zw0[m];
 #pragma unroll
-                for (int k = 0; k < 6; k++) jv[k] = sh.J[k][t + kLanes * m];
+                for (int k = 0; k < 6; k++) jv[k] = (float)sJ[k][t + kLanes * m];
             } else {
                 r = d.ph_r[i];  // written by this thread above
                 zw = d.ph_zw[i];
 #pragma unroll
-                for (int k = 0; k < 6; k++) jv[k] = __ldg(J + k * P + i);
+                for (int k = 0; k < 6; k++) jv[k] = ldf(J + k * P + i);
             }
             float wv = tukey_weight(r, zw, s);
             float jw[6];
@@ -1334,7 +1367,9 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
     fx_clear(sh);
     __syncthreads();
     if (set == 0) {
-        if (!photo_cluster(d, sh, level, role)) return;
+        bool had = d.precision == RECON_PRECISION_MIXED ? photo_cluster<true>(d, sh, level, role)
+                                                        : photo_cluster<false>(d, sh, level, role);
+        if (!had) return;
     } else {
         int c0 = (role - kCluster) * icp_per_cta;
         icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), npix);

@@ -1,6 +1,8 @@
 // track_kernels.cuh -- device-side instance descriptor shared by the kernels
 // and the host code of librecon_track.so.
 #pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -42,6 +44,11 @@ struct InstDesc {
     float *sel_xyz;               // 3 * P (SoA)
     float *sel_I[kMaxLevels];     // P
     float *sel_J[kMaxLevels];     // 6 * P (SoA)
+    // mixed precision (precision == RECON_PRECISION_MIXED): the FP16 / BF16
+    // copies the photometric term reads instead of sel_I, sel_J and cur_gray
+    __half *sel_Ih[kMaxLevels];         // P
+    __nv_bfloat16 *sel_Jb[kMaxLevels];  // 6 * P (SoA)
+    __half *cur_grayh[kMaxLevels];      // W*H of the level
     // current frame
     float *cur_gray[kMaxLevels];
     float *cur_z;

@@ -5,6 +5,8 @@
 // so each value is bit-identical to the reference semantics evaluated without
 // fused multiply-adds.
 #pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -58,13 +60,19 @@ __device__ __forceinline__ void distort(float pux, float puy, const float *kc, c
     pdy = K[4] * puy * radialDist + K[5];
 }
 
+// a stored value widened to FP32 (exact for FP16 and BF16)
+__device__ __forceinline__ float ldf(const float *p) { return __ldg(p); }
+__device__ __forceinline__ float ldf(const __half *p) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ float ldf(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
+
 // bilinearInterpolation(int,int,float,float,...), kernelUtils.h:298-303
-__device__ __forceinline__ float bilin(int xdi, int ydi, float fx, float fy, int width, const float *src) {
+template <typename TImg>
+__device__ __forceinline__ float bilin(int xdi, int ydi, float fx, float fy, int width, const TImg *src) {
     int o = xdi + ydi * width;
-    float v0 = __ldg(src + o);
-    float v1 = __ldg(src + o + 1);
-    float v2 = __ldg(src + o + width);
-    float v3 = __ldg(src + o + width + 1);
+    float v0 = ldf(src + o);
+    float v1 = ldf(src + o + 1);
+    float v2 = ldf(src + o + width);
+    float v3 = ldf(src + o + width + 1);
     return (1 - fx) * (1 - fy) * v0 + fx * (1 - fy) * v1 + (1 - fx) * fy * v2 + fx * fy * v3;
 }
 
@@ -125,9 +133,11 @@ __device__ __forceinline__ int mad_bin(float r, int nbins) {
 }
 
 // interpolateResidualKernel2, warp.cu:269-332: photometric residual and depth
-// consistency weight of one keyframe point at pyramid layer `layer`.
+// consistency weight of one keyframe point at pyramid layer `layer` (the image
+// stored in FP32, or in FP16 for the mixed-precision mode).
+template <typename TImg>
 __device__ __forceinline__ void photo_residual(const float *calib, const float *T, float a, float b, float px3,
-                                               float py3, float pz3, float Iref, const float *img, int width,
+                                               float py3, float pz3, float Iref, const TImg *img, int width,
                                                int height, const float *zcur, int zwidth, int zheight, float &res,
                                                float &zweight) {
     const float *KR = calib + RC_KR;

@@ -29,6 +29,7 @@ class OrcConfig(ctypes.Structure):
         ("n_select", ctypes.c_int32), ("hist_bins", ctypes.c_int32), ("select_bins", ctypes.c_int32),
         ("solver", ctypes.c_int32), ("mode", ctypes.c_int32), ("lambda_", ctypes.c_float),
         ("iters", ctypes.c_int32 * 4), ("opt_scale_in", ctypes.c_float), ("opt_scale_out", ctypes.c_float),
+        ("precision", ctypes.c_int32),
     ]
 
 
@@ -77,6 +78,10 @@ def lib() -> ctypes.CDLL:
             L.orc_solve_cholesky.argtypes = [vp, vp, vp]
             L.orc_solve_cg.argtypes = [vp, vp, ctypes.c_double, i32, vp]
             L.orc_reduce27.argtypes = [vp, vp, i32, vp, vp]
+            L.orc_f16_round.argtypes = [f32]
+            L.orc_f16_round.restype = f32
+            L.orc_bf16_round.argtypes = [f32]
+            L.orc_bf16_round.restype = f32
             L.orc_reduce27_refordered.argtypes = [vp, vp, i32, vp, vp]
             L.orc_fx_add.argtypes = [vp, f32, vp]
             L.orc_fx_to_double.argtypes = [vp]
@@ -143,7 +148,7 @@ def ptrs(arrays) -> ctypes.Array:
 
 
 def make_config(width, height, levels, mode=PHOTOMETRIC, iters=(1, 3, 10, 5), n_select=8192, hist_bins=64,
-                select_bins=256, solver=CHOLESKY, lam=0.5) -> OrcConfig:
+                select_bins=256, solver=CHOLESKY, lam=0.5, precision=0) -> OrcConfig:
     c = OrcConfig()
     c.width, c.height, c.levels = width, height, levels
     c.n_select, c.hist_bins, c.select_bins = n_select, hist_bins, select_bins
@@ -151,6 +156,7 @@ def make_config(width, height, levels, mode=PHOTOMETRIC, iters=(1, 3, 10, 5), n_
     it = list(iters) + [0] * (4 - len(iters))
     c.iters[:] = it[:4]
     c.opt_scale_in, c.opt_scale_out = 1e-3, 1e3
+    c.precision = precision
     return c
 
 
