@@ -20,9 +20,9 @@
 #include "track_kernels.cuh"
 
 namespace rt {
-__global__ void k_convert_level0(const InstDesc *D, int is_ref, const uint8_t *const *in_gray,
-                                 const uint16_t *const *in_depth, const float *const *in_rgbd);
-__global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int *active);
+__global__ void k_convert_level0(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
+                                 const float *const *in_rgbd);
+__global__ void k_downsample(const InstDesc *D, int level, const int *active);
 __global__ void k_normals(const InstDesc *D, const int *active);
 __global__ void k_xyz2cloud(const InstDesc *D, const int *active);
 __global__ void k_seg_count(const InstDesc *D, const int *active);
@@ -386,12 +386,12 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
     auto in = b->d_inptr;
     if (from_inputs)
         k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, s>>>(
-            D, 1, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
+            D, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
     else
         k_ref_from_z<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
     k_normals<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
     for (int l = 1; l < b->max_L; l++)
-        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, 1, b->d_active);
+        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, b->d_active);
     k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, b->d_active);
     k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
     k_seg_count<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, b->d_active);

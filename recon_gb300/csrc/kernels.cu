@@ -33,24 +33,16 @@ __device__ __forceinline__ void load_desc(InstDesc &sd, const InstDesc *src_desc
 // input conversion and pyramids
 // ------------------------------------------------------------------
 
-// uint8 gray -> [0,1], uint16 mm -> z = -mm (rgb2gray.cu:64-76 for the u8/u16
-// form); the current frame also gets its ICP cloud (genPointsCloud6Kernel,
-// d2z.cu:436-469) and the reference its xyz + mask (convertZMapToXYZ6Kernel,
-// rgb2gray.cu:595-624; the same formula as convertZMapToXYZKernel, 570-593).
-__global__ void k_convert_level0(const InstDesc *D, int is_ref, const uint8_t *const *in_gray,
-                                 const uint16_t *const *in_depth, const float *const *in_rgbd) {
-    INST_DESC;
-    const uint8_t *gp = in_gray[blockIdx.y];
-    const uint16_t *dp = in_depth[blockIdx.y];
-    const float *fp = in_rgbd[blockIdx.y];
-    if (!fp && (!gp || !dp)) return;  // instance not updated by this call
-    int n = d.W * d.H;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float g, z;
+// The reference frame's level 0: uint8 gray -> [0,1], uint16 mm -> z = -mm
+// (rgb2gray.cu:64-76 for the u8/u16 form, or the float4 RGBA+depth frame with
+// its y-flip, rgbTex2GrayHdrZKernel), and its xyz + mask
+// (convertZMapToXYZ6Kernel, rgb2gray.cu:595-624; the same formula as
+// convertZMapToXYZKernel, 570-593).  The current frame uses
+// k_prep_current_pyramid.
+__device__ __forceinline__ void convert_pixel(const InstDesc &d, const uint8_t *gp, const uint16_t *dp, const float *fp,
+                                              int i, int xi, int yi, float &g, float &z) {
     if (fp) {
         // rgbTex2GrayHdrZKernel: texture read at (x, H-1-y)
-        int xi = i % d.W, yi = i / d.W;
         float4 p = __ldg((const float4 *)fp + xi + (d.H - 1 - yi) * d.W);
         g = 0.3f * p.x + 0.59f * p.y + 0.11f * p.z;
         float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
@@ -60,39 +52,40 @@ __global__ void k_convert_level0(const InstDesc *D, int is_ref, const uint8_t *c
         uint16_t dm = __ldg(dp + i);
         z = dm ? -(float)dm : 0.0f;
     }
-    int xi = i % d.W, yi = i / d.W;
-    float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
-    float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
-    if (is_ref) {
-        d.ref_gray[0][i] = g;
-        d.ref_z[i] = z;
-        float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
-        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (z < -minDist && z > -maxDist) {
-            o.x = ((float)xi - cx) * z / fx;
-            o.y = ((float)yi - cy) * z / fy;
-            o.z = z;
-            o.w = 1.0f;
-        }
-        d.ref_pts[0][i] = o;
-    } else {
-        d.cur_gray[0][i] = g;
-        d.cur_z[i] = z;
-        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (z < 0) {
-            o.x = ((float)xi - cx) * z / fx;
-            o.y = ((float)yi - cy) * z / fy;
-            o.z = z;
-            o.w = 1.0f;
-        }
-        d.cur_pts[0][i] = o;
-    }
 }
 
-// The current frame's whole pyramid in one pass: k_convert_level0's
-// conversion of the level-0 pixels and k_downsample's 2x2 reductions for the
-// coarser levels (the same expressions in the same order, so every value is
-// identical), computed per 16x16 tile of level 0 with the intermediate levels
+__global__ void k_convert_level0(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
+                                 const float *const *in_rgbd) {
+    INST_DESC;
+    const uint8_t *gp = in_gray[blockIdx.y];
+    const uint16_t *dp = in_depth[blockIdx.y];
+    const float *fp = in_rgbd[blockIdx.y];
+    if (!fp && (!gp || !dp)) return;  // instance not updated by this call
+    int n = d.W * d.H;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int xi = i % d.W, yi = i / d.W;
+    float g, z;
+    convert_pixel(d, gp, dp, fp, i, xi, yi, g, z);
+    float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
+    float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
+    d.ref_gray[0][i] = g;
+    d.ref_z[i] = z;
+    float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (z < -minDist && z > -maxDist) {
+        o.x = ((float)xi - cx) * z / fx;
+        o.y = ((float)yi - cy) * z / fy;
+        o.z = z;
+        o.w = 1.0f;
+    }
+    d.ref_pts[0][i] = o;
+}
+
+// The current frame's whole pyramid in one pass: the level-0 conversion
+// (convert_pixel, and genPointsCloud6Kernel, d2z.cu:436-469, for the cloud)
+// and the 2x2 reductions of fastDownSampleHdrKernel and downSampleCloud6Kernel
+// for the coarser levels (the expressions of k_downsample, in its order), computed per 16x16 tile of level 0 with the intermediate levels
 // in shared memory, so level 0 is not read back from memory.  One thread per
 // level-0 pixel of the tile; grid: tiles of the batch's largest frame x
 // instances.
@@ -116,7 +109,6 @@ __global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(con
     int W = d.W, H = d.H;
     float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
     float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
-    float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
     int lx = threadIdx.x % kPyrTile, ly = threadIdx.x / kPyrTile;
     // tiles with a grid stride (the launch uses one tile per CTA)
     for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
@@ -124,19 +116,11 @@ __global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(con
         if (tx * kPyrTile >= W || ty * kPyrTile >= H) continue;  // uniform over the CTA
         int xi = tx * kPyrTile + lx, yi = ty * kPyrTile + ly;
         __syncthreads();  // the previous tile's shared values are consumed
-        // level 0 (k_convert_level0)
+        // level 0
         if (xi < W && yi < H) {
             int i = xi + yi * W;
             float g, z;
-            if (fp) {
-                float4 p = __ldg((const float4 *)fp + xi + (H - 1 - yi) * W);
-                g = 0.3f * p.x + 0.59f * p.y + 0.11f * p.z;
-                z = -(p.w * (maxDist - minDist) + minDist);
-            } else {
-                g = (float)__ldg(gp + i) / 255.0f;
-                uint16_t dm = __ldg(dp + i);
-                z = dm ? -(float)dm : 0.0f;
-            }
+            convert_pixel(d, gp, dp, fp, i, xi, yi, g, z);
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
             if (z < 0) {
                 o.x = ((float)xi - cx) * z / fx;
@@ -190,9 +174,10 @@ __global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(con
     }
 }
 
-// fastDownSampleHdrKernel (downSample2Cuda.cu:35-42) for the gray pyramid and
-// downSampleCloud6Kernel (d2z.cu:557-588) for the point pyramid.
-__global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int *active) {
+// fastDownSampleHdrKernel (downSample2Cuda.cu:35-42) for the reference gray
+// pyramid and downSampleCloud6Kernel (d2z.cu:557-588) for its point and normal
+// pyramid.
+__global__ void k_downsample(const InstDesc *D, int level, const int *active) {
     INST_DESC;
     if (!active[blockIdx.y]) return;
     if (level >= d.L) return;
@@ -202,11 +187,10 @@ __global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int
     int x = i % wlo, y = i / wlo;
     int w2 = 2 * wlo;
     int h0 = 2 * x + 2 * y * w2;
-    const float *hi = is_ref ? d.ref_gray[level - 1] : d.cur_gray[level - 1];
-    float *lo = is_ref ? d.ref_gray[level] : d.cur_gray[level];
-    lo[i] = (hi[h0] + hi[h0 + 1] + hi[h0 + w2] + hi[h0 + w2 + 1]) / 4.0f;
+    const float *hi = d.ref_gray[level - 1];
+    d.ref_gray[level][i] = (hi[h0] + hi[h0 + 1] + hi[h0 + w2] + hi[h0 + w2 + 1]) / 4.0f;
 
-    const float4 *src = is_ref ? d.ref_pts[level - 1] : d.cur_pts[level - 1];
+    const float4 *src = d.ref_pts[level - 1];
     int offs[4] = {h0, h0 + 1, h0 + w2, h0 + w2 + 1};
     float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
     float ns = 0.0f;
@@ -217,36 +201,26 @@ __global__ void k_downsample(const InstDesc *D, int level, int is_ref, const int
             p0 += s.x;
             p1 += s.y;
             p2 += s.z;
-            if (is_ref) {
-                float4 nn = d.ref_nrm[level - 1][offs[k]];
-                n0 += nn.x;
-                n1 += nn.y;
-                n2 += nn.z;
-            }
+            float4 nn = d.ref_nrm[level - 1][offs[k]];
+            n0 += nn.x;
+            n1 += nn.y;
+            n2 += nn.z;
         }
     }
     if (ns > 0.0f) {
         p0 /= ns;
         p1 /= ns;
         p2 /= ns;
-        if (is_ref) {
-            n0 /= ns;
-            n1 /= ns;
-            n2 /= ns;
-            normalize3(n0, n1, n2);
-            d.ref_nrm[level][i] = make_float4(n0, n1, n2, 0.0f);
-        }
-        float4 o = make_float4(p0, p1, p2, 1.0f);
-        if (is_ref) d.ref_pts[level][i] = o;
-        else d.cur_pts[level][i] = o;
+        n0 /= ns;
+        n1 /= ns;
+        n2 /= ns;
+        normalize3(n0, n1, n2);
+        d.ref_nrm[level][i] = make_float4(n0, n1, n2, 0.0f);
+        d.ref_pts[level][i] = make_float4(p0, p1, p2, 1.0f);
     } else {
         float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (is_ref) {
-            d.ref_pts[level][i] = o;
-            d.ref_nrm[level][i] = o;
-        } else {
-            d.cur_pts[level][i] = o;
-        }
+        d.ref_pts[level][i] = o;
+        d.ref_nrm[level][i] = o;
     }
 }
 
@@ -973,7 +947,9 @@ __device__ void photo_iteration(const InstDesc &d, IterShared &sh, int level) {
 }
 
 // The inputs of ICP pixel `idx` of the level: its last Student-t weight and
-// its reference point and normal (weight 0 past the end of the grid).
+// its reference point and normal (weight 0 past the end of the grid).  (A
+// packed 24-byte point + normal layout was measured: no change, the kernel is
+// bound by latency and issue, not by these bytes.)
 __device__ __forceinline__ void icp_load(const InstDesc &d, int level, int idx, int npix, float &weight, float4 &p,
                                          float4 &rn) {
     weight = 0.0f;
