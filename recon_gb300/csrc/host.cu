@@ -30,10 +30,9 @@ __global__ void k_seg_scan(const InstDesc *D, const int *active);
 __global__ void k_seg_scatter(const InstDesc *D, const int *active);
 __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
-constexpr int kPyrTile = 16;
+constexpr int kPyrTile = 32;  // level-0 tile of k_prep_current_pyramid
 __global__ void k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *in_gray,
-                                       const uint16_t *const *in_depth, const float *const *in_rgbd, int tiles_x,
-                                       int tiles_y);
+                                       const uint16_t *const *in_depth, const float *const *in_rgbd, int tiles_x);
 __global__ void k_icp_student3(const InstDesc *D, int level);
 __global__ void k_icp_prepare(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
@@ -415,10 +414,9 @@ int prepare_current(recon_batch *b, const void **in = nullptr) {
         maxh = std::max(maxh, c.height);
     }
     int tx = (maxw + kPyrTile - 1) / kPyrTile, ty = (maxh + kPyrTile - 1) / kPyrTile;
-    // one tile per CTA (measured faster than fewer CTAs walking several tiles)
-    k_prep_current_pyramid<<<dim3(tx * ty, n), kPyrTile * kPyrTile, 0, b->stream>>>(
+    k_prep_current_pyramid<<<dim3(tx * ty, n), 256, 0, b->stream>>>(
         b->d_desc, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n),
-        tx, ty);
+        tx);
     g_launches += 1;
     CK(cudaGetLastError());
     return RECON_OK;

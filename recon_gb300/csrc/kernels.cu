@@ -85,20 +85,49 @@ __global__ void k_convert_level0(const InstDesc *D, const uint8_t *const *in_gra
 // The current frame's whole pyramid in one pass: the level-0 conversion
 // (convert_pixel, and genPointsCloud6Kernel, d2z.cu:436-469, for the cloud)
 // and the 2x2 reductions of fastDownSampleHdrKernel and downSampleCloud6Kernel
-// for the coarser levels (the expressions of k_downsample, in its order), computed per 16x16 tile of level 0 with the intermediate levels
-// in shared memory, so level 0 is not read back from memory.  One thread per
-// level-0 pixel of the tile; grid: tiles of the batch's largest frame x
-// instances.
-constexpr int kPyrTile = 16;
+// for the coarser levels (the expressions of k_downsample, in its order), so
+// every value is identical to the separate kernels'.  A CTA of 256 threads
+// takes a 32x32 tile of level 0: each thread converts one 2x2 block and
+// reduces it to its level-1 pixel in registers; levels 2 and 3 come from the
+// level-1 tile in shared memory.  Level 0 is never read back.
+constexpr int kPyrTile = 32;
 
-__global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(const InstDesc *D,
-                                                                             const uint8_t *const *in_gray,
-                                                                             const uint16_t *const *in_depth,
-                                                                             const float *const *in_rgbd, int tiles_x,
-                                                                             int tiles_y) {
+__device__ __forceinline__ void cloud_point(const InstDesc &d, int xi, int yi, float z, float4 &o) {
+    float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
+    float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
+    o = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (z < 0) {
+        o.x = ((float)xi - cx) * z / fx;
+        o.y = ((float)yi - cy) * z / fy;
+        o.z = z;
+        o.w = 1.0f;
+    }
+}
+
+// downSampleCloud6Kernel's average of the valid points among four (d2z.cu:557-588)
+__device__ __forceinline__ float4 down_points(const float4 &a, const float4 &b, const float4 &c, const float4 &e) {
+    float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, ns = 0.0f;
+    const float4 *q[4] = {&a, &b, &c, &e};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (q[k]->w != 0.0f) {
+            ns++;
+            p0 += q[k]->x;
+            p1 += q[k]->y;
+            p2 += q[k]->z;
+        }
+    }
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (ns > 0.0f) o = make_float4(p0 / ns, p1 / ns, p2 / ns, 1.0f);
+    return o;
+}
+
+__global__ void __launch_bounds__(256) k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *in_gray,
+                                                              const uint16_t *const *in_depth,
+                                                              const float *const *in_rgbd, int tiles_x) {
     __shared__ InstDesc sd;
-    __shared__ float sg[2][kPyrTile * kPyrTile];   // gray of the current and the next level (ping-pong)
-    __shared__ float4 sp[2][kPyrTile * kPyrTile];  // points (x y z mask)
+    __shared__ float sg[2][256];   // gray of levels 1 (16x16) and 2 (8x8)
+    __shared__ float4 sp[2][256];  // points of levels 1 and 2
     load_desc(sd, D + blockIdx.y);
     __syncthreads();
     const InstDesc &d = sd;
@@ -107,68 +136,67 @@ __global__ void __launch_bounds__(kPyrTile *kPyrTile) k_prep_current_pyramid(con
     const float *fp = in_rgbd[blockIdx.y];
     if (!fp && (!gp || !dp)) return;  // instance not updated by this call
     int W = d.W, H = d.H;
-    float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
-    float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
-    int lx = threadIdx.x % kPyrTile, ly = threadIdx.x / kPyrTile;
-    // tiles with a grid stride (the launch uses one tile per CTA)
-    for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
-        int tx = tile % tiles_x, ty = tile / tiles_x;
-        if (tx * kPyrTile >= W || ty * kPyrTile >= H) continue;  // uniform over the CTA
-        int xi = tx * kPyrTile + lx, yi = ty * kPyrTile + ly;
-        __syncthreads();  // the previous tile's shared values are consumed
-        // level 0
-        if (xi < W && yi < H) {
+    int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    if (tx * kPyrTile >= W || ty * kPyrTile >= H) return;
+    int t = threadIdx.x;
+    int bx = t % 16, by = t / 16;
+    int x0 = tx * kPyrTile + 2 * bx, y0 = ty * kPyrTile + 2 * by;
+    // level 0: the 2x2 block (x0, y0) .. (x0 + 1, y0 + 1), in k_downsample's order
+    float g[4];
+    float4 pt[4];
+    bool in0 = x0 < W && y0 < H;
+    if (in0) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int xi = x0 + (k & 1), yi = y0 + (k >> 1);
+            g[k] = 0.0f;
+            pt[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (xi >= W || yi >= H) continue;
             int i = xi + yi * W;
-            float g, z;
-            convert_pixel(d, gp, dp, fp, i, xi, yi, g, z);
-            float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (z < 0) {
-                o.x = ((float)xi - cx) * z / fx;
-                o.y = ((float)yi - cy) * z / fy;
-                o.z = z;
-                o.w = 1.0f;
-            }
-            d.cur_gray[0][i] = g;
-            if (d.cur_grayh[0]) d.cur_grayh[0][i] = __float2half_rn(g);  // mixed precision
+            float z;
+            convert_pixel(d, gp, dp, fp, i, xi, yi, g[k], z);
+            cloud_point(d, xi, yi, z, pt[k]);
+            d.cur_gray[0][i] = g[k];
+            if (d.cur_grayh[0]) d.cur_grayh[0][i] = __float2half_rn(g[k]);  // mixed precision
             d.cur_z[i] = z;
-            d.cur_pts[0][i] = o;
-            sg[0][threadIdx.x] = g;
-            sp[0][threadIdx.x] = o;
+            d.cur_pts[0][i] = pt[k];
         }
-        // levels 1.. (k_downsample, is_ref = 0): a tile of side kPyrTile >> l
-        int side = kPyrTile;
-        for (int l = 1; l < d.L; l++) {
-            __syncthreads();
-            int cur = (l - 1) & 1, nxt = l & 1;
-            int hs = side;  // side of the finer tile
-            side >>= 1;
-            int wlo = W >> l, hlo = H >> l;
-            if ((int)threadIdx.x < side * side) {
-                int ox = threadIdx.x % side, oy = threadIdx.x / side;
-                int gx = tx * side + ox, gy = ty * side + oy;
-                if (gx < wlo && gy < hlo) {
-                    int c0 = 2 * ox + 2 * oy * hs;
-                    int offs[4] = {c0, c0 + 1, c0 + hs, c0 + hs + 1};
-                    float gl = (sg[cur][offs[0]] + sg[cur][offs[1]] + sg[cur][offs[2]] + sg[cur][offs[3]]) / 4.0f;
-                    float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, ns = 0.0f;
-                    for (int k = 0; k < 4; k++) {
-                        float4 q = sp[cur][offs[k]];
-                        if (q.w != 0.0f) {
-                            ns++;
-                            p0 += q.x;
-                            p1 += q.y;
-                            p2 += q.z;
-                        }
-                    }
-                    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (ns > 0.0f) o = make_float4(p0 / ns, p1 / ns, p2 / ns, 1.0f);
-                    int i = gx + gy * wlo;
-                    d.cur_gray[l][i] = gl;
-                    if (d.cur_grayh[l]) d.cur_grayh[l][i] = __float2half_rn(gl);
-                    d.cur_pts[l][i] = o;
-                    sg[nxt][threadIdx.x] = gl;
-                    sp[nxt][threadIdx.x] = o;
-                }
+    }
+    if (d.L < 2) return;
+    // level 1 in registers (its pixel exists iff the whole block does)
+    int w1 = W >> 1, h1 = H >> 1;
+    int x1 = x0 >> 1, y1 = y0 >> 1;
+    if (in0 && x1 < w1 && y1 < h1) {
+        float gl = (g[0] + g[1] + g[2] + g[3]) / 4.0f;
+        float4 o = down_points(pt[0], pt[1], pt[2], pt[3]);
+        int i = x1 + y1 * w1;
+        d.cur_gray[1][i] = gl;
+        if (d.cur_grayh[1]) d.cur_grayh[1][i] = __float2half_rn(gl);
+        d.cur_pts[1][i] = o;
+        sg[0][t] = gl;
+        sp[0][t] = o;
+    }
+    // levels 2 and 3 from the 16x16 level-1 tile (slot 0), level 2 in slot 1
+    int side = 16;
+    for (int l = 2; l < d.L; l++) {
+        __syncthreads();
+        int src = (l - 2) & 1;
+        int hs = side;
+        side >>= 1;
+        int wl = W >> l, hl = H >> l;
+        if (t < side * side) {
+            int ox = t % side, oy = t / side;
+            int gx = tx * (kPyrTile >> l) + ox, gy = ty * (kPyrTile >> l) + oy;
+            if (gx < wl && gy < hl) {
+                int c0 = 2 * ox + 2 * oy * hs;
+                float gl = (sg[src][c0] + sg[src][c0 + 1] + sg[src][c0 + hs] + sg[src][c0 + hs + 1]) / 4.0f;
+                float4 o = down_points(sp[src][c0], sp[src][c0 + 1], sp[src][c0 + hs], sp[src][c0 + hs + 1]);
+                int i = gx + gy * wl;
+                d.cur_gray[l][i] = gl;
+                if (d.cur_grayh[l]) d.cur_grayh[l][i] = __float2half_rn(gl);
+                d.cur_pts[l][i] = o;
+                sg[1 - src][t] = gl;
+                sp[1 - src][t] = o;
             }
         }
     }
