@@ -48,7 +48,7 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
                              const float *Tf, float gate, const int *active);
 __global__ void k_ref_from_z(const InstDesc *D, const int *active);
 __global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
-                             __nv_bfloat16 *out);
+                             const __nv_bfloat16 *prev, __nv_bfloat16 *out, __nv_bfloat16 *net_in);
 __global__ void k_gate_candidate(const InstDesc *D, const float *net_out, const float *scale, float *cand,
                                  long long *cost);
 __global__ void k_gate_cost(const InstDesc *D, const float *cand, long long *cost);
@@ -555,13 +555,13 @@ int run_schedule(recon_batch *b) {
 int learned_start(recon_batch *b, const void **row) {
     int n = b->n;
     int cur = 1 - b->coarse_prev;
-    k_net_coarse<<<dim3((kNetW * kNetH + 255) / 256, n), 256, 0, b->stream>>>(
-        b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n), (__nv_bfloat16 *)b->d_coarse[cur]);
+    // the current coarse image and the network input (previous, current) in one pass
+    k_net_coarse<<<dim3((kNetW * kNetH + 31) / 32, n), 256, 0, b->stream>>>(
+        b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n),
+        (const __nv_bfloat16 *)b->d_coarse[b->coarse_prev], (__nv_bfloat16 *)b->d_coarse[cur],
+        (__nv_bfloat16 *)b->d_netin);
     g_launches += 1;
-    int rc = recon_initnet_pair(b->d_coarse[b->coarse_prev], b->d_coarse[cur], n, b->d_netin, b->stream);
-    if (rc) return rc;
-    g_launches += 1;
-    rc = nn::forward_on(b->net, b->d_netin, n, b->d_netout, b->stream);
+    int rc = nn::forward_on(b->net, b->d_netin, n, b->d_netout, b->stream);
     if (rc) return rc;
     g_launches += nn::forward_kernels(n);
     k_gate_candidate<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_netout, nn::scale_dev(b->net), b->d_cand, b->d_cost);
@@ -578,9 +578,9 @@ int learned_keyframe(recon_batch *b) {
     if (!b->net) return RECON_OK;
     int n = b->n;
     const void **row = b->d_inptr;
-    k_net_coarse<<<dim3((kNetW * kNetH + 255) / 256, n), 256, 0, b->stream>>>(
-        b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n),
-        (__nv_bfloat16 *)b->d_coarse[b->coarse_prev]);
+    k_net_coarse<<<dim3((kNetW * kNetH + 31) / 32, n), 256, 0, b->stream>>>(
+        b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n), nullptr,
+        (__nv_bfloat16 *)b->d_coarse[b->coarse_prev], nullptr);
     g_launches += 1;
     CK(cudaGetLastError());
     return RECON_OK;

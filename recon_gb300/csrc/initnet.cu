@@ -252,6 +252,7 @@ __global__ void k_conv_split_finish(const float *partial, int S, long long M, co
     long long m = e / (COUT / 2);
     int col = 2 * (int)(e % (COUT / 2));
     float v0 = 0.0f, v1 = 0.0f;
+#pragma unroll 4
     for (int q = 0; q < S; q++) {
         const float *pp = partial + ((long long)q * M + m) * COUT + col;
         v0 += pp[0];
@@ -498,6 +499,7 @@ int fsplit_for(int l, int n) {
     long long ctas = (M + 15) / 16;
     int NF = kCout[l] / 8, NG = NF < 8 ? NF : 8, KS = kConvWarps / NG;
     int nk = kpad(kCin[l]) / 16;
+    if (ctas > 76) return 1;  // at least half the SMs busy: the finishing pass would cost more
     long long s = (2 * 152) / ctas;
     if (s > nk / KS) s = nk / KS;
     return (int)(s < 1 ? 1 : s);

@@ -1593,33 +1593,52 @@ __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentT
 // Coarse network image ([60][80][2] BF16: gray, depth in metres / 4) of each
 // instance's uint8 / uint16 input frame, from the input pointer table
 // (gray pointers, then depth pointers); the formula of recon_initnet_coarse.
-__global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
-                             __nv_bfloat16 *out) {
+__global__ void __launch_bounds__(256) k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray,
+                                                     const uint16_t *const *in_depth, const __nv_bfloat16 *prev,
+                                                     __nv_bfloat16 *out, __nv_bfloat16 *net_in) {
+    // 8 threads per coarse pixel: thread s sums rows s, s + 8, ... of its block;
+    // the integer sums are exact, so the grouping does not change the result
     const InstDesc &d = D[blockIdx.y];
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= kNetW * kNetH) return;
+    int s = threadIdx.x & 7;
+    int p = blockIdx.x * (blockDim.x / 8) + (threadIdx.x >> 3);
     const uint8_t *g = in_gray[blockIdx.y];
     const uint16_t *dp = in_depth[blockIdx.y];
     if (!g || !dp) return;
+    bool valid = p < kNetW * kNetH;
     int W = d.W, bx = d.W / kNetW, by = d.H / kNetH;
-    int ox = p % kNetW, oy = p / kNetW;
+    int ox = valid ? p % kNetW : 0, oy = valid ? p / kNetW : 0;
     int gs = 0, cnt = 0;
     long long ds = 0;
-    for (int y = 0; y < by; y++)
-        for (int x = 0; x < bx; x++) {
-            long long o = (long long)(oy * by + y) * W + ox * bx + x;
-            gs += g[o];
-            int dv = dp[o];
-            if (dv) {
-                ds += dv;
-                cnt++;
+    if (valid)
+        for (int y = s; y < by; y += 8)
+            for (int x = 0; x < bx; x++) {
+                long long o = (long long)(oy * by + y) * W + ox * bx + x;
+                gs += __ldg(g + o);
+                int dv = __ldg(dp + o);
+                if (dv) {
+                    ds += dv;
+                    cnt++;
+                }
             }
-        }
+#pragma unroll
+    for (int m = 1; m < 8; m <<= 1) {
+        gs += __shfl_xor_sync(0xffffffffu, gs, m);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, m);
+        ds += __shfl_xor_sync(0xffffffffu, ds, m);
+    }
+    if (!valid || s != 0) return;
     float gv = (float)gs / (255.0f * (float)(bx * by));
     float dv = cnt ? ((float)ds / (float)cnt) / 4000.0f : 0.0f;
-    __nv_bfloat16 *o = out + ((long long)blockIdx.y * kNetW * kNetH + p) * 2;
-    o[0] = __float2bfloat16_rn(gv);
-    o[1] = __float2bfloat16_rn(dv);
+    long long q = (long long)blockIdx.y * kNetW * kNetH + p;
+    __nv_bfloat16 bg = __float2bfloat16_rn(gv), bd = __float2bfloat16_rn(dv);
+    out[2 * q] = bg;
+    out[2 * q + 1] = bd;
+    if (net_in) {  // the network input (previous gray, depth, current gray, depth)
+        net_in[4 * q + 0] = prev[2 * q];
+        net_in[4 * q + 1] = prev[2 * q + 1];
+        net_in[4 * q + 2] = bg;
+        net_in[4 * q + 3] = bd;
+    }
 }
 
 // Integer start-pose cost of one point: min(trunc(|r| * 1024), 1024) of its
