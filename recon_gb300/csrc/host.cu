@@ -172,6 +172,12 @@ struct recon_batch {
     int coarse_prev = 0;
     uint16_t *d_netin = nullptr;  // [n][60][80][4]
     float *d_netout = nullptr;    // [n][6]
+    // sequences: the network runs one frame ahead on net_stream (its input
+    // does not depend on the poses), into alternate output buffers
+    float *d_netout_seq[2] = {nullptr, nullptr};
+    const float *netout_last = nullptr;  // the outputs recon_batch_get_init reports
+    cudaStream_t net_stream = nullptr;
+    cudaEvent_t ev_net[2] = {nullptr, nullptr}, ev_gate[2] = {nullptr, nullptr}, ev_seq = nullptr;
     int *d_choice = nullptr;      // [n]: 1 where the learned start pose was taken
     float *d_cand = nullptr;      // [n][16]: candidate start poses
     long long *d_cost = nullptr;  // [n][2]: gate costs of the current pose and the candidate
@@ -552,25 +558,42 @@ int run_schedule(recon_batch *b) {
 // Learned start poses for the frame whose uint8 / uint16 inputs the pointer
 // table `row` (gray pointers, then depth pointers) holds: coarse image, network
 // on (previous, current), gate.  The current coarse image becomes the previous.
-int learned_start(recon_batch *b, const void **row) {
+// The network part on stream s: the coarse image of the frame whose inputs
+// `row` holds, the network input (previous, current) and the forward pass into
+// `out`.  The current coarse image becomes the previous.
+int learned_net(recon_batch *b, const void **row, cudaStream_t s, float *out) {
     int n = b->n;
     int cur = 1 - b->coarse_prev;
-    // the current coarse image and the network input (previous, current) in one pass
-    k_net_coarse<<<dim3((kNetW * kNetH + 31) / 32, n), 256, 0, b->stream>>>(
+    k_net_coarse<<<dim3((kNetW * kNetH + 31) / 32, n), 256, 0, s>>>(
         b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n),
         (const __nv_bfloat16 *)b->d_coarse[b->coarse_prev], (__nv_bfloat16 *)b->d_coarse[cur],
         (__nv_bfloat16 *)b->d_netin);
     g_launches += 1;
-    int rc = nn::forward_on(b->net, b->d_netin, n, b->d_netout, b->stream);
+    int rc = nn::forward_on(b->net, b->d_netin, n, out, s);
     if (rc) return rc;
     g_launches += nn::forward_kernels(n);
-    k_gate_candidate<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_netout, nn::scale_dev(b->net), b->d_cand, b->d_cost);
-    k_gate_cost<<<dim3((b->max_P + 255) / 256, n), 256, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost);
-    k_gate_pick<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost, b->d_choice);
-    g_launches += 3;
     b->coarse_prev = cur;
     CK(cudaGetLastError());
     return RECON_OK;
+}
+
+// The gate on the batch stream: candidate pose from the network outputs `out`
+// and the previous pose, the two coarse costs, the choice.
+int learned_gate(recon_batch *b, const float *out) {
+    int n = b->n;
+    k_gate_candidate<<<n, 32, 0, b->stream>>>(b->d_desc, out, nn::scale_dev(b->net), b->d_cand, b->d_cost);
+    k_gate_cost<<<dim3((b->max_P + 255) / 256, n), 256, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost);
+    k_gate_pick<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost, b->d_choice);
+    g_launches += 3;
+    b->netout_last = out;
+    CK(cudaGetLastError());
+    return RECON_OK;
+}
+
+int learned_start(recon_batch *b, const void **row) {
+    int rc = learned_net(b, row, b->stream, b->d_netout);
+    if (rc) return rc;
+    return learned_gate(b, b->d_netout);
 }
 
 // coarse image of the keyframe: the "previous frame" of the first tracked frame
@@ -789,6 +812,13 @@ int recon_batch_destroy(recon_batch *b) {
         if (b->ev_free[k]) cudaEventDestroy(b->ev_free[k]);
     }
     if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
+    for (int k = 0; k < 2; k++) {
+        if (b->d_netout_seq[k]) cudaFree(b->d_netout_seq[k]);
+        if (b->ev_net[k]) cudaEventDestroy(b->ev_net[k]);
+        if (b->ev_gate[k]) cudaEventDestroy(b->ev_gate[k]);
+    }
+    if (b->ev_seq) cudaEventDestroy(b->ev_seq);
+    if (b->net_stream) cudaStreamDestroy(b->net_stream);
     if (b->recon_stream) cudaStreamDestroy(b->recon_stream);
     if (b->ev_pose) cudaEventDestroy(b->ev_pose);
     if (b->ev_fused) cudaEventDestroy(b->ev_fused);
@@ -1160,33 +1190,71 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         CK(cudaEventRecord(b->ev_free[0], b->stream));
         CK(cudaEventRecord(b->ev_free[1], b->stream));
     }
-    for (int f = 0; f < nf; f++) {
-        const void **row;
-        if (on_device) {
-            row = b->d_seqptr + (size_t)f * 3 * n;
-        } else {
-            int k = f & 1;
-            row = b->d_seqptr + (size_t)k * 3 * n;
-            // copy frame f into slot k once the frame that used it (f-2) is done
-            CK(cudaStreamWaitEvent(b->copy_stream, b->ev_free[k], 0));
-            for (int i = 0; i < n; i++) {
-                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + i], gray[(size_t)f * n + i], px[i],
-                                   cudaMemcpyHostToDevice, b->copy_stream));
-                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + n + i], depth[(size_t)f * n + i],
-                                   2 * px[i], cudaMemcpyHostToDevice, b->copy_stream));
-            }
-            CK(cudaEventRecord(b->ev_copied[k], b->copy_stream));
-            CK(cudaStreamWaitEvent(b->stream, b->ev_copied[k], 0));
+    // the input row of frame f (staged frames alternate between two slots)
+    auto row_of = [&](int f) -> const void ** {
+        return b->d_seqptr + (size_t)(on_device ? f : (f & 1)) * 3 * n;
+    };
+    // copy frame f into slot f & 1 once the frame that used it (f - 2) is done
+    auto stage = [&](int f) -> int {
+        if (on_device) return RECON_OK;
+        int k = f & 1;
+        CK(cudaStreamWaitEvent(b->copy_stream, b->ev_free[k], 0));
+        for (int i = 0; i < n; i++) {
+            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + i], gray[(size_t)f * n + i], px[i],
+                               cudaMemcpyHostToDevice, b->copy_stream));
+            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + n + i], depth[(size_t)f * n + i],
+                               2 * px[i], cudaMemcpyHostToDevice, b->copy_stream));
         }
+        CK(cudaEventRecord(b->ev_copied[k], b->copy_stream));
+        return RECON_OK;
+    };
+    // The network input of a frame is two images, not a pose, so the network
+    // runs one frame ahead on its own stream while the batch stream tracks the
+    // previous frame; only the gate (which needs the previous pose) waits for it.
+    // Frame f's outputs go to d_netout_seq[f & 1], free once gate(f - 2) ran.
+    auto net_ahead = [&](int f) -> int {
+        int k = f & 1;
+        if (!on_device) CK(cudaStreamWaitEvent(b->net_stream, b->ev_copied[k], 0));
+        CK(cudaStreamWaitEvent(b->net_stream, b->ev_gate[k], 0));
+        int rc = learned_net(b, row_of(f), b->net_stream, b->d_netout_seq[k]);
+        if (rc) return rc;
+        CK(cudaEventRecord(b->ev_net[k], b->net_stream));
+        return RECON_OK;
+    };
+    if (b->net) {
+        if (!b->net_stream) CK(cudaStreamCreateWithFlags(&b->net_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) {
+            if (!b->ev_net[k]) CK(cudaEventCreateWithFlags(&b->ev_net[k], cudaEventDisableTiming));
+            if (!b->ev_gate[k]) CK(cudaEventCreateWithFlags(&b->ev_gate[k], cudaEventDisableTiming));
+        }
+        if (!b->ev_seq) CK(cudaEventCreateWithFlags(&b->ev_seq, cudaEventDisableTiming));
+        // the pointer table and the keyframe's coarse image are written on the batch stream
+        CK(cudaEventRecord(b->ev_seq, b->stream));
+        CK(cudaStreamWaitEvent(b->net_stream, b->ev_seq, 0));
+    }
+    int rc0 = stage(0);
+    if (rc0) return rc0;
+    if (b->net && (rc0 = net_ahead(0))) return rc0;
+    for (int f = 0; f < nf; f++) {
+        const void **row = row_of(f);
+        if (f + 1 < nf) {
+            int rc = stage(f + 1);
+            if (rc) return rc;
+            if (b->net && (rc = net_ahead(f + 1))) return rc;
+        }
+        if (!on_device) CK(cudaStreamWaitEvent(b->stream, b->ev_copied[f & 1], 0));
         int rc = prepare_current(b, row);
         if (rc) return rc;
         k_begin_track<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, 0);
         g_launches += 1;
         if (b->net) {
-            rc = learned_start(b, row);
+            CK(cudaStreamWaitEvent(b->stream, b->ev_net[f & 1], 0));
+            rc = learned_gate(b, b->d_netout_seq[f & 1]);
             if (rc) return rc;
+            CK(cudaEventRecord(b->ev_gate[f & 1], b->stream));
         }
-        // every reader of this frame's staged inputs has been issued
+        // every reader of this frame's staged inputs has been issued (the
+        // network's coarse image read it before ev_net, which the gate waited for)
         if (!on_device) CK(cudaEventRecord(b->ev_free[f & 1], b->stream));
         rc = run_schedule(b);
         if (rc) return rc;
@@ -1231,6 +1299,8 @@ int recon_batch_set_init_net(recon_batch *b, recon_initnet *net, const int32_t i
         for (int k = 0; k < 2; k++) CK(cudaMalloc(&b->d_coarse[k], px * 2 * sizeof(uint16_t)));
         CK(cudaMalloc(&b->d_netin, px * 4 * sizeof(uint16_t)));
         CK(cudaMalloc(&b->d_netout, (size_t)n * 6 * sizeof(float)));
+        for (int k = 0; k < 2; k++) CK(cudaMalloc(&b->d_netout_seq[k], (size_t)n * 6 * sizeof(float)));
+        b->netout_last = b->d_netout;
         CK(cudaMalloc(&b->d_choice, (size_t)n * sizeof(int)));
         CK(cudaMalloc(&b->d_cand, (size_t)n * 16 * sizeof(float)));
         CK(cudaMalloc(&b->d_cost, (size_t)n * 2 * sizeof(long long)));
@@ -1260,7 +1330,8 @@ int recon_batch_get_init(recon_batch *b, int32_t *choice, float *net_out) {
     if (!b || !b->net) return fail(RECON_ERR_STATE, "no network attached");
     if (choice) CK(cudaMemcpyAsync(choice, b->d_choice, (size_t)b->n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
     if (net_out)
-        CK(cudaMemcpyAsync(net_out, b->d_netout, (size_t)b->n * 6 * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaMemcpyAsync(net_out, b->netout_last, (size_t)b->n * 6 * sizeof(float), cudaMemcpyDeviceToHost,
+                           b->stream));
     CK(cudaStreamSynchronize(b->stream));
     return RECON_OK;
 }
