@@ -49,10 +49,9 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
 __global__ void k_ref_from_z(const InstDesc *D, const int *active);
 __global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
                              const __nv_bfloat16 *prev, __nv_bfloat16 *out, __nv_bfloat16 *net_in);
-__global__ void k_gate_candidate(const InstDesc *D, const float *net_out, const float *scale, float *cand,
-                                 long long *cost);
-__global__ void k_gate_cost(const InstDesc *D, const float *cand, long long *cost);
-__global__ void k_gate_pick(const InstDesc *D, const float *cand, const long long *cost, int *choice);
+__global__ void k_gate_twist(const InstDesc *D, const float *net_out, const float *scale, float *Dout);
+__global__ void k_gate(const InstDesc *D, const float *Dm_all, long long *cost, unsigned int *ticket, float *cand,
+                       int *choice);
 }  // namespace rt
 
 namespace nn {
@@ -180,7 +179,10 @@ struct recon_batch {
     cudaEvent_t ev_net[2] = {nullptr, nullptr}, ev_gate[2] = {nullptr, nullptr}, ev_seq = nullptr;
     int *d_choice = nullptr;      // [n]: 1 where the learned start pose was taken
     float *d_cand = nullptr;      // [n][16]: candidate start poses
-    long long *d_cost = nullptr;  // [n][2]: gate costs of the current pose and the candidate
+    long long *d_cost = nullptr;  // [n][2]: gate costs of the current pose and the candidate (0 between frames)
+    unsigned int *d_ticket = nullptr;  // [n]: CTAs of the gate that finished (0 between frames)
+    float *d_gateD = nullptr;     // [n][16]: exp of the network twist (single-frame path)
+    float *d_gateD_seq[2] = {nullptr, nullptr};  // the same for alternate frames of a sequence
     std::vector<std::vector<int>> plain_iters;  // schedules restored when the network is detached
 };
 
@@ -561,7 +563,7 @@ int run_schedule(recon_batch *b) {
 // The network part on stream s: the coarse image of the frame whose inputs
 // `row` holds, the network input (previous, current) and the forward pass into
 // `out`.  The current coarse image becomes the previous.
-int learned_net(recon_batch *b, const void **row, cudaStream_t s, float *out) {
+int learned_net(recon_batch *b, const void **row, cudaStream_t s, float *out, float *gateD) {
     int n = b->n;
     int cur = 1 - b->coarse_prev;
     k_net_coarse<<<dim3((kNetW * kNetH + 31) / 32, n), 256, 0, s>>>(
@@ -572,28 +574,29 @@ int learned_net(recon_batch *b, const void **row, cudaStream_t s, float *out) {
     int rc = nn::forward_on(b->net, b->d_netin, n, out, s);
     if (rc) return rc;
     g_launches += nn::forward_kernels(n);
+    k_gate_twist<<<n, 32, 0, s>>>(b->d_desc, out, nn::scale_dev(b->net), gateD);
+    g_launches += 1;
     b->coarse_prev = cur;
     CK(cudaGetLastError());
     return RECON_OK;
 }
 
-// The gate on the batch stream: candidate pose from the network outputs `out`
-// and the previous pose, the two coarse costs, the choice.
-int learned_gate(recon_batch *b, const float *out) {
+// The gate on the batch stream (one launch): candidate pose from the network's
+// exp(twist) `gateD` and the previous pose, the two coarse costs, the choice.
+int learned_gate(recon_batch *b, const float *out, const float *gateD) {
     int n = b->n;
-    k_gate_candidate<<<n, 32, 0, b->stream>>>(b->d_desc, out, nn::scale_dev(b->net), b->d_cand, b->d_cost);
-    k_gate_cost<<<dim3((b->max_P + 255) / 256, n), 256, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost);
-    k_gate_pick<<<n, 32, 0, b->stream>>>(b->d_desc, b->d_cand, b->d_cost, b->d_choice);
-    g_launches += 3;
+    k_gate<<<dim3((b->max_P + 255) / 256, n), 256, 0, b->stream>>>(b->d_desc, gateD, b->d_cost, b->d_ticket,
+                                                                    b->d_cand, b->d_choice);
+    g_launches += 1;
     b->netout_last = out;
     CK(cudaGetLastError());
     return RECON_OK;
 }
 
 int learned_start(recon_batch *b, const void **row) {
-    int rc = learned_net(b, row, b->stream, b->d_netout);
+    int rc = learned_net(b, row, b->stream, b->d_netout, b->d_gateD);
     if (rc) return rc;
-    return learned_gate(b, b->d_netout);
+    return learned_gate(b, b->d_netout, b->d_gateD);
 }
 
 // coarse image of the keyframe: the "previous frame" of the first tracked frame
@@ -837,6 +840,10 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->d_choice) cudaFree(b->d_choice);
     if (b->d_cand) cudaFree(b->d_cand);
     if (b->d_cost) cudaFree(b->d_cost);
+    if (b->d_ticket) cudaFree(b->d_ticket);
+    if (b->d_gateD) cudaFree(b->d_gateD);
+    for (int k = 0; k < 2; k++)
+        if (b->d_gateD_seq[k]) cudaFree(b->d_gateD_seq[k]);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RECON_OK;
@@ -1216,7 +1223,7 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         int k = f & 1;
         if (!on_device) CK(cudaStreamWaitEvent(b->net_stream, b->ev_copied[k], 0));
         CK(cudaStreamWaitEvent(b->net_stream, b->ev_gate[k], 0));
-        int rc = learned_net(b, row_of(f), b->net_stream, b->d_netout_seq[k]);
+        int rc = learned_net(b, row_of(f), b->net_stream, b->d_netout_seq[k], b->d_gateD_seq[k]);
         if (rc) return rc;
         CK(cudaEventRecord(b->ev_net[k], b->net_stream));
         return RECON_OK;
@@ -1249,7 +1256,7 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         g_launches += 1;
         if (b->net) {
             CK(cudaStreamWaitEvent(b->stream, b->ev_net[f & 1], 0));
-            rc = learned_gate(b, b->d_netout_seq[f & 1]);
+            rc = learned_gate(b, b->d_netout_seq[f & 1], b->d_gateD_seq[f & 1]);
             if (rc) return rc;
             CK(cudaEventRecord(b->ev_gate[f & 1], b->stream));
         }
@@ -1304,6 +1311,11 @@ int recon_batch_set_init_net(recon_batch *b, recon_initnet *net, const int32_t i
         CK(cudaMalloc(&b->d_choice, (size_t)n * sizeof(int)));
         CK(cudaMalloc(&b->d_cand, (size_t)n * 16 * sizeof(float)));
         CK(cudaMalloc(&b->d_cost, (size_t)n * 2 * sizeof(long long)));
+        CK(cudaMalloc(&b->d_ticket, (size_t)n * sizeof(unsigned int)));
+        CK(cudaMalloc(&b->d_gateD, (size_t)n * 16 * sizeof(float)));
+        for (int k = 0; k < 2; k++) CK(cudaMalloc(&b->d_gateD_seq[k], (size_t)n * 16 * sizeof(float)));
+        CK(cudaMemsetAsync(b->d_cost, 0, (size_t)n * 2 * sizeof(long long), b->stream));
+        CK(cudaMemsetAsync(b->d_ticket, 0, (size_t)n * sizeof(unsigned int), b->stream));
         CK(cudaMemsetAsync(b->d_coarse[0], 0, px * 2 * sizeof(uint16_t), b->stream));
         CK(cudaMemsetAsync(b->d_coarse[1], 0, px * 2 * sizeof(uint16_t), b->stream));
     }

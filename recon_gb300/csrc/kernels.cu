@@ -1654,46 +1654,47 @@ __device__ __forceinline__ long long gate_cost_point(const InstDesc &d, const fl
     return (u >= 1024.0f || !(u == u)) ? 1024 : (long long)(int)u;  // 0 <= u < 1024: a 32-bit conversion
 }
 
-// The learned start pose, step 1 (one warp per instance): the network's
-// frame-to-frame twist x = net_out * scale gives D = exp(A(x)) (the pose
-// update's exponential applied to the identity) and the candidate D * T;
-// the two gate costs of the instance are reset.
-__global__ void __launch_bounds__(32) k_gate_candidate(const InstDesc *D, const float *net_out, const float *scale,
-                                                       float *cand, long long *cost) {
+// The learned start pose, step 1 (one warp per instance, no pose needed, so it
+// runs with the network): the network's twist x = out * scale (FP32) mapped to
+// D = exp(A(x)) applied to the identity (wexpm_update, FP64, the tracker's own
+// pose update), stored as the float matrix the candidate D * T is formed from.
+__global__ void __launch_bounds__(32) k_gate_twist(const InstDesc *D, const float *net_out, const float *scale,
+                                                   float *Dout) {
     const InstDesc &d = D[blockIdx.x];
-    __shared__ float Tp[16], Dm[16];
+    __shared__ float Dm[16];
     __shared__ SolveScratch S;
     int t = threadIdx.x;
-    if (t < 16) {
-        Tp[t] = d.T[t];
-        Dm[t] = (t % 5 == 0) ? 1.0f : 0.0f;
-    }
-    if (t < 2) cost[2 * blockIdx.x + t] = 0;
+    if (t < 16) Dm[t] = (t % 5 == 0) ? 1.0f : 0.0f;
     __syncwarp();
     double x[6];
     for (int k = 0; k < 6; k++) x[k] = (double)(net_out[blockIdx.x * 6 + k] * scale[k]);
     wexpm_update(S, x, Dm, (double)d.opt_out, t);
-    if (t < 16) {
-        int r = t >> 2, c = t & 3;
-        cand[16 * blockIdx.x + t] = Dm[r * 4 + 0] * Tp[0 * 4 + c] + Dm[r * 4 + 1] * Tp[1 * 4 + c] +
-                                    Dm[r * 4 + 2] * Tp[2 * 4 + c] + Dm[r * 4 + 3] * Tp[3 * 4 + c];
-    }
+    if (t < 16) Dout[16 * blockIdx.x + t] = Dm[t];
 }
 
-// Step 2 (grid: point blocks x instances): the integer costs of the current
-// pose and of the candidate at the coarsest level, summed with atomics (exact,
-// so the sum does not depend on the order).
-__global__ void __launch_bounds__(256) k_gate_cost(const InstDesc *D, const float *cand, long long *cost) {
+// Step 2 (grid: point blocks x instances): the candidate Tc = D * T from the
+// previous pose T (FP32, as the oracle forms it), the integer costs of T and of
+// Tc at the coarsest level (exact integer sums, any order), and in the
+// instance's last CTA to finish (an atomic ticket) the choice: Tc replaces T
+// when its cost is strictly lower.  That CTA resets the costs and the ticket
+// for the next frame.
+__global__ void __launch_bounds__(256) k_gate(const InstDesc *D, const float *Dm_all, long long *cost,
+                                              unsigned int *ticket, float *cand, int *choice) {
     __shared__ InstDesc sd;
     __shared__ float Tp[16], Tc[16];
     __shared__ long long part[2][8];
+    __shared__ bool last;
     load_desc(sd, D + blockIdx.y);
     __syncthreads();
     const InstDesc &d = sd;
-    int t = threadIdx.x;
+    int t = threadIdx.x, inst = blockIdx.y;
+    if (t < 16) Tp[t] = __ldcg(d.T + t);
+    __syncthreads();
     if (t < 16) {
-        Tp[t] = __ldcg(d.T + t);
-        Tc[t] = __ldcg(cand + 16 * blockIdx.y + t);
+        const float *Dm = Dm_all + 16 * inst;
+        int r = t >> 2, c = t & 3;
+        Tc[t] = Dm[r * 4 + 0] * Tp[0 * 4 + c] + Dm[r * 4 + 1] * Tp[1 * 4 + c] + Dm[r * 4 + 2] * Tp[2 * 4 + c] +
+                Dm[r * 4 + 3] * Tp[3 * 4 + c];
     }
     __syncthreads();
     int level = d.L - 1;
@@ -1702,7 +1703,6 @@ __global__ void __launch_bounds__(256) k_gate_cost(const InstDesc *D, const floa
         c0 += gate_cost_point(d, Tp, level, i);
         c1 += gate_cost_point(d, Tc, level, i);
     }
-    // integer sums: any order gives the same totals
     for (int o = 16; o > 0; o >>= 1) {
         c0 += __shfl_xor_sync(0xffffffffu, c0, o);
         c1 += __shfl_xor_sync(0xffffffffu, c1, o);
@@ -1712,20 +1712,34 @@ __global__ void __launch_bounds__(256) k_gate_cost(const InstDesc *D, const floa
         part[1][t >> 5] = c1;
     }
     __syncthreads();
-    if (t < 2) {
-        long long s = 0;
-        for (int w = 0; w < 8; w++) s += part[t][w];
-        atomicAdd(reinterpret_cast<unsigned long long *>(cost + 2 * blockIdx.y + t), (unsigned long long)s);
+    if (t == 0) {
+        long long s0 = 0, s1 = 0;
+        for (int w = 0; w < 8; w++) {
+            s0 += part[0][w];
+            s1 += part[1][w];
+        }
+        atomicAdd(reinterpret_cast<unsigned long long *>(cost + 2 * inst), (unsigned long long)s0);
+        atomicAdd(reinterpret_cast<unsigned long long *>(cost + 2 * inst + 1), (unsigned long long)s1);
+        __threadfence();
+        last = atomicAdd(ticket + inst, 1u) == gridDim.x - 1;
     }
-}
-
-// Step 3: the candidate replaces the pose when its cost is strictly lower.
-__global__ void k_gate_pick(const InstDesc *D, const float *cand, const long long *cost, int *choice) {
-    const InstDesc &d = D[blockIdx.x];
-    int t = threadIdx.x;
-    bool take = cost[2 * blockIdx.x + 1] < cost[2 * blockIdx.x];
-    if (t < 16 && take) d.T[t] = cand[16 * blockIdx.x + t];
-    if (t == 0 && choice) choice[blockIdx.x] = take ? 1 : 0;
+    __syncthreads();
+    if (!last) return;
+    // every CTA's costs are in: the choice
+    __threadfence();
+    long long k0 = (long long)__ldcg(reinterpret_cast<unsigned long long *>(cost + 2 * inst));
+    long long k1 = (long long)__ldcg(reinterpret_cast<unsigned long long *>(cost + 2 * inst + 1));
+    bool take = k1 < k0;
+    if (t < 16) {
+        cand[16 * inst + t] = Tc[t];
+        if (take) d.T[t] = Tc[t];
+    }
+    if (t == 0) {
+        if (choice) choice[inst] = take ? 1 : 0;
+        cost[2 * inst] = 0;
+        cost[2 * inst + 1] = 0;
+        ticket[inst] = 0u;
+    }
 }
 
 // ------------------------------------------------------------------
