@@ -566,7 +566,7 @@ int run_schedule(recon_batch *b) {
 int learned_net(recon_batch *b, const void **row, cudaStream_t s, float *out, float *gateD) {
     int n = b->n;
     int cur = 1 - b->coarse_prev;
-    k_net_coarse<<<dim3((kNetW * kNetH + 31) / 32, n), 256, 0, s>>>(
+    k_net_coarse<<<dim3((kNetW * kNetH + 255) / 256, n), 256, 0, s>>>(
         b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n),
         (const __nv_bfloat16 *)b->d_coarse[b->coarse_prev], (__nv_bfloat16 *)b->d_coarse[cur],
         (__nv_bfloat16 *)b->d_netin);
@@ -604,7 +604,7 @@ int learned_keyframe(recon_batch *b) {
     if (!b->net) return RECON_OK;
     int n = b->n;
     const void **row = b->d_inptr;
-    k_net_coarse<<<dim3((kNetW * kNetH + 31) / 32, n), 256, 0, b->stream>>>(
+    k_net_coarse<<<dim3((kNetW * kNetH + 255) / 256, n), 256, 0, b->stream>>>(
         b->d_desc, (const uint8_t *const *)row, (const uint16_t *const *)(row + n), nullptr,
         (__nv_bfloat16 *)b->d_coarse[b->coarse_prev], nullptr);
     g_launches += 1;

@@ -1596,37 +1596,26 @@ __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentT
 __global__ void __launch_bounds__(256) k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray,
                                                      const uint16_t *const *in_depth, const __nv_bfloat16 *prev,
                                                      __nv_bfloat16 *out, __nv_bfloat16 *net_in) {
-    // 8 threads per coarse pixel: thread s sums rows s, s + 8, ... of its block;
-    // the integer sums are exact, so the grouping does not change the result
     const InstDesc &d = D[blockIdx.y];
-    int s = threadIdx.x & 7;
-    int p = blockIdx.x * (blockDim.x / 8) + (threadIdx.x >> 3);
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= kNetW * kNetH) return;
     const uint8_t *g = in_gray[blockIdx.y];
     const uint16_t *dp = in_depth[blockIdx.y];
     if (!g || !dp) return;
-    bool valid = p < kNetW * kNetH;
     int W = d.W, bx = d.W / kNetW, by = d.H / kNetH;
-    int ox = valid ? p % kNetW : 0, oy = valid ? p / kNetW : 0;
+    int ox = p % kNetW, oy = p / kNetW;
     int gs = 0, cnt = 0;
     long long ds = 0;
-    if (valid)
-        for (int y = s; y < by; y += 8)
-            for (int x = 0; x < bx; x++) {
-                long long o = (long long)(oy * by + y) * W + ox * bx + x;
-                gs += __ldg(g + o);
-                int dv = __ldg(dp + o);
-                if (dv) {
-                    ds += dv;
-                    cnt++;
-                }
+    for (int y = 0; y < by; y++)
+        for (int x = 0; x < bx; x++) {
+            long long o = (long long)(oy * by + y) * W + ox * bx + x;
+            gs += __ldg(g + o);
+            int dv = __ldg(dp + o);
+            if (dv) {
+                ds += dv;
+                cnt++;
             }
-#pragma unroll
-    for (int m = 1; m < 8; m <<= 1) {
-        gs += __shfl_xor_sync(0xffffffffu, gs, m);
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, m);
-        ds += __shfl_xor_sync(0xffffffffu, ds, m);
-    }
-    if (!valid || s != 0) return;
+        }
     float gv = (float)gs / (255.0f * (float)(bx * by));
     float dv = cnt ? ((float)ds / (float)cnt) / 4000.0f : 0.0f;
     long long q = (long long)blockIdx.y * kNetW * kNetH + p;
