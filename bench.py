@@ -46,10 +46,10 @@ B_PHOTO = 60
 B_ICP = 84
 # learned initialisation: trained parameters and the shortened schedule it runs
 LEARNED_WEIGHTS = "initnet_200k.npz"
-# (the schedule with the most frames per second inside the pose bound in a
-# sweep of shortened schedules on this trajectory; 1/2/4/2 keeps 97% of the
-# frames in bound but tracks 13% fewer of them per second)
-LEARNED_ITERS = (1, 2, 3, 1)
+# (in a sweep of shortened schedules on this trajectory: the most frames per
+# second inside the pose bound among schedules that run every level and keep
+# at least 90% of the frames in bound)
+LEARNED_ITERS = (1, 2, 2, 1)
 BOUND_MM, BOUND_DEG = 1.0, 0.05
 METRIC = "tracked frames/s at 640x480, pose err <=1mm/0.05deg vs the oracle: learned-init vs plain GPU"
 
