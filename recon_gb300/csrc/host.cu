@@ -32,7 +32,8 @@ __global__ void k_attr_jac(const InstDesc *D, const int *active);
 __global__ void k_icp_mask(const InstDesc *D, int level);
 constexpr int kPyrTile = 32;  // level-0 tile of k_prep_current_pyramid
 __global__ void k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *in_gray,
-                                       const uint16_t *const *in_depth, const float *const *in_rgbd, int tiles_x);
+                                       const uint16_t *const *in_depth, const float *const *in_rgbd, int tiles_x,
+                                       float *store_prev, int begin);
 __global__ void k_icp_student3(const InstDesc *D, int level);
 __global__ void k_icp_prepare(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
@@ -412,7 +413,9 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
 }
 
 // the current frame's level-0 conversion and pyramid in one launch
-int prepare_current(recon_batch *b, const void **in = nullptr) {
+// (in sequences the same launch stores the previous frame's pose into
+// `store_prev` and, with `begin`, starts the frame as k_begin_track does)
+int prepare_current(recon_batch *b, const void **in = nullptr, float *store_prev = nullptr, bool begin = false) {
     TimedScope ts(b, b->stream, TK_PREP_CUR, false);
     int n = b->n;
     if (!in) in = b->d_inptr;
@@ -424,7 +427,7 @@ int prepare_current(recon_batch *b, const void **in = nullptr) {
     int tx = (maxw + kPyrTile - 1) / kPyrTile, ty = (maxh + kPyrTile - 1) / kPyrTile;
     k_prep_current_pyramid<<<dim3(tx * ty, n), 256, 0, b->stream>>>(
         b->d_desc, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n),
-        tx);
+        tx, store_prev, begin ? 1 : 0);
     g_launches += 1;
     CK(cudaGetLastError());
     return RECON_OK;
@@ -1250,10 +1253,8 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
             if (b->net && (rc = net_ahead(f + 1))) return rc;
         }
         if (!on_device) CK(cudaStreamWaitEvent(b->stream, b->ev_copied[f & 1], 0));
-        int rc = prepare_current(b, row);
+        int rc = prepare_current(b, row, f > 0 ? b->d_Tseq + (size_t)(f - 1) * n * 16 : nullptr, true);
         if (rc) return rc;
-        k_begin_track<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tinit, 0);
-        g_launches += 1;
         if (b->net) {
             CK(cudaStreamWaitEvent(b->stream, b->ev_net[f & 1], 0));
             rc = learned_gate(b, b->d_netout_seq[f & 1], b->d_gateD_seq[f & 1]);
@@ -1265,10 +1266,11 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         if (!on_device) CK(cudaEventRecord(b->ev_free[f & 1], b->stream));
         rc = run_schedule(b);
         if (rc) return rc;
-        k_store_pose<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tseq + (size_t)f * n * 16);
-        g_launches += 1;
         CK(cudaGetLastError());
     }
+    // the last frame's pose (the earlier ones were stored by the next frame's pyramid launch)
+    k_store_pose<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tseq + (size_t)(nf - 1) * n * 16);
+    g_launches += 1;
     b->have_cur = true;
     if (T_out) CK(cudaMemcpyAsync(T_out, b->d_Tseq, need_T * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
     return recon_batch_get_poses(b, nullptr, stats);

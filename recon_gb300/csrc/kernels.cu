@@ -122,15 +122,33 @@ __device__ __forceinline__ float4 down_points(const float4 &a, const float4 &b, 
     return o;
 }
 
+// In a sequence the kernel also does the per-frame bookkeeping in CTA 0 of
+// each instance (saving two launches a frame): with `store_prev` it stores the
+// previous frame's tracked pose (k_store_pose), with `begin` it resets the
+// frame's statistics and sums (k_begin_track without an initial pose).
 __global__ void __launch_bounds__(256) k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *in_gray,
                                                               const uint16_t *const *in_depth,
-                                                              const float *const *in_rgbd, int tiles_x) {
+                                                              const float *const *in_rgbd, int tiles_x,
+                                                              float *store_prev, int begin) {
     __shared__ InstDesc sd;
     __shared__ float sg[2][256];   // gray of levels 1 (16x16) and 2 (8x8)
     __shared__ float4 sp[2][256];  // points of levels 1 and 2
     load_desc(sd, D + blockIdx.y);
     __syncthreads();
     const InstDesc &d = sd;
+    if (blockIdx.x == 0) {
+        int t = threadIdx.x;
+        if (store_prev && t < 16) store_prev[16 * blockIdx.y + t] = d.T[t];
+        if (begin) {
+            if (t < ST_COUNT) d.stats[t] = 0;
+            if (t == 0) {
+                *d.counter = 0u;
+                if (d.trace_count) *d.trace_count = 0;
+            }
+            for (int k = t; k < 2 * 27 * kFxLimbs; k += blockDim.x) d.fx[k] = 0ull;
+            if (t < 2) d.fx_bad[t] = 0;
+        }
+    }
     const uint8_t *gp = in_gray[blockIdx.y];
     const uint16_t *dp = in_depth[blockIdx.y];
     const float *fp = in_rgbd[blockIdx.y];
