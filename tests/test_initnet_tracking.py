@@ -91,6 +91,35 @@ def test_learned_start_matches_oracle(kind):
     assert_bitexact(Ts, T, f"sequence vs single-frame ({kind})")
 
 
+def test_device_and_host_sequences_agree():
+    """The sequence path with the network one frame ahead on a second stream:
+    device-resident frames and host frames (staged one frame ahead) give the
+    same decisions and poses, also for a second call on the same batch."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    cal, poses, g, d = _trajectory_frames(W, H, 6, seed=93)
+    params = IN.init_params(5, np.full(6, 0.01, np.float32))
+    out = []
+    for on_device in (False, True):
+        net = IN.InitNet(max_batch=2)
+        net.set_params(params)
+        cfg = rg.make_config(W, H, L, mode=rg.BIOBJECTIVE, iters=(2, 3, 4))
+        b = rg.Batch([cfg, cfg], [cal.calib, cal.calib])
+        b.set_init_net(net, ITERS)
+        if on_device:
+            gs = [torch.from_numpy(x).cuda() for x in g]
+            ds = [torch.from_numpy(x.view(np.int16)).cuda() for x in d]
+        else:
+            gs, ds = g, d
+        b.set_reference([gs[0], gs[1]], [ds[0], ds[1]])
+        T1, _ = b.track_sequence([[gs[f], gs[f + 1]] for f in range(1, 4)], [[ds[f], ds[f + 1]] for f in range(1, 4)])
+        T2, _ = b.track_sequence([[gs[f], gs[f]] for f in range(4, 6)], [[ds[f], ds[f]] for f in range(4, 6)])
+        c, o = b.init_choice()
+        out.append((T1, T2, c, o))
+    for k, what in enumerate(("first call", "second call", "choices", "network outputs")):
+        assert_bitexact(np.asarray(out[1][k]), np.asarray(out[0][k]), f"device vs host: {what}")
+
+
 def test_detaching_restores_plain_tracking():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
