@@ -196,21 +196,28 @@ def make_batch(cal, n_inst, stream, precision=0):
     return rg.Batch([cfg] * n_inst, [cal.calib] * n_inst, stream=stream)
 
 
-def run_step(batch, segs, gray_src, depth_src, poses_out):
-    """Tracks every segment of the trajectory once (inputs: device tensors or pinned host arrays).
+def step_plan(segs):
+    """The frame indices of one step: every segment's keyframe, and for each
+    sequence position s frame s of every segment (a shorter segment repeats
+    its last frame), with the mask of the positions that are its own frames."""
+    steps = max(len(fr) for _, fr in segs)
+    ref = np.array([k for k, _ in segs], np.int64)
+    seq = np.array([[fr[min(s, len(fr) - 1)] for _, fr in segs] for s in range(steps)], np.int64)
+    own = np.array([[s < len(fr) for _, fr in segs] for s in range(steps)])
+    return ref, seq, own
+
+
+def run_step(batch, plan, gray_src, depth_src, poses_out):
+    """Tracks every segment of the trajectory once (inputs: frame stacks
+    [frames, H, W] on the device or in pinned host memory).
 
     The keyframes of all segments are set in one call; the segments' frames are
     then tracked as one sequence (recon_batch_track_sequence): frame s of every
     segment per launch, each starting from the previous frame's pose."""
-    batch.set_reference([gray_src[k] for k, _ in segs], [depth_src[k] for k, _ in segs])
-    steps = max(len(fr) for _, fr in segs)
-    idx = [[fr[min(s, len(fr) - 1)] for _, fr in segs] for s in range(steps)]
-    T, st = batch.track_sequence([[gray_src[i] for i in row] for row in idx],
-                                 [[depth_src[i] for i in row] for row in idx])
-    for s in range(steps):
-        for j, (_, fr) in enumerate(segs):
-            if s < len(fr):
-                poses_out[fr[s]] = T[s, j]
+    ref, seq, own = plan
+    batch.set_reference_frames(gray_src, depth_src, ref)
+    T, _ = batch.track_sequence_frames(gray_src, depth_src, seq)
+    poses_out[seq[own]] = T[own]
     return poses_out
 
 
@@ -475,6 +482,7 @@ def main():
     cal, scene, poses = make_workload(seed, args.frames)
     segs = segments(args.frames)
     frames = [f for _, fr in segs for f in fr]
+    plan = step_plan(segs)
     gray, depth = render_frames_gpu(cal, scene, poses, seed, torch)
     stream = torch.cuda.Stream()
     batch = make_batch(cal, len(segs), stream.cuda_stream)
@@ -504,12 +512,12 @@ def main():
         """W warm-up steps, then K steps between a barrier + synchronize on both
         sides; (device ms, wall ms), slowest rank."""
         for _ in range(args.warmup):
-            run_step(batch, segs, src_g, src_d, out)
+            run_step(batch, plan, src_g, src_d, out)
         barrier()
         t0 = time.perf_counter()
         e0.record(stream)
         for _ in range(args.steps):
-            run_step(batch, segs, src_g, src_d, out)
+            run_step(batch, plan, src_g, src_d, out)
         e1.record(stream)
         barrier()
         wall = time.perf_counter() - t0
@@ -531,7 +539,7 @@ def main():
     batch.work(reset=True)
     batch.timing(reset=True)
     for _ in range(args.steps):
-        run_step(batch, segs, gray, depth, poses_plain)
+        run_step(batch, plan, gray, depth, poses_plain)
     torch.cuda.synchronize()
     timing = batch.timing(reset=True)
     work = batch.work(reset=True).astype(np.float64)
@@ -629,11 +637,11 @@ def main():
         mb.set_icp_chunks_per_cta(batch.icp_chunks_per_cta())
         poses_mixed = np.zeros_like(poses_plain)
         for _ in range(args.warmup):
-            run_step(mb, segs, gray, depth, poses_mixed)
+            run_step(mb, plan, gray, depth, poses_mixed)
         barrier()
         e0.record(stream)
         for _ in range(args.steps):
-            run_step(mb, segs, gray, depth, poses_mixed)
+            run_step(mb, plan, gray, depth, poses_mixed)
         e1.record(stream)
         barrier()
         ms_mixed = max_over_ranks(e0.elapsed_time(e1), world, "cuda")

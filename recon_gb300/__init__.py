@@ -174,6 +174,7 @@ class Batch:
         L = lib()
         self.n = len(configs)
         self.configs = list(configs)
+        self._resolutions = {(c.width, c.height) for c in self.configs}
         cfg_arr = (Config * self.n)(*configs)
         cal = np.ascontiguousarray(np.stack([np.asarray(c, np.float32).reshape(CALIB_SIZE) for c in calibs]))
         self._calib = cal
@@ -221,6 +222,70 @@ class Batch:
             g[i] = _ptr(gi).value
             d[i] = _ptr(di).value
         return g, d, int(dev or 0), keep
+
+    def _stack_table(self, stack, index, itemsize):
+        """Addresses of frames `index` (an integer array of any shape) of a
+        C-contiguous frame stack [F, H, W] (numpy array or torch tensor, host
+        or CUDA) as a uint64 pointer table, computed with numpy: base + index
+        times the frame's bytes.  Every instance must have the stack's
+        resolution.  Returns (table, on_device)."""
+        if isinstance(stack, np.ndarray):
+            if not stack.flags["C_CONTIGUOUS"]:
+                raise ValueError("frame stack must be C-contiguous")
+            base, dev, esz = stack.ctypes.data, 0, stack.itemsize
+        elif hasattr(stack, "data_ptr"):
+            if not stack.is_contiguous():
+                raise ValueError("frame stack must be contiguous")
+            base, dev, esz = stack.data_ptr(), int(stack.is_cuda), stack.element_size()
+        else:
+            raise TypeError(type(stack))
+        if len(stack.shape) != 3 or esz != itemsize:
+            raise ValueError(f"frame stack must be [frames, H, W] of {itemsize}-byte elements")
+        F, H, W = (int(v) for v in stack.shape)
+        if self._resolutions != {(W, H)}:
+            raise ValueError(f"instance resolutions {sorted(self._resolutions)} differ from the stack's {W}x{H}")
+        idx = np.asarray(index, np.int64)
+        if idx.size and (idx.min() < 0 or idx.max() >= F):
+            raise IndexError("frame index out of the stack")
+        table = np.uint64(base) + idx.astype(np.uint64) * np.uint64(H * W * itemsize)
+        return np.ascontiguousarray(table, np.uint64), dev
+
+    def _stack_tables(self, grays, depths, index, shape):
+        idx = np.asarray(index, np.int64)
+        if idx.shape != shape:
+            raise ValueError(f"frame index must have shape {shape}")
+        g, dg = self._stack_table(grays, idx, 1)
+        d, dd = self._stack_table(depths, idx, 2)
+        if dg != dd:
+            raise ValueError("mix of host and device inputs")
+        return g, d, dg
+
+    def set_reference_frames(self, grays, depths, index):
+        """set_reference from frame stacks: instance i takes frame index[i] of
+        grays [F, H, W] uint8 and depths [F, H, W] uint16 (or int16)."""
+        g, d, dev = self._stack_tables(grays, depths, index, (self.n,))
+        check(lib().recon_batch_set_reference(self.h, g.ctypes.data, d.ctypes.data, dev))
+
+    def set_current_frames(self, grays, depths, index):
+        """set_current from frame stacks (as set_reference_frames)."""
+        g, d, dev = self._stack_tables(grays, depths, index, (self.n,))
+        self._keep = [grays, depths]
+        check(lib().recon_batch_set_current(self.h, g.ctypes.data, d.ctypes.data, dev))
+
+    def track_sequence_frames(self, grays, depths, index):
+        """track_sequence from frame stacks: frame f of instance i is
+        index[f, i] of grays [F, H, W] uint8 and depths [F, H, W] uint16 (or
+        int16).  Returns poses [nf, n, 4, 4] and the last frame's stats."""
+        idx = np.asarray(index, np.int64)
+        if idx.ndim != 2:
+            raise ValueError("frame index must be [frames, instances]")
+        nf = idx.shape[0]
+        g, d, dev = self._stack_tables(grays, depths, idx, (nf, self.n))
+        T = np.zeros((nf, self.n, 16), np.float32)
+        stats = (TrackStats * self.n)()
+        check(lib().recon_batch_track_sequence(self.h, nf, g.ctypes.data, d.ctypes.data, dev, _ptr(T),
+                                               ctypes.cast(stats, ctypes.c_void_p)))
+        return T.reshape(nf, self.n, 4, 4), list(stats)
 
     def set_reference(self, grays, depths):
         g, d, dev, keep = self._ptr_tables(grays, depths)

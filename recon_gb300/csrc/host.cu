@@ -45,6 +45,7 @@ __global__ void k_reset_pose(const InstDesc *D, const int *active);
 __global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_init);
 __global__ void k_clear_ref(const InstDesc *D, const int *active);
 __global__ void k_store_pose(const InstDesc *D, float *dst);
+__global__ void k_gather_results(const InstDesc *D, int *dst);
 __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const uint16_t *const *depth,
                              const float *Tf, float gate, const int *active);
 __global__ void k_ref_from_z(const InstDesc *D, const int *active);
@@ -127,6 +128,10 @@ struct recon_batch {
     uint8_t *d_stage = nullptr;
     size_t stage_bytes = 0;
     float *d_Tinit = nullptr;
+    // [n][32] words: each instance's pose (16 floats) and statistics (16 ints),
+    // gathered by one kernel so the results come back in one copy
+    int *d_results = nullptr;
+    int *h_results = nullptr;  // pinned
     int trace_max = 0;
     recon_iter_trace *d_trace = nullptr;
     int *d_trace_count = nullptr;
@@ -643,6 +648,13 @@ __global__ void k_store_pose(const InstDesc *D, float *dst) {
     if (threadIdx.x < 16) dst[16 * blockIdx.y + threadIdx.x] = d.T[threadIdx.x];
 }
 
+__global__ void k_gather_results(const InstDesc *D, int *dst) {
+    const InstDesc &d = D[blockIdx.y];
+    int t = threadIdx.x;
+    if (t < 16) dst[32 * blockIdx.y + t] = __float_as_int(d.T[t]);
+    else if (t < 16 + ST_COUNT) dst[32 * blockIdx.y + t] = d.stats[t - 16];
+}
+
 __global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_init) {
     const InstDesc &d = D[blockIdx.y];
     int t = threadIdx.x;
@@ -778,6 +790,8 @@ int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs,
     if (e == cudaSuccess) e = cudaMalloc(&b->d_inptr, 3 * (size_t)n * sizeof(void *));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_active, n * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_Tinit, 16 * (size_t)n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_results, 32 * (size_t)n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_results, 32 * (size_t)n * sizeof(int));
     if (e != cudaSuccess) {
         recon_batch_destroy(b);
         return cuda_fail(e, "cudaMalloc(batch)");
@@ -807,6 +821,8 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->d_active) cudaFree(b->d_active);
     if (b->d_stage) cudaFree(b->d_stage);
     if (b->d_Tinit) cudaFree(b->d_Tinit);
+    if (b->d_results) cudaFree(b->d_results);
+    if (b->h_results) cudaFreeHost(b->h_results);
     if (b->d_trace) cudaFree(b->d_trace);
     if (b->d_trace_count) cudaFree(b->d_trace_count);
     if (b->d_seqptr) cudaFree(b->d_seqptr);
@@ -928,21 +944,25 @@ int recon_batch_track_async(recon_batch *b, const float *T_init_host) {
 int recon_batch_get_poses(recon_batch *b, float *T_out, recon_track_stats *stats) {
     clear_stale_error();
     if (!b) return fail(RECON_ERR_INVALID_ARG, "null batch");
-    std::vector<int> st((size_t)b->n * ST_COUNT);
-    for (int i = 0; i < b->n; i++) {
-        if (T_out) CK(cudaMemcpyAsync(T_out + 16 * (size_t)i, b->desc[i].T, 64, cudaMemcpyDeviceToHost, b->stream));
-        if (stats)
-            CK(cudaMemcpyAsync(st.data() + (size_t)i * ST_COUNT, b->desc[i].stats, ST_COUNT * sizeof(int),
-                               cudaMemcpyDeviceToHost, b->stream));
+    int n = b->n;
+    if (T_out || stats) {
+        static_assert(16 + ST_COUNT <= 32, "results record");
+        k_gather_results<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_results);
+        g_launches += 1;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(b->h_results, b->d_results, 32 * (size_t)n * sizeof(int), cudaMemcpyDeviceToHost,
+                           b->stream));
     }
     CK(cudaStreamSynchronize(b->stream));
+    if (T_out)
+        for (int i = 0; i < n; i++) memcpy(T_out + 16 * (size_t)i, b->h_results + 32 * (size_t)i, 64);
     if (b->timing) {
         collect_events(b, b->graph_events, false);
         collect_events(b, b->direct_events, true);
     }
     if (stats) {
         for (int i = 0; i < b->n; i++) {
-            const int *s = st.data() + (size_t)i * ST_COUNT;
+            const int *s = b->h_results + 32 * (size_t)i + 16;
             recon_track_stats &o = stats[i];
             memset(&o, 0, sizeof(o));
             o.iterations = s[ST_ITERS];
