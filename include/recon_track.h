@@ -238,6 +238,13 @@ typedef struct recon_photo_view {
 } recon_photo_view;
 int recon_photometric_iteration_noalloc(const recon_photo_view *view, float *T_dev, void *stream);
 
+/* ---- self-test of the Student-t truncation (no reference counterpart) ----
+ * The Student-t passes truncate r2 * w in [0, 2^23) to an integer with a
+ * round-toward-zero add of 2^23 instead of a conversion.  This compares the
+ * two for every float in [0, 2^23) on the current GPU and stores the number of
+ * mismatches (0 on a correct device). */
+int recon_selftest_exact_arith(int64_t *mismatches);
+
 /* ---- single tracker (PhotoTracker-style handle = batch of one) ---- */
 typedef recon_batch recon_tracker;
 int recon_tracker_create(const recon_config *cfg, const float *calib, void *stream, recon_tracker **out);

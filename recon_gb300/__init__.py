@@ -142,6 +142,7 @@ def lib() -> ctypes.CDLL:
             L.recon_launch_count.restype = i64
             L.recon_render_depth.argtypes = [vp, vp, f32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
             L.recon_render_gray.argtypes = [vp, vp, vp, vp]
+            L.recon_selftest_exact_arith.argtypes = [vp]
             _lib = L
     return _lib
 
@@ -432,6 +433,14 @@ TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_student_t", "prep_current", "pr
 
 def launch_count() -> int:
     return int(lib().recon_launch_count())
+
+
+def selftest_exact_arith() -> int:
+    """Mismatches of the Student-t passes' truncation against the conversion
+    over every float in [0, 2^23), run on the current GPU."""
+    out = np.zeros(1, np.int64)
+    check(lib().recon_selftest_exact_arith(out.ctypes.data))
+    return int(out[0])
 
 
 def _batch_extras():

@@ -439,9 +439,14 @@ int prepare_current(recon_batch *b, const void **in = nullptr, float *store_prev
 }
 
 // Levels with at most this many pixels per instance prepare their ICP
-// correspondences and weights in one cluster launch (k_icp_prepare, at most
-// 16 pixels per thread); larger ones use the wide mask grid + k_icp_student3.
-constexpr int kPrepareFusedMaxPix = 16 * 8 * 1024;
+// correspondences and weights in one cluster launch (k_icp_prepare, at most 4
+// pixels per thread); larger ones use the wide mask grid + k_icp_student3,
+// whose many small CTAs hide the gathers' latency better (at 320x240 with 30
+// instances the two launches beat the fused one by 1% of the frame).
+#ifndef RECON_PREPARE_FUSED_MAX_PIX
+#define RECON_PREPARE_FUSED_MAX_PIX (4 * 8 * 1024)
+#endif
+constexpr int kPrepareFusedMaxPix = RECON_PREPARE_FUSED_MAX_PIX;
 
 // Launches a kernel of the per-frame schedule as a programmatic dependent of
 // the previous kernel in the stream (a programmatic edge inside a graph): it

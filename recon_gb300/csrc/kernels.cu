@@ -12,6 +12,7 @@
 #include <mutex>
 
 #include "scene.h"
+#include "exact_arith.cuh"
 #include "fx.cuh"
 #include "solve.cuh"
 #include "track_kernels.cuh"
@@ -670,8 +671,13 @@ __device__ __forceinline__ long long trunc_f32_nonneg(float x) {
 // the reference's int truncation of r^2 w (estimateVariance1024, rgb2gray.cu:519-521)
 __device__ __forceinline__ long long trunc_prod(float r2, float w) {
     float prod = r2 * w;
+    if (prod >= 0.0f && prod < 8388608.0f) return trunc_small(prod);
     return (prod >= 0.0f && prod < 9.0e18f) ? trunc_f32_nonneg(prod) : (prod >= 9.0e18f ? 9000000000000000000LL : 0);
 }
+
+// The Student-t weight (rgb2gray.cu:537-540; the first pass's sigma^2 is 100,
+// rgb2gray.cu:827-850)
+__device__ __forceinline__ float student_w(float r2, float sigma2) { return 6 / (5 + r2 / sigma2); }
 
 // The residual and mask of pixel i of the level (icpResidualKernel2) from its
 // loaded reference point p and normal rn; returns the mask, sets r2.
@@ -750,7 +756,7 @@ __global__ void __launch_bounds__(kLanes) k_icp_mask(const InstDesc *D, int leve
             float r2;
             uint8_t ok = icp_mask_pixel(d, sT, level, p[u], rn[u], r2);
             if (ok) {
-                float w0 = 6 / (5 + r2 / 100.0f);
+                float w0 = student_w(r2, 100.0f);
                 vsum += trunc_prod(r2, w0);
             }
             d.icp_r2[i] = r2;
@@ -1431,7 +1437,6 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int 
 // correspondence count and the first sum are k_icp_mask's block totals.
 constexpr int kStudentThreads = 1024;
 
-__device__ __forceinline__ float student_w(float r2, float sigma2) { return 6 / (5 + r2 / sigma2); }
 
 // The body of the Student-t kernels.  With kMask the cluster first evaluates
 // the level's correspondences itself (k_icp_mask's per-pixel work, over the
@@ -1481,7 +1486,7 @@ __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
                 if (i >= n) continue;
                 float r2;
                 uint8_t ok = icp_mask_pixel(d, sT, level, p[u], rn[u], r2);
-                if (ok) v += trunc_prod(r2, 6 / (5 + r2 / 100.0f));
+                if (ok) v += trunc_prod(r2, student_w(r2, 100.0f));
                 d.icp_r2[i] = r2;
                 d.icp_mask[i] = ok;
                 c += ok;
@@ -1543,25 +1548,65 @@ __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
         float vv = (nsel <= 1024) ? Sf : (Sf < minVal ? minVal : Sf);
         float sigma2 = vv / (float)nsel;
         long long vsum = 0;
-        int i = rank * kStudentThreads + t;
-        float r_next = 0.0f;
-        uint8_t m_next = 0;
-        if (i < n) {
-            r_next = __ldg(d.icp_r2 + i);
-            m_next = __ldg(d.icp_mask + i);
-        }
-        for (; i < n; i += stride) {
-            // the next pixel's loads are in flight while this one is weighed
-            float r = r_next;
-            uint8_t mk = m_next;
-            if (i + stride < n) {
-                r_next = __ldg(d.icp_r2 + i + stride);
-                m_next = __ldg(d.icp_mask + i + stride);
+        if (!kMask && (n & 3) == 0) {
+            // k_icp_mask wrote the grid: any thread may read any pixel, so each
+            // takes four consecutive pixels per vector load, two groups in
+            // flight (the passes are bound by load latency, not by bytes)
+            const float4 *r4 = reinterpret_cast<const float4 *>(d.icp_r2);
+            const uchar4 *m4 = reinterpret_cast<const uchar4 *>(d.icp_mask);
+            float4 *w4 = reinterpret_cast<float4 *>(d.icp_w);
+            int ng = n >> 2;
+            for (int g0 = rank * kStudentThreads + t; g0 < ng; g0 += 2 * stride) {
+                float4 r[2];
+                uchar4 m[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    int g = g0 + u * stride;
+                    r[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    m[u] = make_uchar4(0, 0, 0, 0);
+                    if (g < ng) {
+                        r[u] = __ldg(r4 + g);
+                        m[u] = __ldg(m4 + g);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    int g = g0 + u * stride;
+                    if (g >= ng) continue;
+                    if (pass == 3) {
+                        w4[g] = make_float4(m[u].x ? fminf(student_w(r[u].x, sigma2), 1.0f) : 0.0f,
+                                            m[u].y ? fminf(student_w(r[u].y, sigma2), 1.0f) : 0.0f,
+                                            m[u].z ? fminf(student_w(r[u].z, sigma2), 1.0f) : 0.0f,
+                                            m[u].w ? fminf(student_w(r[u].w, sigma2), 1.0f) : 0.0f);
+                    } else {
+                        if (m[u].x) vsum += trunc_prod(r[u].x, student_w(r[u].x, sigma2));
+                        if (m[u].y) vsum += trunc_prod(r[u].y, student_w(r[u].y, sigma2));
+                        if (m[u].z) vsum += trunc_prod(r[u].z, student_w(r[u].z, sigma2));
+                        if (m[u].w) vsum += trunc_prod(r[u].w, student_w(r[u].w, sigma2));
+                    }
+                }
             }
-            if (pass == 3) {
-                d.icp_w[i] = mk ? fminf(student_w(r, sigma2), 1.0f) : 0.0f;
-            } else if (mk) {
-                vsum += trunc_prod(r, student_w(r, sigma2));
+        } else {
+            int i = rank * kStudentThreads + t;
+            float r_next = 0.0f;
+            uint8_t m_next = 0;
+            if (i < n) {
+                r_next = __ldg(d.icp_r2 + i);
+                m_next = __ldg(d.icp_mask + i);
+            }
+            for (; i < n; i += stride) {
+                // the next pixel's loads are in flight while this one is weighed
+                float r = r_next;
+                uint8_t mk = m_next;
+                if (i + stride < n) {
+                    r_next = __ldg(d.icp_r2 + i + stride);
+                    m_next = __ldg(d.icp_mask + i + stride);
+                }
+                if (pass == 3) {
+                    d.icp_w[i] = mk ? fminf(student_w(r, sigma2), 1.0f) : 0.0f;
+                } else if (mk) {
+                    vsum += trunc_prod(r, student_w(r, sigma2));
+                }
             }
         }
         if (pass == 3) break;
