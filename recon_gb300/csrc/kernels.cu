@@ -1362,6 +1362,11 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
 // its fixed-point sums to the instance's with integer atomics, so the result
 // does not depend on K or on the order in which CTAs finish; k_solve then
 // fuses, solves and updates the pose.
+//
+// Even iterations visit the instances, and the chunks within each, in reverse
+// order (CTAs start roughly in block order): a level-0 pass streams several
+// times L2's capacity, and the lines it touched last (or k_icp_mask touched
+// last, before iteration 0) are the ones the next pass then starts with.
 #ifndef RECON_ITER_MIN_BLOCKS
 #define RECON_ITER_MIN_BLOCKS 4
 #endif
@@ -1369,7 +1374,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
     k_iter(const InstDesc *D, int level, int it, int icp_per_cta) {
     pdl_trigger();
     __shared__ InstDesc sd;
-    load_desc(sd, D + blockIdx.y);
+    const bool rev = (it & 1) == 0;
+    load_desc(sd, D + (rev ? gridDim.y - 1 - blockIdx.y : blockIdx.y));
     __syncthreads();
     const InstDesc &d = sd;
     if (level >= d.L) return;
@@ -1399,7 +1405,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
                                                         : photo_cluster<false>(d, sh, level, role);
         if (!had) return;
     } else {
-        int c0 = (role - kCluster) * icp_per_cta;
+        int j = role - kCluster;
+        int c0 = (rev ? nicp - 1 - j : j) * icp_per_cta;
         icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), npix);
     }
     __syncthreads();
