@@ -160,6 +160,26 @@ def test_icp_correspondences_and_student_t_weights(pair):
                     "Student-t weights per pixel")
 
 
+@pytest.mark.parametrize("iters", [(3, 0), (2, 2)], ids=["level1_only", "both_levels"])
+def test_odd_level_size_matches_oracle(iters):
+    """482x362 with two levels: level 1 is 241x181 = 43,621 pixels, not a
+    multiple of 4 and above the fused preparation's limit, so its Student-t
+    passes take the scalar loop instead of the four-pixel vector loads (level 0
+    takes the vector loads).  With level 0 skipped, the per-pixel mask and
+    weights left by level 1 are compared too."""
+    p = frame_pair(482, 362, L=2, seed=31)
+    trk, orc, T, st, To, tro = run_pair(p, rg.BIOBJECTIVE, iters=iters)
+    compare_traces(trk.trace(0), tro)
+    assert_bitexact(T, To, "final pose")
+    if iters[1] == 0:
+        n = (482 >> 1) * (362 >> 1)
+        mask = trk.get_array(0, "icp_mask", 1, np.uint8, n)
+        sel = orc.get("icp_select", 1, n, np.int32)
+        assert np.array_equal(np.flatnonzero(mask), sel), "level-1 correspondence mask"
+        assert_bitexact(trk.get_array(0, "icp_w", 1, np.float32, n), orc.get("icp_w_px", 1, n, np.float32),
+                        "level-1 Student-t weights per pixel")
+
+
 def test_cg_solver_matches_oracle():
     p = frame_pair(320, 240, seed=21)
     trk, orc, T, st, To, tro = run_pair(p, rg.BIOBJECTIVE, solver=rg.SOLVER_CG, iters=(10, 10, 10))
