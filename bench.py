@@ -113,12 +113,14 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    """nvidia-smi clock / throttle-reason samples during the timed region,
+    kept in $RECON_BENCH_OUT (default bench_out/) as clocks_rank<i>.csv."""
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        out = os.environ.get("RECON_BENCH_OUT", os.path.join(ROOT, "bench_out"))
+        self.path = os.path.join(out, f"clocks_rank{index}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
