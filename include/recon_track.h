@@ -130,23 +130,15 @@ int recon_batch_get_poses(recon_batch *b, float *T_out, recon_track_stats *stats
  * reference, each frame starting from the previous frame's pose (the
  * reference tracker's behaviour between reference updates,
  * phototracker.cpp:691-728).  gray/depth: nf x n pointers, row f = frame f of
- * every instance.  Host inputs are copied on a second stream into two staging
- * slots, overlapping frame f+1's upload with frame f's tracking (pinned host
- * memory makes the copies asynchronous).  T_out: nf x n x 16 floats (host) or
- * NULL; stats: statistics of the last frame.  Synchronises once at the end. */
+ * every instance.  Host inputs are copied on a second stream into one device
+ * slot per frame, overlapping frame f+1's upload with frame f's tracking
+ * (pinned host memory makes the copies asynchronous); the slots keep the
+ * frames until the next call (recon_batch_fuse_sequence reads them).  T_out:
+ * nf x n x 16 floats (host) or NULL; stats: statistics of the last frame.
+ * Synchronises once at the end. */
 int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const *gray, const uint16_t *const *depth,
                                int32_t on_device, float *T_out, recon_track_stats *stats);
 
-/* Keyframe depth fusion: fuses nframes (1..8) tracked frames' depth maps into
- * every instance's keyframe depth (T_host: nframes x n x 16, keyframe -> frame
- * poses as returned by tracking; depth: nframes x n uint16 mm maps), gating on
- * |dz| < gate_mm, then rebuilds the photometric selection/Jacobians and the ICP
- * reference pyramid from the fused depth with the keyframe's gray image.  The
- * current pose is kept.  Runs on the batch's second (reconstruction) stream;
- * later tracking on the pose stream waits for it.  Reference analogues:
- * filterDepthIIRKernel (warp.cu:398-467, disabled), updateVoxelsKernel's
- * running mean (VoxelGrid_cuda.cu:1005-1013), KeyFrameModel::integrateDepthMaps
- * (KeyFrameModel.cpp:537-583, not compiled). */
 /* Learned initialisation (include/recon_initnet.h; no counterpart in the
  * reference, which starts every frame from the previous frame's pose).  With a
  * network attached, each tracked frame (recon_batch_track without a T_init,
@@ -162,6 +154,32 @@ int recon_batch_set_init_net(recon_batch *b, recon_initnet *net, const int32_t i
 /* The last frame's gate decisions (1: learned start pose) and network outputs [n][6]. */
 int recon_batch_get_init(recon_batch *b, int32_t *choice, float *net_out);
 
+/* Keyframe depth and colour fusion: fuses nframes (1..8) tracked frames into
+ * every instance's keyframe.  depth: nframes x n uint16 mm maps; gray:
+ * nframes x n uint8 images, or NULL to fuse depth only (the vertex colours are
+ * then kept).  T: nframes x n x 16 keyframe -> frame poses (host memory) as
+ * returned by tracking.  Every valid keyframe pixel is warped into each frame and back;
+ * a frame's depth that agrees within gate_mm enters the running mean of the
+ * pixel's depth, and its gray sample at the point enters the running mean of
+ * the pixel's vertex colour (which then replaces the keyframe's own sample as
+ * the photometric reference intensity at level 0).  The photometric selection
+ * and Jacobians and the ICP reference pyramid are rebuilt from the fused depth
+ * with the keyframe's gray image; the current pose is kept.  Runs on the
+ * batch's second (reconstruction) stream; later tracking on the pose stream
+ * waits for it.  Reference analogues: filterDepthIIRKernel (warp.cu:398-467,
+ * disabled), updateVoxelsKernel's running mean (VoxelGrid_cuda.cu:1005-1013),
+ * KeyFrameModel::integrateDepthMaps, which warps the neighbours' depth and RGB
+ * into the keyframe (KeyFrameModel.cpp:537-583, not compiled). */
+int recon_batch_fuse_keyframe_rgbd(recon_batch *b, int32_t nframes, const uint8_t *const *gray,
+                                   const uint16_t *const *depth, const float *T, int32_t on_device, float gate_mm);
+/* The same fusion (depth and colour) of the first nframes frames of the last
+ * recon_batch_track_sequence call, with their tracked poses: frames, poses and
+ * pointer tables are all taken on the device (the caller's device frames, or
+ * the library's device copies of host frames), so nothing is copied and the
+ * host does not wait.  It fails with RECON_ERR_STATE if that sequence had
+ * fewer frames. */
+int recon_batch_fuse_sequence(recon_batch *b, int32_t nframes, float gate_mm);
+/* Depth only, host poses: recon_batch_fuse_keyframe_rgbd with gray = NULL. */
 int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *const *depth, const float *T_host,
                               int32_t on_device, float gate_mm);
 
@@ -185,7 +203,7 @@ int recon_batch_get_trace(recon_batch *b, int32_t inst, recon_iter_trace *out, i
  * the schedule with CUDA events on the batch's stream; totals per kernel kind
  * (0 GN iteration linearisation, 1 ICP mask, 2 ICP compaction, 3 Student-t
  * pass, 4 current-frame preparation, 5 reference preparation, 6 GN iteration
- * solve and pose update) accumulate in
+ * solve and pose update, 7 keyframe fusion) accumulate in
  * recon_batch_get_poses and are read with recon_batch_get_timing.  Work
  * counters: per instance [photometric point-iterations, ICP point-iterations,
  * ICP mask pixels, 0]. */
@@ -196,7 +214,7 @@ void *recon_batch_stream(recon_batch *b); /* the cudaStream_t all work of the ba
 int64_t recon_launch_count(void);         /* kernels launched by the library so far (graph replays included) */
 
 /* Copies an internal device array of instance `inst` to host memory (tests).
- * Names: ref_gray, cur_gray, ref_z, cur_z, ref_pts, ref_nrm, cur_pts, sel_idx,
+ * Names: ref_gray, cur_gray, ref_z, ref_col, cur_z, ref_pts, ref_nrm, cur_pts, sel_idx,
  * sel_xyz, sel_I, sel_J, vtx, grad_hist, icp_nsel, and icp_mask (uint8) /
  * icp_w (float) per pixel of the last level the ICP term prepared (`level`
  * gives its size; icp_w is 0 where the pixel is not a correspondence).

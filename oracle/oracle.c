@@ -267,6 +267,14 @@ void orc_zmap_to_xyz(const float *zp, int W, int H, const float *calib, float *x
 /* xyz2CloudKernel, d2z.cu:235-331.  vdata uses the reference's stride-24 record
  * (rendering/VertexBuffer2.h:24). */
 void orc_xyz2cloud(const float *xyzw, int W, int H, const float *calib, const float *img, float *vdata) {
+    orc_xyz2cloud_col(xyzw, W, H, calib, img, NULL, vdata);
+}
+
+/* The same with a fused keyframe colour per IR pixel (orc_fuse_rgbd): where
+ * col[offset] >= 0 it is the vertex colour (slot 14) in place of the bilinear
+ * sample of img; the gradients are still taken from img. */
+void orc_xyz2cloud_col(const float *xyzw, int W, int H, const float *calib, const float *img, const float *col,
+                       float *vdata) {
     const float *T = &calib[TLR_OFFSET];
     const float *KR = &calib[KR_OFFSET];
     const float *kc = &calib[KCR_OFFSET];
@@ -286,6 +294,7 @@ void orc_xyz2cloud(const float *xyzw, int W, int H, const float *calib, const fl
                 int xdi = ftoi(px), ydi = ftoi(py);
                 float fx = px - xdi, fy = py - ydi;
                 float color1 = bilin(xdi, ydi, fx, fy, W, img);
+                if (col && col[offset] >= 0.0f) color1 = col[offset];
                 float colorN = bilin(ftoi(px), ftoi(py - 1.0f), fx, fy, W, img);
                 float colorE = bilin(ftoi(px + 1.0f), ftoi(py), fx, fy, W, img);
                 float colorW = bilin(ftoi(px - 1.0f), ftoi(py), fx, fy, W, img);
@@ -1300,10 +1309,41 @@ void orc_linear_fuse(double A1[36], double b1[6], double w1, int N1, const doubl
  * mean of updateVoxelsKernel, VoxelGrid_cuda.cu:1005-1013). */
 void orc_fuse_depth(const float *zkey, int W, int H, const float *calib, int nframes, const float *const *zframes,
                     const float *Tframes, float gate_mm, float *zout, float *wout) {
+    orc_fuse_rgbd(zkey, NULL, W, H, calib, nframes, zframes, NULL, Tframes, gate_mm, zout, wout, NULL);
+}
+
+/* Gray value the RGB camera sees at point q of its rig's IR frame: TLR,
+ * distortPoint and the bilinear tap of xyz2CloudKernel's color1
+ * (d2z.cu:235-331).  -1 where the 2x2 taps leave the image. */
+static inline float rgb_sample(const float *calib, const float *q, const float *img, int W, int H) {
+    float r3[3];
+    mul4(&calib[TLR_OFFSET], q, r3);
+    float pux = r3[0] / r3[2];
+    float puy = r3[1] / r3[2];
+    float px, py;
+    distort(pux, puy, &calib[KCR_OFFSET], &calib[KR_OFFSET], &px, &py);
+    int xdi = ftoi(px), ydi = ftoi(py);
+    if (!(xdi >= 0 && ydi >= 0 && xdi < W - 1 && ydi < H - 1)) return -1.0f;
+    float fx = px - xdi, fy = py - ydi;
+    return bilin(xdi, ydi, fx, fy, W, img);
+}
+
+/* Keyframe depth and colour fusion.  Depth as orc_fuse_depth.  Colour (when
+ * gkey, gframes and cout are given): the vertex colour of every valid keyframe
+ * pixel is the mean of the keyframe's own sample at the point (rgb_sample of
+ * gkey) and the samples of the frames whose depth passed the gate (rgb_sample
+ * of frame f's gray image at T_f p), the weighted running mean of
+ * updateVoxelsKernel (VoxelGrid_cuda.cu:1005-1013) with unit weights, as
+ * KeyFrameModel::integrateDepthMaps warps the neighbours' RGB images into the
+ * keyframe (KeyFrameModel.cpp:537-583).  cout is -1 where no sample exists. */
+void orc_fuse_rgbd(const float *zkey, const float *gkey, int W, int H, const float *calib, int nframes,
+                   const float *const *zframes, const float *const *gframes, const float *Tframes, float gate_mm,
+                   float *zout, float *wout, float *cout) {
     float minDist = calib[MIND_OFFSET];
     float maxDist = calib[MAXD_OFFSET];
     const float *KL = &calib[KL_OFFSET];
     float fx = KL[0], fy = KL[4], cx = KL[2], cy = KL[5];
+    int colour = gkey && gframes && cout;
     float Tinv[8][16];
     for (int f = 0; f < nframes && f < 8; f++) invert_rt4f(&Tframes[16 * f], Tinv[f]);
 #pragma omp parallel for schedule(static)
@@ -1313,10 +1353,19 @@ void orc_fuse_depth(const float *zkey, int W, int H, const float *calib, int nfr
         if (!(z < -minDist && z > -maxDist)) {
             zout[idx] = z;
             wout[idx] = 0.0f;
+            if (colour) cout[idx] = -1.0f;
             continue;
         }
         float p[3] = {((float)xi - cx) * z / fx, ((float)yi - cy) * z / fy, z};
         float zsum = z, wsum = 1.0f;
+        float csum = 0.0f, cw = 0.0f;
+        if (colour) {
+            float c0 = rgb_sample(calib, p, gkey, W, H);
+            if (c0 >= 0.0f) {
+                csum = c0;
+                cw = 1.0f;
+            }
+        }
         for (int f = 0; f < nframes && f < 8; f++) {
             float q[3];
             mul4(&Tframes[16 * f], p, q);
@@ -1334,10 +1383,18 @@ void orc_fuse_depth(const float *zkey, int W, int H, const float *calib, int nfr
             if (fabsf(dz) < gate_mm) {
                 zsum += mk[2];
                 wsum += 1.0f;
+                if (colour) {
+                    float c = rgb_sample(calib, q, gframes[f], W, H);
+                    if (c >= 0.0f) {
+                        csum += c;
+                        cw += 1.0f;
+                    }
+                }
             }
         }
         zout[idx] = zsum / wsum;
         wout[idx] = wsum;
+        if (colour) cout[idx] = cw > 0.0f ? csum / cw : -1.0f;
     }
 }
 
@@ -1370,6 +1427,8 @@ struct orc_tracker {
     /* reference */
     float *ref_gray[ORC_MAX_LEVELS];
     float *ref_z;
+    float *ref_col;    /* fused vertex colour per IR pixel (orc_fuse_rgbd), valid when has_col */
+    int has_col;
     float *ref_xyzw;
     float *vdata;
     int32_t *sel_idx;
@@ -1425,6 +1484,7 @@ orc_tracker *orc_create(const orc_config *cfg, const float *calib) {
         t->sel_J[l] = (float *)xmalloc(6 * P * sizeof(float));
     }
     t->ref_z = (float *)xmalloc(W * H * sizeof(float));
+    t->ref_col = (float *)xmalloc(W * H * sizeof(float));
     t->cur_z = (float *)xmalloc(W * H * sizeof(float));
     t->ref_xyzw = (float *)xmalloc(4 * W * H * sizeof(float));
     t->vdata = (float *)xmalloc(24 * (size_t)W * H * sizeof(float));
@@ -1463,7 +1523,7 @@ void orc_destroy(orc_tracker *t) {
         free(t->ref_gray[l]); free(t->cur_gray[l]); free(t->ref6[l]); free(t->cur6[l]);
         free(t->refmask[l]); free(t->curmask[l]); free(t->sel_I[l]); free(t->sel_J[l]);
     }
-    free(t->ref_z); free(t->cur_z); free(t->ref_xyzw); free(t->vdata); free(t->sel_idx); free(t->sel_xyz);
+    free(t->ref_z); free(t->ref_col); free(t->cur_z); free(t->ref_xyzw); free(t->vdata); free(t->sel_idx); free(t->sel_xyz);
     free(t->r); free(t->zw); free(t->w); free(t->rw);
     for (int c = 0; c < 6; c++) free(t->Jw[c]);
     free(t->full_res); free(t->rmask); free(t->select);
@@ -1482,7 +1542,7 @@ static int prepare_reference(orc_tracker *t, const float *gray0, const float *z0
     for (int l = 1; l < L; l++) orc_downsample2(t->ref_gray[l - 1], W >> l, H >> l, t->ref_gray[l]);
     /* photometric */
     orc_zmap_to_xyz(t->ref_z, W, H, t->calib, t->ref_xyzw);
-    orc_xyz2cloud(t->ref_xyzw, W, H, t->calib, t->ref_gray[0], t->vdata);
+    orc_xyz2cloud_col(t->ref_xyzw, W, H, t->calib, t->ref_gray[0], t->has_col ? t->ref_col : NULL, t->vdata);
     float *grad = (float *)xmalloc(W * H * sizeof(float));
     for (int i = 0; i < W * H; i++) grad[i] = t->vdata[i * 24 + 13];
     int32_t hist[1024];
@@ -1519,6 +1579,7 @@ static int prepare_reference(orc_tracker *t, const float *gray0, const float *z0
 }
 
 int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0) {
+    t->has_col = 0;
     return prepare_reference(t, gray0, z0, 1);
 }
 
@@ -1526,18 +1587,36 @@ int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0)
  * (keyframe -> frame), then the reference is rebuilt from the fused depth
  * with the keyframe's gray image; the current pose is kept. */
 int orc_fuse_keyframe(orc_tracker *t, int nframes, const uint16_t *const *depth, const float *Tframes, float gate) {
+    return orc_fuse_keyframe_rgbd(t, nframes, NULL, depth, Tframes, gate);
+}
+
+/* The same with the frames' gray images (uint8, RGB camera): the keyframe's
+ * vertex colours become the fused colours (orc_fuse_rgbd).  gray NULL fuses
+ * depth only and leaves the colours as they were. */
+int orc_fuse_keyframe_rgbd(orc_tracker *t, int nframes, const uint8_t *const *gray, const uint16_t *const *depth,
+                           const float *Tframes, float gate) {
     if (!t->has_ref || nframes < 0 || nframes > 8) return -1;
     int n = t->W * t->H;
-    float *zf[8];
+    float *zf[8], *gf[8];
     for (int f = 0; f < nframes; f++) {
         zf[f] = (float *)xmalloc(n * sizeof(float));
         orc_convert_depth(depth[f], n, zf[f]);
+        gf[f] = NULL;
+        if (gray) {
+            gf[f] = (float *)xmalloc(n * sizeof(float));
+            orc_convert_gray(gray[f], n, gf[f]);
+        }
     }
     float *zout = (float *)xmalloc(n * sizeof(float));
     float *wout = (float *)xmalloc(n * sizeof(float));
-    orc_fuse_depth(t->ref_z, t->W, t->H, t->calib, nframes, (const float *const *)zf, Tframes, gate, zout, wout);
+    orc_fuse_rgbd(t->ref_z, gray ? t->ref_gray[0] : NULL, t->W, t->H, t->calib, nframes, (const float *const *)zf,
+                  gray ? (const float *const *)gf : NULL, Tframes, gate, zout, wout, gray ? t->ref_col : NULL);
+    if (gray) t->has_col = 1;
     int rc = prepare_reference(t, NULL, zout, 0);
-    for (int f = 0; f < nframes; f++) free(zf[f]);
+    for (int f = 0; f < nframes; f++) {
+        free(zf[f]);
+        free(gf[f]);
+    }
     free(zout);
     free(wout);
     return rc;
@@ -1754,6 +1833,7 @@ int orc_get_array(orc_tracker *t, const char *name, int level, void *dst, int64_
     else if (!strcmp(name, "vdata")) { src = t->vdata; n = (int64_t)t->W * t->H * 96; }
     else if (!strcmp(name, "cur_z")) { src = t->cur_z; n = (int64_t)t->W * t->H * 4; }
     else if (!strcmp(name, "ref_z")) { src = t->ref_z; n = (int64_t)t->W * t->H * 4; }
+    else if (!strcmp(name, "ref_col")) { src = t->ref_col; n = (int64_t)t->W * t->H * 4; }
     else if (!strcmp(name, "T")) { src = t->T; n = 64; }
     else if (!strcmp(name, "icp_w")) { src = t->icp_w; n = (int64_t)t->nsel[level] * 4; }
     else if (!strcmp(name, "icp_select")) { src = t->select; n = (int64_t)t->nsel[level] * 4; }

@@ -89,6 +89,8 @@ void orc_downsample2(const float *hi, int wlo, int hlo, float *lo);
 /* ---- photometric reference preparation ---- */
 void orc_zmap_to_xyz(const float *z, int W, int H, const float *calib, float *xyzw);
 void orc_xyz2cloud(const float *xyzw, int W, int H, const float *calib, const float *gray0, float *vdata);
+void orc_xyz2cloud_col(const float *xyzw, int W, int H, const float *calib, const float *gray0, const float *col,
+                       float *vdata);
 void orc_grad_histogram(const float *grad, int n, int nbins, int32_t *hist);
 int orc_filter_indices(const float *grad, int n, const int32_t *hist, int nbins, int P, int32_t *idx_out);
 void orc_add_vertex_attributes(const int32_t *idx, int P, float *vdata, int W, int H, const float *calib,
@@ -143,6 +145,9 @@ void orc_linear_fuse(double A1[36], double b1[6], double w1, int N1, const doubl
 /* ---- keyframe fusion ---- */
 void orc_fuse_depth(const float *zkey, int W, int H, const float *calib, int nframes, const float *const *zframes,
                     const float *Tframes, float gate_mm, float *zout, float *wout);
+void orc_fuse_rgbd(const float *zkey, const float *gkey, int W, int H, const float *calib, int nframes,
+                   const float *const *zframes, const float *const *gframes, const float *Tframes, float gate_mm,
+                   float *zout, float *wout, float *cout);
 
 /* ---- whole tracker (operator level, phototracker.cpp / shapetracker.cpp) ---- */
 orc_tracker *orc_create(const orc_config *cfg, const float *calib);
@@ -151,6 +156,8 @@ int orc_set_reference(orc_tracker *t, const uint8_t *gray, const uint16_t *depth
 int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0);
 int orc_set_current(orc_tracker *t, const uint8_t *gray, const uint16_t *depth);
 int orc_fuse_keyframe(orc_tracker *t, int nframes, const uint16_t *const *depth, const float *Tframes, float gate);
+int orc_fuse_keyframe_rgbd(orc_tracker *t, int nframes, const uint8_t *const *gray, const uint16_t *const *depth,
+                           const float *Tframes, float gate);
 int orc_track(orc_tracker *t, float *T, orc_iter_trace *trace, int max_trace);
 /* learned start pose gate (k_init_gate); 1 when the network's candidate was taken */
 int orc_init_gate(orc_tracker *t, const float net_out[6], const float scale[6]);
@@ -158,6 +165,22 @@ void orc_set_pose(orc_tracker *t, const float T[16]);
 void orc_get_pose(orc_tracker *t, float T[16]);
 int orc_get_array(orc_tracker *t, const char *name, int level, void *dst, int64_t nbytes);
 int orc_n_icp_selected(orc_tracker *t, int level);
+
+/* ---- FP64 oracle (oracle_fp64.c): the same tracker with every operation in
+ * double and the pose kept in double; the judge of pose error ---- */
+typedef struct orc64_tracker orc64_tracker;
+orc64_tracker *orc64_create(const orc_config *cfg, const float *calib);
+void orc64_destroy(orc64_tracker *t);
+int orc64_set_reference(orc64_tracker *t, const uint8_t *gray, const uint16_t *depth);
+int orc64_set_current(orc64_tracker *t, const uint8_t *gray, const uint16_t *depth);
+/* depth and (gray non-NULL) colour fusion of nframes frames, poses keyframe -> frame */
+int orc64_fuse_keyframe(orc64_tracker *t, int nframes, const uint8_t *const *gray, const uint16_t *const *depth,
+                        const double *Tframes, double gate);
+/* the plain schedule from T (NULL: the tracker's pose); returns iterations run */
+int orc64_track(orc64_tracker *t, double *T);
+void orc64_get_pose(const orc64_tracker *t, double T[16]);
+void orc64_set_pose(orc64_tracker *t, const double T[16]);
+int orc64_get_array(orc64_tracker *t, const char *name, int level, void *dst, int64_t nbytes);
 
 /* ---- procedural scene (CPU twin of the GPU renderer) ---- */
 struct recon_scene;

@@ -134,6 +134,8 @@ def lib() -> ctypes.CDLL:
             L.recon_reset.argtypes = [vp]
             L.recon_batch_track_sequence.argtypes = [vp, i32, vp, vp, i32, vp, vp]
             L.recon_batch_fuse_keyframe.argtypes = [vp, i32, vp, vp, i32, f32]
+            L.recon_batch_fuse_keyframe_rgbd.argtypes = [vp, i32, vp, vp, vp, i32, f32]
+            L.recon_batch_fuse_sequence.argtypes = [vp, i32, f32]
             L.recon_batch_enable_timing.argtypes = [vp, i32]
             L.recon_batch_get_timing.argtypes = [vp, vp, vp, i32]
             L.recon_batch_get_work.argtypes = [vp, vp, i32]
@@ -349,10 +351,13 @@ class Batch:
                                                ctypes.cast(stats, ctypes.c_void_p)))
         return T.reshape(nf, self.n, 4, 4), list(stats)
 
-    def fuse_keyframe(self, depths, T, gate_mm: float = 30.0):
-        """depths: nframes lists of n depth maps; T: [nframes, n, 4, 4] keyframe -> frame poses."""
+    def fuse_keyframe(self, depths, T, gate_mm: float = 30.0, grays=None):
+        """Keyframe fusion (recon_batch_fuse_keyframe_rgbd).  depths (and
+        optionally grays): nframes lists of n images; T: [nframes, n, 4, 4]
+        keyframe -> frame poses."""
         nf = len(depths)
         d = (ctypes.c_void_p * (nf * self.n))()
+        g = (ctypes.c_void_p * (nf * self.n))() if grays is not None else None
         dev = None
         keep = []
         for f in range(nf):
@@ -364,9 +369,23 @@ class Batch:
                 od = _on_device(di)
                 dev = od if dev is None else dev
                 d[f * self.n + i] = _ptr(di).value
+                if g is not None:
+                    gi = grays[f][i]
+                    if isinstance(gi, np.ndarray):
+                        gi = np.ascontiguousarray(gi, np.uint8)
+                    keep.append(gi)
+                    if _on_device(gi) != od:
+                        raise ValueError("mix of host and device inputs")
+                    g[f * self.n + i] = _ptr(gi).value
         Tn = np.ascontiguousarray(np.asarray(T, np.float32).reshape(nf * self.n, 16))
-        check(lib().recon_batch_fuse_keyframe(self.h, nf, ctypes.cast(d, ctypes.c_void_p), _ptr(Tn), int(dev or 0),
-                                              gate_mm))
+        check(lib().recon_batch_fuse_keyframe_rgbd(self.h, nf, None if g is None else ctypes.cast(g, ctypes.c_void_p),
+                                                   ctypes.cast(d, ctypes.c_void_p), _ptr(Tn), int(dev or 0), gate_mm))
+
+    def fuse_sequence(self, nframes: int, gate_mm: float = 30.0):
+        """Fuses the first nframes frames of the last tracked sequence (depth
+        and colour, tracked poses) into the keyframes, all on the device
+        (recon_batch_fuse_sequence)."""
+        check(lib().recon_batch_fuse_sequence(self.h, int(nframes), float(gate_mm)))
 
     def track_async(self, T_init=None):
         T = None if T_init is None else np.ascontiguousarray(np.asarray(T_init, np.float32).reshape(self.n, 16))
@@ -428,7 +447,7 @@ class Batch:
 
 
 TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_student_t", "prep_current", "prep_reference", "gn_solve",
-                "icp_prepare"]
+                "icp_prepare", "keyframe_fusion"]
 
 
 def launch_count() -> int:

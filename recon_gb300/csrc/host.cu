@@ -47,7 +47,7 @@ __global__ void k_clear_ref(const InstDesc *D, const int *active);
 __global__ void k_store_pose(const InstDesc *D, float *dst);
 __global__ void k_gather_results(const InstDesc *D, int *dst);
 __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const uint16_t *const *depth,
-                             const float *Tf, float gate, const int *active);
+                             const uint8_t *const *gray, const float *Tf, float gate, const int *active);
 __global__ void k_ref_from_z(const InstDesc *D, const int *active);
 __global__ void k_net_coarse(const InstDesc *D, const uint8_t *const *in_gray, const uint16_t *const *in_depth,
                              const __nv_bfloat16 *prev, __nv_bfloat16 *out, __nv_bfloat16 *net_in);
@@ -156,16 +156,21 @@ struct recon_batch {
     const void **h_seqptr = nullptr;  // pinned
     float *d_Tseq = nullptr;
     size_t Tseq_cap = 0;
-    uint8_t *d_slot[2] = {nullptr, nullptr};
-    size_t slot_bytes = 0;
+    int seq_frames = 0;  // frames of the last recon_batch_track_sequence call (their poses are in d_Tseq)
+    // host-input sequences: one device slot per frame of the call (kept after
+    // the call, so that recon_batch_fuse_sequence can read the frames)
+    uint8_t *d_slots = nullptr;
+    size_t slots_bytes = 0;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
     // keyframe fusion runs on a second stream (the reference's reconstruction GPU)
     cudaStream_t recon_stream = nullptr;
     cudaEvent_t ev_pose = nullptr, ev_fused = nullptr;
-    uint16_t *d_fuse = nullptr;
+    uint8_t *d_fuse = nullptr;
     size_t fuse_bytes = 0;
     const void **d_fuse_ptr = nullptr;
+    const void **h_fuse_ptr = nullptr;  // pinned: the fusion's pointer table
+    int *d_all_active = nullptr;        // [n] ones: the fusion updates every instance
     float *d_fuse_T = nullptr;
     size_t fuse_cap = 0;
     // host pose bookkeeping for the single-tracker API (applyIncrement)
@@ -241,6 +246,7 @@ size_t layout(InstDesc &d, char *base) {
         d.cur_grayh[l] = mixed ? a.take<__half>(nl) : nullptr;
     }
     d.ref_z = a.take<float>(n);
+    d.ref_col = a.take<float>(n);
     d.cur_z = a.take<float>(n);
     d.vtx = a.take<float>((size_t)kVtxPlanes * n);
     d.grad_hist = a.take<int>(1024);
@@ -331,7 +337,10 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
 
 dim3 grid_pix(int pix, int n, int block = 256) { return dim3((pix + block - 1) / block, n, 1); }
 
-enum TimingKind { TK_ITER = 0, TK_ICP_MASK, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_ICP_PREP, TK_COUNT };
+enum TimingKind {
+    TK_ITER = 0, TK_ICP_MASK, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_ICP_PREP, TK_FUSE, TK_COUNT
+};
+static_assert(TK_COUNT <= 8, "timing slots");
 
 // brackets one launch with a pair of events when timing is enabled; events
 // recorded during stream capture become graph nodes and are re-recorded by
@@ -391,27 +400,28 @@ void collect_events(recon_batch *b, std::vector<std::pair<int, std::pair<cudaEve
 // reference preparation; from_inputs: convert the staged images (else rebuild
 // from the current ref_z, keeping the keyframe gray); reset_pose: T <- I
 int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose = true,
-                      cudaStream_t st = nullptr) {
+                      cudaStream_t st = nullptr, const int *active_flags = nullptr) {
     cudaStream_t s = st ? st : b->stream;
     TimedScope ts(b, s, TK_PREP_REF, false);
     int n = b->n;
     auto D = b->d_desc;
     auto in = b->d_inptr;
+    const int *active = active_flags ? active_flags : b->d_active;
     if (from_inputs)
         k_convert_level0<<<grid_pix(b->max_pix, n), 256, 0, s>>>(
             D, (const uint8_t *const *)in, (const uint16_t *const *)(in + n), (const float *const *)(in + 2 * n));
     else
-        k_ref_from_z<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
-    k_normals<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
+        k_ref_from_z<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
+    k_normals<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
     for (int l = 1; l < b->max_L; l++)
-        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, b->d_active);
-    k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, b->d_active);
-    k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, b->d_active);
-    k_seg_count<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, b->d_active);
-    k_seg_scan<<<dim3(1, n), 32, 0, s>>>(D, b->d_active);
-    k_seg_scatter<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, b->d_active);
-    k_attr_jac<<<grid_pix(b->max_P, n), 256, 0, s>>>(D, b->d_active);
-    if (reset_pose) k_reset_pose<<<dim3(1, n), 32, 0, s>>>(D, b->d_active);
+        k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, active);
+    k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, active);
+    k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
+    k_seg_count<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, active);
+    k_seg_scan<<<dim3(1, n), 32, 0, s>>>(D, active);
+    k_seg_scatter<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, active);
+    k_attr_jac<<<grid_pix(b->max_P, n), 256, 0, s>>>(D, active);
+    if (reset_pose) k_reset_pose<<<dim3(1, n), 32, 0, s>>>(D, active);
     g_launches += 9 + (b->max_L - 1) + (reset_pose ? 1 : 0);
     CK(cudaGetLastError());
     return RECON_OK;
@@ -625,6 +635,59 @@ int learned_keyframe(recon_batch *b) {
     return RECON_OK;
 }
 
+// Fusion buffers (second stream, events, pointer tables for cnt frame-instance pairs).
+int fuse_prepare(recon_batch *b, size_t cnt) {
+    if (!b->recon_stream) {
+        CK(cudaStreamCreateWithFlags(&b->recon_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&b->ev_pose, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b->ev_fused, cudaEventDisableTiming));
+        std::vector<int> ones(b->n, 1);
+        CK(cudaMalloc(&b->d_all_active, b->n * sizeof(int)));
+        CK(cudaMemcpy(b->d_all_active, ones.data(), b->n * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    if (cnt > b->fuse_cap) {
+        // the previous fusion may still read the tables
+        CK(cudaStreamSynchronize(b->recon_stream));
+        if (b->d_fuse_ptr) cudaFree(b->d_fuse_ptr);
+        if (b->h_fuse_ptr) cudaFreeHost(b->h_fuse_ptr);
+        if (b->d_fuse_T) cudaFree(b->d_fuse_T);
+        b->d_fuse_ptr = nullptr;
+        b->h_fuse_ptr = nullptr;
+        b->d_fuse_T = nullptr;
+        b->fuse_cap = 0;
+        CK(cudaMalloc(&b->d_fuse_ptr, 2 * cnt * sizeof(void *)));
+        CK(cudaMallocHost(&b->h_fuse_ptr, 2 * cnt * sizeof(void *)));
+        CK(cudaMalloc(&b->d_fuse_T, cnt * 16 * sizeof(float)));
+        b->fuse_cap = cnt;
+    } else {
+        // the pinned table is rewritten by the host: the previous fusion's copy of it is done
+        CK(cudaStreamSynchronize(b->recon_stream));
+    }
+    return RECON_OK;
+}
+
+int prepare_reference(recon_batch *b, bool from_inputs, bool reset_pose, cudaStream_t st, const int *active_flags);
+
+// The fusion kernel and the reference rebuild on the second stream, reading
+// the device table d_fuse_ptr (depth, then gray) and poses Tdev; the pose
+// stream then waits for the fused keyframe.
+int fuse_launch(recon_batch *b, int nframes, bool colour, const float *Tdev, float gate_mm) {
+    int n = b->n;
+    size_t cnt = (size_t)nframes * n;
+    {
+        TimedScope ts(b, b->recon_stream, TK_FUSE, false);
+        k_fuse_depth<<<grid_pix(b->max_pix, n), 256, 0, b->recon_stream>>>(
+            b->d_desc, nframes, n, (const uint16_t *const *)b->d_fuse_ptr,
+            colour ? (const uint8_t *const *)(b->d_fuse_ptr + cnt) : nullptr, Tdev, gate_mm, b->d_all_active);
+    }
+    g_launches += 1;
+    int rc = prepare_reference(b, false, false, b->recon_stream, b->d_all_active);
+    if (rc) return rc;
+    CK(cudaEventRecord(b->ev_fused, b->recon_stream));
+    CK(cudaStreamWaitEvent(b->stream, b->ev_fused, 0));
+    return RECON_OK;
+}
+
 int upload_desc(recon_batch *b) {
     CK(cudaMemcpyAsync(b->d_desc, b->desc.data(), b->n * sizeof(InstDesc), cudaMemcpyHostToDevice, b->stream));
     CK(cudaStreamSynchronize(b->stream));
@@ -833,8 +896,8 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->d_seqptr) cudaFree(b->d_seqptr);
     if (b->h_seqptr) cudaFreeHost(b->h_seqptr);
     if (b->d_Tseq) cudaFree(b->d_Tseq);
+    if (b->d_slots) cudaFree(b->d_slots);
     for (int k = 0; k < 2; k++) {
-        if (b->d_slot[k]) cudaFree(b->d_slot[k]);
         if (b->ev_copied[k]) cudaEventDestroy(b->ev_copied[k]);
         if (b->ev_free[k]) cudaEventDestroy(b->ev_free[k]);
     }
@@ -851,7 +914,9 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->ev_fused) cudaEventDestroy(b->ev_fused);
     if (b->d_fuse) cudaFree(b->d_fuse);
     if (b->d_fuse_ptr) cudaFree(b->d_fuse_ptr);
+    if (b->h_fuse_ptr) cudaFreeHost(b->h_fuse_ptr);
     if (b->d_fuse_T) cudaFree(b->d_fuse_T);
+    if (b->d_all_active) cudaFree(b->d_all_active);
     for (auto &ev : b->graph_events) {
         cudaEventDestroy(ev.second.first);
         cudaEventDestroy(ev.second.second);
@@ -1092,6 +1157,7 @@ int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, in
     if (nm == "ref_gray") { src = d.ref_gray[level]; sz = (int64_t)W * H * 4; }
     else if (nm == "cur_gray") { src = d.cur_gray[level]; sz = (int64_t)W * H * 4; }
     else if (nm == "ref_z") { src = d.ref_z; sz = (int64_t)n0 * 4; }
+    else if (nm == "ref_col") { src = d.ref_col; sz = (int64_t)n0 * 4; }
     else if (nm == "cur_z") { src = d.cur_z; sz = (int64_t)n0 * 4; }
     else if (nm == "ref_pts") { src = d.ref_pts[level]; sz = (int64_t)W * H * 16; }
     else if (nm == "ref_nrm") { src = d.ref_nrm[level]; sz = (int64_t)W * H * 16; }
@@ -1159,8 +1225,19 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     int n = b->n;
     for (size_t k = 0; k < (size_t)nf * n; k++)
         if (!gray[k] || !depth[k]) return fail(RECON_ERR_INVALID_ARG, "null frame pointer");
-    size_t rows = on_device ? (size_t)nf : 2;
-    size_t need_ptr = rows * 3 * n;
+    size_t need_ptr = (size_t)nf * 3 * n;
+    size_t need_T = (size_t)nf * n * 16;
+    std::vector<size_t> px(n);
+    size_t frame_bytes = 0;
+    for (int i = 0; i < n; i++) {
+        px[i] = (size_t)b->cfg[i].width * b->cfg[i].height;
+        frame_bytes += align256(px[i]) + align256(2 * px[i]);
+    }
+    // a keyframe fusion may still read the last sequence's poses and slots:
+    // let it finish before any buffer is reallocated
+    if (b->recon_stream && (need_ptr > b->seqptr_cap || need_T > b->Tseq_cap ||
+                            (!on_device && frame_bytes * nf > b->slots_bytes)))
+        CK(cudaStreamSynchronize(b->recon_stream));
     if (need_ptr > b->seqptr_cap) {
         if (b->d_seqptr) cudaFree(b->d_seqptr);
         if (b->h_seqptr) cudaFreeHost(b->h_seqptr);
@@ -1171,7 +1248,6 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         CK(cudaMallocHost(&b->h_seqptr, need_ptr * sizeof(void *)));
         b->seqptr_cap = need_ptr;
     }
-    size_t need_T = (size_t)nf * n * 16;
     if (need_T > b->Tseq_cap) {
         if (b->d_Tseq) cudaFree(b->d_Tseq);
         b->d_Tseq = nullptr;
@@ -1179,36 +1255,33 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         CK(cudaMalloc(&b->d_Tseq, need_T * sizeof(float)));
         b->Tseq_cap = need_T;
     }
-    std::vector<size_t> px(n);
-    size_t frame_bytes = 0;
-    for (int i = 0; i < n; i++) {
-        px[i] = (size_t)b->cfg[i].width * b->cfg[i].height;
-        frame_bytes += align256(px[i]) + align256(2 * px[i]);
-    }
+    b->seq_frames = 0;
     if (!on_device) {
-        if (frame_bytes > b->slot_bytes) {
-            for (int k = 0; k < 2; k++) {
-                if (b->d_slot[k]) cudaFree(b->d_slot[k]);
-                b->d_slot[k] = nullptr;
-            }
-            b->slot_bytes = 0;
-            for (int k = 0; k < 2; k++) CK(cudaMalloc(&b->d_slot[k], frame_bytes));
-            b->slot_bytes = frame_bytes;
+        if (frame_bytes * nf > b->slots_bytes) {
+            if (b->d_slots) cudaFree(b->d_slots);
+            b->d_slots = nullptr;
+            b->slots_bytes = 0;
+            CK(cudaMalloc(&b->d_slots, frame_bytes * nf));
+            b->slots_bytes = frame_bytes * nf;
         }
         if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
         for (int k = 0; k < 2; k++) {
             if (!b->ev_copied[k]) CK(cudaEventCreateWithFlags(&b->ev_copied[k], cudaEventDisableTiming));
             if (!b->ev_free[k]) CK(cudaEventCreateWithFlags(&b->ev_free[k], cudaEventDisableTiming));
         }
-        // the two staging slots are the only two rows of the pointer table
-        for (int k = 0; k < 2; k++) {
-            size_t off = 0;
+        // work already queued on the batch stream (a keyframe fusion reading the
+        // previous call's slots) ends before the copies into the slots begin
+        CK(cudaEventRecord(b->ev_free[0], b->stream));
+        CK(cudaStreamWaitEvent(b->copy_stream, b->ev_free[0], 0));
+        // frame f is copied into slot f, the only source of row f of the pointer table
+        for (int f = 0; f < nf; f++) {
+            size_t off = frame_bytes * f;
             for (int i = 0; i < n; i++) {
-                b->h_seqptr[(size_t)k * 3 * n + i] = b->d_slot[k] + off;
+                b->h_seqptr[(size_t)f * 3 * n + i] = b->d_slots + off;
                 off += align256(px[i]);
-                b->h_seqptr[(size_t)k * 3 * n + n + i] = b->d_slot[k] + off;
+                b->h_seqptr[(size_t)f * 3 * n + n + i] = b->d_slots + off;
                 off += align256(2 * px[i]);
-                b->h_seqptr[(size_t)k * 3 * n + 2 * n + i] = nullptr;
+                b->h_seqptr[(size_t)f * 3 * n + 2 * n + i] = nullptr;
             }
         }
     } else {
@@ -1220,27 +1293,20 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
             }
     }
     CK(cudaMemcpyAsync(b->d_seqptr, b->h_seqptr, need_ptr * sizeof(void *), cudaMemcpyHostToDevice, b->stream));
-    if (!on_device) {
-        // the previous call's last kernels may still read the slots
-        CK(cudaEventRecord(b->ev_free[0], b->stream));
-        CK(cudaEventRecord(b->ev_free[1], b->stream));
-    }
-    // the input row of frame f (staged frames alternate between two slots)
-    auto row_of = [&](int f) -> const void ** {
-        return b->d_seqptr + (size_t)(on_device ? f : (f & 1)) * 3 * n;
-    };
-    // copy frame f into slot f & 1 once the frame that used it (f - 2) is done
+    // the input row of frame f
+    auto row_of = [&](int f) -> const void ** { return b->d_seqptr + (size_t)f * 3 * n; };
+    // copy frame f into its slot on the copy stream (ev_copied[f & 1] marks it;
+    // frame f's copies are issued after frame f - 1's, so the event recorded
+    // later on the same stream also covers the earlier frames)
     auto stage = [&](int f) -> int {
         if (on_device) return RECON_OK;
-        int k = f & 1;
-        CK(cudaStreamWaitEvent(b->copy_stream, b->ev_free[k], 0));
         for (int i = 0; i < n; i++) {
-            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + i], gray[(size_t)f * n + i], px[i],
+            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + i], gray[(size_t)f * n + i], px[i],
                                cudaMemcpyHostToDevice, b->copy_stream));
-            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)k * 3 * n + n + i], depth[(size_t)f * n + i],
+            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + n + i], depth[(size_t)f * n + i],
                                2 * px[i], cudaMemcpyHostToDevice, b->copy_stream));
         }
-        CK(cudaEventRecord(b->ev_copied[k], b->copy_stream));
+        CK(cudaEventRecord(b->ev_copied[f & 1], b->copy_stream));
         return RECON_OK;
     };
     // The network input of a frame is two images, not a pose, so the network
@@ -1286,9 +1352,6 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
             if (rc) return rc;
             CK(cudaEventRecord(b->ev_gate[f & 1], b->stream));
         }
-        // every reader of this frame's staged inputs has been issued (the
-        // network's coarse image read it before ev_net, which the gate waited for)
-        if (!on_device) CK(cudaEventRecord(b->ev_free[f & 1], b->stream));
         rc = run_schedule(b);
         if (rc) return rc;
         CK(cudaGetLastError());
@@ -1297,6 +1360,7 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     k_store_pose<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tseq + (size_t)(nf - 1) * n * 16);
     g_launches += 1;
     b->have_cur = true;
+    b->seq_frames = nf;
     if (T_out) CK(cudaMemcpyAsync(T_out, b->d_Tseq, need_T * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
     return recon_batch_get_poses(b, nullptr, stats);
 }
@@ -1377,39 +1441,56 @@ int recon_batch_get_init(recon_batch *b, int32_t *choice, float *net_out) {
 
 int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *const *depth, const float *T_host,
                               int32_t on_device, float gate_mm) {
+    return recon_batch_fuse_keyframe_rgbd(b, nframes, nullptr, depth, T_host, on_device, gate_mm);
+}
+
+int recon_batch_fuse_sequence(recon_batch *b, int32_t nframes, float gate_mm) {
     clear_stale_error();
-    if (!b || nframes < 1 || nframes > 8 || !depth || !T_host || !(gate_mm > 0.0f))
+    if (!b || nframes < 1 || nframes > 8 || !(gate_mm > 0.0f))
         return fail(RECON_ERR_INVALID_ARG, "bad argument (1..8 frames, positive gate)");
+    if (!b->have_ref) return fail(RECON_ERR_STATE, "reference frame missing");
+    if (nframes > b->seq_frames) return fail(RECON_ERR_STATE, "the last sequence has fewer frames");
+    int rc = fuse_prepare(b, (size_t)nframes * b->n);
+    if (rc) return rc;
+    int n = b->n;
+    size_t cnt = (size_t)nframes * n;
+    // depth pointers [cnt], then gray pointers [cnt], from the sequence's rows
+    for (int f = 0; f < nframes; f++)
+        for (int i = 0; i < n; i++) {
+            size_t k = (size_t)f * n + i;
+            b->h_fuse_ptr[k] = b->h_seqptr[(size_t)f * 3 * n + n + i];
+            b->h_fuse_ptr[cnt + k] = b->h_seqptr[(size_t)f * 3 * n + i];
+        }
+    CK(cudaEventRecord(b->ev_pose, b->stream));
+    CK(cudaStreamWaitEvent(b->recon_stream, b->ev_pose, 0));
+    CK(cudaMemcpyAsync(b->d_fuse_ptr, b->h_fuse_ptr, 2 * cnt * sizeof(void *), cudaMemcpyHostToDevice,
+                       b->recon_stream));
+    return fuse_launch(b, nframes, true, b->d_Tseq, gate_mm);
+}
+
+int recon_batch_fuse_keyframe_rgbd(recon_batch *b, int32_t nframes, const uint8_t *const *gray,
+                                   const uint16_t *const *depth, const float *T, int32_t on_device, float gate_mm) {
+    clear_stale_error();
+    if (!b || nframes < 1 || nframes > 8 || !depth || !T || !(gate_mm > 0.0f))
+        return fail(RECON_ERR_INVALID_ARG, "bad argument (1..8 frames, poses, positive gate)");
     if (!b->have_ref) return fail(RECON_ERR_STATE, "reference frame missing");
     int n = b->n;
     size_t cnt = (size_t)nframes * n;
     for (size_t k = 0; k < cnt; k++)
-        if (!depth[k]) return fail(RECON_ERR_INVALID_ARG, "null depth pointer");
-    if (!b->recon_stream) {
-        CK(cudaStreamCreateWithFlags(&b->recon_stream, cudaStreamNonBlocking));
-        CK(cudaEventCreateWithFlags(&b->ev_pose, cudaEventDisableTiming));
-        CK(cudaEventCreateWithFlags(&b->ev_fused, cudaEventDisableTiming));
-    }
-    if (cnt > b->fuse_cap) {
-        if (b->d_fuse_ptr) cudaFree(b->d_fuse_ptr);
-        if (b->d_fuse_T) cudaFree(b->d_fuse_T);
-        b->d_fuse_ptr = nullptr;
-        b->d_fuse_T = nullptr;
-        b->fuse_cap = 0;
-        CK(cudaMalloc(&b->d_fuse_ptr, cnt * sizeof(void *)));
-        CK(cudaMalloc(&b->d_fuse_T, cnt * 16 * sizeof(float)));
-        b->fuse_cap = cnt;
-    }
-    std::vector<const void *> ptrs(cnt);
+        if (!depth[k] || (gray && !gray[k])) return fail(RECON_ERR_INVALID_ARG, "null frame pointer");
+    int rc = fuse_prepare(b, cnt);
+    if (rc) return rc;
     std::vector<size_t> px(n);
     size_t bytes = 0;
     for (int i = 0; i < n; i++) {
         px[i] = (size_t)b->cfg[i].width * b->cfg[i].height;
-        bytes += (size_t)nframes * align256(2 * px[i]);
+        bytes += (size_t)nframes * (align256(2 * px[i]) + (gray ? align256(px[i]) : 0));
     }
     // the fusion waits for the pose stream's pending work (tracked frames)
     CK(cudaEventRecord(b->ev_pose, b->stream));
     CK(cudaStreamWaitEvent(b->recon_stream, b->ev_pose, 0));
+    // pointer table: depth pointers [cnt], then gray pointers [cnt]
+    for (size_t k = 0; k < 2 * cnt; k++) b->h_fuse_ptr[k] = nullptr;
     if (!on_device) {
         if (bytes > b->fuse_bytes) {
             if (b->d_fuse) cudaFree(b->d_fuse);
@@ -1421,28 +1502,30 @@ int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *c
         size_t off = 0;
         for (int f = 0; f < nframes; f++)
             for (int i = 0; i < n; i++) {
-                uint8_t *dst = (uint8_t *)b->d_fuse + off;
-                CK(cudaMemcpyAsync(dst, depth[(size_t)f * n + i], 2 * px[i], cudaMemcpyHostToDevice,
-                                   b->recon_stream));
-                ptrs[(size_t)f * n + i] = dst;
+                size_t k = (size_t)f * n + i;
+                uint8_t *dst = b->d_fuse + off;
+                CK(cudaMemcpyAsync(dst, depth[k], 2 * px[i], cudaMemcpyHostToDevice, b->recon_stream));
+                b->h_fuse_ptr[k] = dst;
                 off += align256(2 * px[i]);
+                if (gray) {
+                    dst = b->d_fuse + off;
+                    CK(cudaMemcpyAsync(dst, gray[k], px[i], cudaMemcpyHostToDevice, b->recon_stream));
+                    b->h_fuse_ptr[cnt + k] = dst;
+                    off += align256(px[i]);
+                }
             }
     } else {
-        for (size_t k = 0; k < cnt; k++) ptrs[k] = depth[k];
+        for (size_t k = 0; k < cnt; k++) {
+            b->h_fuse_ptr[k] = depth[k];
+            if (gray) b->h_fuse_ptr[cnt + k] = gray[k];
+        }
     }
-    std::vector<int> ones(n, 1);
-    CK(cudaMemcpyAsync(b->d_fuse_ptr, ptrs.data(), cnt * sizeof(void *), cudaMemcpyHostToDevice, b->recon_stream));
-    CK(cudaMemcpyAsync(b->d_fuse_T, T_host, cnt * 16 * sizeof(float), cudaMemcpyHostToDevice, b->recon_stream));
-    CK(cudaMemcpyAsync(b->d_active, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->recon_stream));
-    k_fuse_depth<<<grid_pix(b->max_pix, n), 256, 0, b->recon_stream>>>(
-        b->d_desc, nframes, n, (const uint16_t *const *)b->d_fuse_ptr, b->d_fuse_T, gate_mm, b->d_active);
-    g_launches += 1;
-    int rc = prepare_reference(b, false, false, b->recon_stream);
+    CK(cudaMemcpyAsync(b->d_fuse_ptr, b->h_fuse_ptr, 2 * cnt * sizeof(void *), cudaMemcpyHostToDevice,
+                       b->recon_stream));
+    CK(cudaMemcpyAsync(b->d_fuse_T, T, cnt * 16 * sizeof(float), cudaMemcpyHostToDevice, b->recon_stream));
+    rc = fuse_launch(b, nframes, gray != nullptr, b->d_fuse_T, gate_mm);
     if (rc) return rc;
-    // the pose stream continues with the fused reference
-    CK(cudaEventRecord(b->ev_fused, b->recon_stream));
-    CK(cudaStreamWaitEvent(b->stream, b->ev_fused, 0));
-    // pageable sources (ptrs, ones, T_host) must outlive the copies
+    // pageable sources (the frames, T) must outlive the copies
     CK(cudaStreamSynchronize(b->recon_stream));
     return RECON_OK;
 }

@@ -72,6 +72,7 @@ __global__ void k_convert_level0(const InstDesc *D, const uint8_t *const *in_gra
     float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
     d.ref_gray[0][i] = g;
     d.ref_z[i] = z;
+    d.ref_col[i] = -1.0f;  // a new keyframe has no fused colour
     float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
     float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
     if (z < -minDist && z > -maxDist) {
@@ -271,16 +272,40 @@ __global__ void k_downsample(const InstDesc *D, int level, const int *active) {
     }
 }
 
-// Keyframe depth fusion (the oracle's orc_fuse_depth restates the same steps):
-// every valid keyframe pixel is back-projected with KL (rgb2gray.cu:570-593),
-// mapped into frame f by its tracked pose, looked up at the nearest IR pixel
-// (the zWeight tap of warp.cu:306-327), mapped back with the inverse pose (as
-// filterDepthIIRKernel does, warp.cu:398-467), gated on |dz| < gate and averaged
-// with unit weights (the running mean of updateVoxelsKernel,
-// VoxelGrid_cuda.cu:1005-1013).  Writes the fused depth in place into ref_z.
-// depth: nframes x n_inst frame pointers; Tf: nframes x n_inst x 16 poses.
+// Gray value the RGB camera sees at point (qx, qy, qz) of its rig's IR frame
+// (TLR, distortPoint and the bilinear color1 tap of xyz2CloudKernel,
+// d2z.cu:235-331), from a float image or a uint8 image scaled by 1/255; -1
+// where the 2x2 taps leave the image.
+template <typename TImg>
+__device__ __forceinline__ float rgb_sample(const float *calib, float qx, float qy, float qz, const TImg *img, int W,
+                                            int H) {
+    float rx, ry, rz;
+    mul4(calib + RC_TLR, qx, qy, qz, rx, ry, rz);
+    float pux = rx / rz, puy = ry / rz;
+    float px, py;
+    distort(pux, puy, calib + RC_KCR, calib + RC_KR, px, py);
+    int xdi = ftoi(px), ydi = ftoi(py);
+    if (!(xdi >= 0 && ydi >= 0 && xdi < W - 1 && ydi < H - 1)) return -1.0f;
+    float fx = px - xdi, fy = py - ydi;
+    return bilin(xdi, ydi, fx, fy, W, img);
+}
+
+// Keyframe depth and colour fusion (the oracle's orc_fuse_rgbd restates the
+// same steps): every valid keyframe pixel is back-projected with KL
+// (rgb2gray.cu:570-593), mapped into frame f by its tracked pose, looked up at
+// the nearest IR pixel (the zWeight tap of warp.cu:306-327), mapped back with
+// the inverse pose (as filterDepthIIRKernel does, warp.cu:398-467), gated on
+// |dz| < gate and averaged with unit weights (the running mean of
+// updateVoxelsKernel, VoxelGrid_cuda.cu:1005-1013).  With gray images the
+// vertex colour is fused under the same gate: the mean of the keyframe's own
+// sample at the point and the accepted frames' samples at T_f p
+// (KeyFrameModel::integrateDepthMaps warps the neighbours' RGB images into the
+// keyframe, KeyFrameModel.cpp:537-583).  Writes the fused depth in place into
+// ref_z and the colour into ref_col (-1 where no sample exists).
+// depth / gray: nframes x n_inst frame pointers (gray may be null: depth only,
+// colours kept); Tf: nframes x n_inst x 16 poses.
 __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const uint16_t *const *depth,
-                             const float *Tf, float gate, const int *active) {
+                             const uint8_t *const *gray, const float *Tf, float gate, const int *active) {
     INST_DESC;
     if (!active[blockIdx.y]) return;
     __shared__ float sT[8][16], sTi[8][16];
@@ -303,9 +328,21 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
     float fx = KL[0], fy = KL[4], cx = KL[2], cy = KL[5];
     int xi = idx % W, yi = idx / W;
     float z = d.ref_z[idx];
-    if (!(z < -minDist && z > -maxDist)) return;
+    const bool colour = gray != nullptr;
+    if (!(z < -minDist && z > -maxDist)) {
+        if (colour) d.ref_col[idx] = -1.0f;
+        return;
+    }
     float px3 = ((float)xi - cx) * z / fx, py3 = ((float)yi - cy) * z / fy, pz3 = z;
     float zsum = z, wsum = 1.0f;
+    float csum = 0.0f, cw = 0.0f;
+    if (colour) {
+        float c0 = rgb_sample(d.calib, px3, py3, pz3, d.ref_gray[0], W, H);
+        if (c0 >= 0.0f) {
+            csum = c0;
+            cw = 1.0f;
+        }
+    }
     for (int f = 0; f < nframes && f < 8; f++) {
         float qx, qy, qz;
         mul4(sT[f], px3, py3, pz3, qx, qy, qz);
@@ -324,9 +361,17 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
         if (fabsf(dz) < gate) {
             zsum += kz;
             wsum += 1.0f;
+            if (colour) {
+                float c = rgb_sample(d.calib, qx, qy, qz, gray[(size_t)f * n_inst + blockIdx.y], W, H);
+                if (c >= 0.0f) {
+                    csum += c;
+                    cw += 1.0f;
+                }
+            }
         }
     }
     d.ref_z[idx] = zsum / wsum;
+    if (colour) d.ref_col[idx] = cw > 0.0f ? csum / cw : -1.0f;
 }
 
 // reference level-0 points from ref_z (convertZMapToXYZ6Kernel, rgb2gray.cu:595-624)
@@ -420,6 +465,8 @@ __global__ void k_xyz2cloud(const InstDesc *D, const int *active) {
                 int xdi = ftoi(px), ydi = ftoi(py);
                 float fx = px - xdi, fy = py - ydi;
                 float color1 = bilin(xdi, ydi, fx, fy, W, img);
+                float fused = d.ref_col[i];  // the keyframe fusion's vertex colour, if any
+                if (fused >= 0.0f) color1 = fused;
                 float colorN = bilin(ftoi(px), ftoi(py - 1.0f), fx, fy, W, img);
                 float colorE = bilin(ftoi(px + 1.0f), ftoi(py), fx, fy, W, img);
                 float colorW = bilin(ftoi(px - 1.0f), ftoi(py), fx, fy, W, img);

@@ -35,6 +35,7 @@ struct InstDesc {
     // reference (keyframe)
     float *ref_gray[kMaxLevels];
     float *ref_z;
+    float *ref_col;               // W*H fused vertex colour (keyframe fusion), -1 where none
     float4 *ref_pts[kMaxLevels];  // x y z mask
     float4 *ref_nrm[kMaxLevels];  // nx ny nz 0
     float *vtx;                   // kVtxPlanes planes of W*H

@@ -64,6 +64,8 @@ __device__ __forceinline__ void distort(float pux, float puy, const float *kc, c
 __device__ __forceinline__ float ldf(const float *p) { return __ldg(p); }
 __device__ __forceinline__ float ldf(const __half *p) { return __half2float(__ldg(p)); }
 __device__ __forceinline__ float ldf(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
+// a uint8 gray value in [0, 1] (the input conversion's (float)g / 255)
+__device__ __forceinline__ float ldf(const uint8_t *p) { return (float)__ldg(p) / 255.0f; }
 
 // bilinearInterpolation(int,int,float,float,...), kernelUtils.h:298-303
 template <typename TImg>

@@ -46,7 +46,8 @@ class OrcIterTrace(ctypes.Structure):
 
 
 def _build() -> None:
-    src = [os.path.join(ORACLE_DIR, f) for f in ("oracle.c", "oracle.h", "initnet_oracle.c", "Makefile")]
+    src = [os.path.join(ORACLE_DIR, f) for f in ("oracle.c", "oracle_fp64.c", "oracle.h", "initnet_oracle.c",
+                                                 "Makefile")]
     src.append(os.path.join(ROOT, "recon_gb300", "csrc", "scene.h"))
     if os.path.exists(LIB_PATH) and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in src):
         return
@@ -121,6 +122,19 @@ def lib() -> ctypes.CDLL:
             L.orc_convert_depth.argtypes = [vp, i32, vp]
             L.orc_rgbd_float4_to_gray_z.argtypes = [vp, i32, i32, vp, vp, vp]
             L.orc_fuse_keyframe.argtypes = [vp, i32, vp, vp, f32]
+            L.orc_fuse_keyframe_rgbd.argtypes = [vp, i32, vp, vp, vp, f32]
+            L.orc64_create.restype = vp
+            L.orc64_create.argtypes = [ctypes.POINTER(OrcConfig), vp]
+            L.orc64_destroy.argtypes = [vp]
+            L.orc64_set_reference.argtypes = [vp, vp, vp]
+            L.orc64_set_current.argtypes = [vp, vp, vp]
+            L.orc64_fuse_keyframe.argtypes = [vp, i32, vp, vp, vp, ctypes.c_double]
+            L.orc64_track.argtypes = [vp, vp]
+            L.orc64_get_pose.argtypes = [vp, vp]
+            L.orc64_set_pose.argtypes = [vp, vp]
+            L.orc64_get_array.argtypes = [vp, ctypes.c_char_p, i32, vp, ctypes.c_int64]
+            L.orc_fuse_rgbd.argtypes = [vp, vp, i32, i32, vp, i32, vp, vp, vp, f32, vp, vp, vp]
+            L.orc_xyz2cloud_col.argtypes = [vp, i32, i32, vp, vp, vp, vp]
             L.orc_init_gate.argtypes = [vp, vp, vp]
             L.orc_init_gate.restype = i32
             L.orc_set_pose.argtypes = [vp, vp]
@@ -209,10 +223,15 @@ class OracleTracker:
         sc = np.ascontiguousarray(scale, np.float32)
         return int(self.L.orc_init_gate(self.h, ptr(y), ptr(sc)))
 
-    def fuse_keyframe(self, depths, Ts, gate: float = 30.0):
+    def fuse_keyframe(self, depths, Ts, gate: float = 30.0, grays=None):
+        """Keyframe fusion of depth (and, with grays, colour) of tracked frames."""
         ds = [np.ascontiguousarray(d, np.uint16) for d in depths]
         T = np.ascontiguousarray(np.asarray(Ts, np.float32).reshape(len(ds), 16))
-        rc = self.L.orc_fuse_keyframe(self.h, len(ds), ptrs(ds), ptr(T), gate)
+        if grays is None:
+            rc = self.L.orc_fuse_keyframe(self.h, len(ds), ptrs(ds), ptr(T), gate)
+        else:
+            gs = [np.ascontiguousarray(g, np.uint8) for g in grays]
+            rc = self.L.orc_fuse_keyframe_rgbd(self.h, len(ds), ptrs(gs), ptrs(ds), ptr(T), gate)
         if rc != 0:
             raise RuntimeError("oracle fuse failed")
 
@@ -222,6 +241,64 @@ class OracleTracker:
         if n < 0:
             raise KeyError(name)
         return out.reshape(-1)[: n // out.itemsize].reshape(-1)
+
+
+class Oracle64Tracker:
+    """The FP64 oracle (orc64_*): the same tracker with every operation in
+    double and the pose kept in double; the judge of pose error."""
+
+    def __init__(self, cfg: OrcConfig, calib: np.ndarray):
+        self.L = lib()
+        self._calib = np.ascontiguousarray(calib, np.float32).reshape(96)
+        self.h = self.L.orc64_create(ctypes.byref(cfg), ptr(self._calib))
+        self.W, self.H, self.P = cfg.width, cfg.height, cfg.n_select
+
+    def close(self):
+        if self.h:
+            self.L.orc64_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_reference(self, gray, depth):
+        g = np.ascontiguousarray(gray, np.uint8)
+        d = np.ascontiguousarray(depth, np.uint16)
+        self.L.orc64_set_reference(self.h, ptr(g), ptr(d))
+
+    def set_current(self, gray, depth):
+        g = np.ascontiguousarray(gray, np.uint8)
+        d = np.ascontiguousarray(depth, np.uint16)
+        self.L.orc64_set_current(self.h, ptr(g), ptr(d))
+
+    def track(self, T=None) -> np.ndarray:
+        """The plain schedule from T (None: the tracker's pose); the FP64 pose."""
+        Tio = np.empty(16, np.float64)
+        if T is None:
+            self.L.orc64_get_pose(self.h, ptr(Tio))
+        else:
+            Tio[:] = np.asarray(T, np.float64).reshape(16)
+        if self.L.orc64_track(self.h, ptr(Tio)) < 0:
+            raise RuntimeError("oracle64 track failed")
+        return Tio.reshape(4, 4)
+
+    def fuse_keyframe(self, depths, Ts, gate: float = 30.0, grays=None):
+        ds = [np.ascontiguousarray(d, np.uint16) for d in depths]
+        T = np.ascontiguousarray(np.asarray(Ts, np.float64).reshape(len(ds), 16))
+        gs = None if grays is None else [np.ascontiguousarray(g, np.uint8) for g in grays]
+        gp = None if gs is None else ptrs(gs)
+        if self.L.orc64_fuse_keyframe(self.h, len(ds), gp, ptrs(ds), ptr(T), gate) != 0:
+            raise RuntimeError("oracle64 fuse failed")
+
+    def get(self, name: str, level: int, count: int, dtype) -> np.ndarray:
+        out = np.zeros(count, dtype=dtype)
+        n = self.L.orc64_get_array(self.h, name.encode(), level, ptr(out), out.nbytes)
+        if n < 0:
+            raise KeyError(name)
+        return out[: n // out.itemsize]
 
 
 def render_pair(scene, cam_ir, cam_rgb, noise_rel=0.01, noise_seed=1, frame=0):

@@ -1,7 +1,8 @@
 """Host logic of the benchmark step: the frame plan of one step (every
-segment's keyframe, then frame s of every segment per sequence position) and
-the scatter of the tracked poses back to frame order.  A recording stand-in
-for the batch checks the indices handed to the frame-stack calls; no GPU."""
+segment's keyframe, then frame s of every segment per sequence position), the
+keyframe fusion between the two halves of each segment, and the scatter of the
+tracked poses back to frame order.  A recording stand-in for the batch checks
+the indices handed to the frame-stack calls; no GPU."""
 import os
 import sys
 
@@ -25,7 +26,12 @@ class RecordingBatch:
         self.calls.append(("seq", idx.copy()))
         # pose of frame f: a matrix filled with f, so the scatter is visible
         T = np.broadcast_to(idx[:, :, None, None].astype(np.float32), idx.shape + (4, 4)).copy()
+        self.last_frames = idx.shape[0]
         return T, []
+
+    def fuse_sequence(self, nframes, gate_mm):
+        assert nframes <= self.last_frames
+        self.calls.append(("fuse", nframes, gate_mm))
 
 
 def test_plan_of_the_benchmark_trajectory():
@@ -54,9 +60,12 @@ def test_run_step_scatters_every_tracked_frame_once():
     b = RecordingBatch()
     out = np.full((26, 4, 4), -1.0, np.float32)
     bench.run_step(b, plan, None, None, out)
-    assert [c[0] for c in b.calls] == ["ref", "seq"]
+    assert [c[0] for c in b.calls] == ["ref", "seq", "fuse", "seq"]
     assert b.calls[0][1].tolist() == [0, 10, 20]
-    assert np.array_equal(b.calls[1][1], plan[1])
+    # the first five frames of every segment, their fusion, then the rest
+    assert np.array_equal(b.calls[1][1], plan[1][:bench.FUSE_FRAMES])
+    assert b.calls[2] == ("fuse", bench.FUSE_FRAMES, bench.GATE_MM)
+    assert np.array_equal(b.calls[3][1], plan[1][bench.FUSE_FRAMES:])
     tracked = [f for _, fr in segs for f in fr]
     for f in range(26):
         if f in tracked:

@@ -303,6 +303,60 @@ def test_keyframe_fusion_matches_oracle():
         assert_bitexact(T6[f - 6, 0], To, f"frame {f} after fusion")
 
 
+def test_keyframe_rgbd_fusion_matches_oracle():
+    """Depth and colour fusion of the frames of the tracked sequence with their
+    poses, all taken on the device (no copy, no host round trip; here the
+    library's device copies of host frames): the fused depth, the fused vertex
+    colours, the rebuilt selection and intensities, and the poses of the
+    frames tracked against the fused keyframe equal the oracle's."""
+    W, H = 320, 240
+    cal, poses, g, d = _trajectory_frames(W, H, 8, seed=83)
+    cfg = rg.make_config(W, H, 3, mode=rg.BIOBJECTIVE, iters=(2, 3, 4))
+    b = rg.Batch([cfg], [cal.calib])
+    b.set_reference([g[0]], [d[0]])
+    assert np.all(b.get_array(0, "ref_col", 0, np.float32, W * H) == -1.0), "a new keyframe has no fused colour"
+    T, _ = b.track_sequence([[g[f]] for f in range(1, 6)], [[d[f]] for f in range(1, 6)])
+    with pytest.raises(rg.ReconError):
+        b.fuse_sequence(6)  # the sequence had five frames
+    b.fuse_sequence(5, gate_mm=30.0)
+    T6, _ = b.track_sequence([[g[6]], [g[7]]], [[d[6]], [d[7]]])
+    orc = O.OracleTracker(O.make_config(W, H, 3, mode=O.BIOBJECTIVE, iters=(2, 3, 4)), cal.calib)
+    orc.set_reference(g[0], d[0])
+    To, Ts = None, []
+    for f in range(1, 6):
+        orc.set_current(g[f], d[f])
+        To, _ = orc.track(To)
+        Ts.append(To.copy())
+    orc.fuse_keyframe([d[f] for f in range(1, 6)], np.stack(Ts), gate=30.0, grays=[g[f] for f in range(1, 6)])
+    assert_bitexact(b.get_array(0, "ref_z", 0, np.float32, W * H), orc.get("ref_z", 0, W * H, np.float32),
+                    "fused keyframe depth")
+    col = b.get_array(0, "ref_col", 0, np.float32, W * H)
+    assert_bitexact(col, orc.get("ref_col", 0, W * H, np.float32), "fused vertex colour")
+    assert (col >= 0).mean() > 0.5, "most valid pixels have a fused colour"
+    P = 8192
+    assert_bitexact(b.get_array(0, "sel_idx", 0, np.int32, P), orc.get("sel_idx", 0, P, np.int32),
+                    "selection after fusion")
+    assert_bitexact(b.get_array(0, "sel_I", 0, np.float32, P), orc.get("sel_I", 0, P, np.float32),
+                    "level-0 reference intensities (fused colours)")
+    for f in (6, 7):
+        orc.set_current(g[f], d[f])
+        To, _ = orc.track(To)
+        assert_bitexact(T6[f - 6, 0], To, f"frame {f} after fusion")
+    # a new keyframe clears the fused colours
+    b.set_reference([g[6]], [d[6]])
+    assert np.all(b.get_array(0, "ref_col", 0, np.float32, W * H) == -1.0)
+    # the caller's device frames give the same fused keyframe and poses
+    gd = [torch.from_numpy(x).cuda() for x in g]
+    dd = [torch.from_numpy(x.view(np.int16)).cuda() for x in d]
+    b2 = rg.Batch([cfg], [cal.calib])
+    b2.set_reference([gd[0]], [dd[0]])
+    T2, _ = b2.track_sequence([[gd[f]] for f in range(1, 6)], [[dd[f]] for f in range(1, 6)])
+    b2.fuse_sequence(5, gate_mm=30.0)
+    T26, _ = b2.track_sequence([[gd[6]], [gd[7]]], [[dd[6]], [dd[7]]])
+    assert_bitexact(b2.get_array(0, "ref_col", 0, np.float32, W * H), col, "fused colour, device frames")
+    assert_bitexact(T26, T6, "poses after fusion, device frames")
+
+
 def test_batch_with_uneven_resolutions_matches_oracle_per_iteration():
     """A batch whose launches are sized by its largest instance: every smaller
     instance must still match the oracle at every iteration (per-instance
