@@ -272,12 +272,31 @@ int recon_set_current(recon_tracker *t, const uint8_t *gray, const uint16_t *dep
 int recon_track(recon_tracker *t, float T_io[16], recon_track_stats *stats);
 int recon_set_iterations(recon_tracker *t, const int32_t iters[RECON_MAX_LEVELS]);
 int recon_set_mode(recon_tracker *t, int32_t mode, float lambda);
-/* getRelativePose / getGlobalPose / resetTracking (phototracker.cpp:223-262):
- * the global pose accumulates T^-1 increments in double (applyIncrement,
- * phototracker.cpp:514-531). */
+/* getRelativePose / getGlobalPose / resetTracking (phototracker.cpp:223-262).
+ * After each recon_track the host pose bookkeeping follows applyIncrement
+ * (phototracker.cpp:514-531): the relative pose T is the tracked pose
+ * inverted in double and stored as float (current -> reference), the
+ * increment inv(double(T_previous)) * inv(double(T_tracked)) is accumulated
+ * into the double global pose.  A new reference resets T to the identity and
+ * keeps the global pose; recon_reset clears both. */
 int recon_get_relative_pose(recon_tracker *t, float T[16]);
 int recon_get_global_pose(recon_tracker *t, double T[16]);
 int recon_reset(recon_tracker *t);
+
+/* Keyframe trigger (setReferenceUpdating, poseDifferenceExceeded,
+ * referenceOutdated; phototracker.cpp:62-68, 268-296, thresholds 125 mm /
+ * 12.5 deg at phototracker.cpp:127-128).  recon_pose_difference_exceeded: 1
+ * when the translation of dT is longer than dist_mm or its rotation angle
+ * (from the unit quaternion) exceeds angle_deg, else 0.
+ * recon_reference_outdated: 1 when the tracker has no reference, or when
+ * reference updating is on and its relative pose exceeds the thresholds (the
+ * caller then sets a new reference), else 0.  The batch form tests every
+ * instance's tracked pose (inverted in double, stored as float, as the
+ * reference tests its host pose) into outdated[n]. */
+int recon_pose_difference_exceeded(const float dT[16], float dist_mm, float angle_deg);
+int recon_set_reference_updating(recon_tracker *t, int32_t on, float dist_mm, float angle_deg);
+int recon_reference_outdated(recon_tracker *t);
+int recon_batch_reference_outdated(recon_batch *b, float dist_mm, float angle_deg, int32_t *outdated);
 
 /* ---- procedural RGB-D renderer (inputs for tests and benchmarks) ----
  * scene / camera: the recon_scene / recon_camera structs of

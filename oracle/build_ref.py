@@ -3,17 +3,19 @@
 Test infrastructure: the library pins the CPU oracle to the reference's code.
 The reference cannot be built as a whole here (OpenCV / GLEW / SDL2 / CUDA
 samples headers are missing and its kernels use texture references that CUDA
-12+ removed), but its one-thread-per-element kernels compile for the host once
-the few CUDA built-ins they use are provided.  This script
+12+ removed), but its kernels compile for the host once the few CUDA built-ins
+they use are provided.  This script
 
-  * copies the named __global__/__device__ functions out of the reference's
-    .cu files (brace matching, read-only) into oracle/_ref/frag_<file>.inc,
+  * copies the named __global__/__device__ functions (and one PhotoTracker
+    method) out of the reference's sources (brace matching, read-only) into
+    oracle/_ref/frag_<file>.inc,
   * compiles oracle/ref_shim.cpp, which includes those fragments and the
     reference's kernels/kernelUtils.h under a small host shim, together with the
-    reference's CPU SE(3) exponential tracker/tracker/expm.c,
+    reference's CPU SE(3) exponential tracker/tracker/expm.c and its 4x4 /
+    quaternion helpers tracker/tracker/basic_math.cpp,
   * writes everything only below oracle/_ref/ (git-ignored).
 
-Usage: python oracle/build_ref.py [reference_root]   (default /root/reference)
+Usage: python oracle/build_ref.py REFERENCE_ROOT   (or $RECON_REFERENCE)
 """
 from __future__ import annotations
 
@@ -25,7 +27,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 
-# (reference file, [function names]) -- one-thread-per-element kernels only
+# (reference file, [function names]): kernels, and one host method
 FRAGMENTS = {
     "tracker/kernels/warp.cu": [
         "interpolateResidualKernel2", "precomputeJacobian4Kernel", "weightJacobianKernel",
@@ -39,8 +41,13 @@ FRAGMENTS = {
     "tracker/kernels/rgb2gray.cu": [
         "icpResidualKernel2", "icpResidualIndexKernel2", "packIndexKernel", "initWeightsKernel",
         "updateWeightsKernel", "clampWeightsKernel", "convertZMapToXYZKernel", "convertZMapToXYZ6Kernel",
+        "rgbTex2GrayHdrZKernel", "rgbdTex2DepthKernel",
     ],
     "tracker/kernels/downSample2Cuda.cu": ["fastDownSampleHdrKernel"],
+    # one-block kernels with shared memory and __syncthreads (run as 512 host threads)
+    "tracker/kernels/filterIndex256.cu": ["seekThreshold256Kernel2", "filterIndexKernel4"],
+    # host code: the keyframe trigger's pose test
+    "tracker/tracker/phototracker.cpp": ["bool PhotoTracker::poseDifferenceExceeded"],
 }
 
 
@@ -50,7 +57,10 @@ def strip_comments(src: str) -> str:
 
 
 def extract(src: str, name: str) -> str:
-    m = re.search(r"(__global__|__device__)[^;{()]*?\b" + re.escape(name) + r"\s*\(", src)
+    if " " in name:  # a full declarator prefix, e.g. "bool Class::method"
+        m = re.search(re.escape(name) + r"\s*\(", src)
+    else:
+        m = re.search(r"(__global__|__device__)[^;{()]*?\b" + re.escape(name) + r"\s*\(", src)
     if not m:
         raise RuntimeError(f"function {name} not found")
     start = m.start()
@@ -67,9 +77,9 @@ def extract(src: str, name: str) -> str:
 
 
 def main() -> int:
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RECON_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "tracker", "kernels")):
-        print(f"reference tree not found at {ref}; oracle/_ref not built")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RECON_REFERENCE", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "tracker", "kernels")):
+        print(f"reference tree not found ({ref or 'no path given'}); oracle/_ref not built")
         return 1
     os.makedirs(OUT, exist_ok=True)
     for rel, names in FRAGMENTS.items():
@@ -80,7 +90,7 @@ def main() -> int:
         with open(os.path.join(OUT, f"frag_{base}.inc"), "w") as f:
             f.write(f"// extracted from {rel}: {', '.join(names)}\n" + body)
     cxx = os.environ.get("CXX", "g++")
-    flags = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w"]
+    flags = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w", "-std=c++20", "-pthread"]
     inc = ["-I" + OUT, "-I" + os.path.join(ref, "tracker"), "-I" + os.path.join(ref, "tracker", "kernels"),
            "-I" + os.path.join(ref, "tracker", "tracker")]
     objs = []
@@ -91,7 +101,11 @@ def main() -> int:
     subprocess.run([cxx, *flags, *inc, "-x", "c++", "-include", "cmath", "-include", "cstdio", "-c",
                     os.path.join(ref, "tracker", "tracker", "expm.c"), "-o", expm_o], check=True)
     objs.append(expm_o)
-    subprocess.run([cxx, "-shared", "-o", os.path.join(OUT, "libreconref.so"), *objs], check=True)
+    bm_o = os.path.join(OUT, "basic_math.o")
+    subprocess.run([cxx, *flags, *inc, "-c", os.path.join(ref, "tracker", "tracker", "basic_math.cpp"), "-o", bm_o],
+                   check=True)
+    objs.append(bm_o)
+    subprocess.run([cxx, "-shared", "-pthread", "-o", os.path.join(OUT, "libreconref.so"), *objs], check=True)
     print("built", os.path.join(OUT, "libreconref.so"))
     return 0
 

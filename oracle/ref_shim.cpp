@@ -1,16 +1,20 @@
 // ref_shim.cpp -- host build of reference kernels (test infrastructure).
 //
 // Compiled only by oracle/build_ref.py into oracle/_ref/libreconref.so.  It
-// supplies the CUDA built-ins used by the reference's one-thread-per-element
-// kernels (float2/3/4, threadIdx/blockIdx/blockDim, __global__/__device__),
-// includes the reference's own kernels/kernelUtils.h and the kernel bodies
-// extracted verbatim from the reference tree into oracle/_ref/frag_*.inc, and
-// exports ref_* launchers that run each kernel over its grid sequentially.
+// supplies the CUDA built-ins used by the reference's kernels (float2/3/4,
+// threadIdx/blockIdx/blockDim, __global__/__device__, __shared__,
+// __syncthreads, a point-sampled tex2D), includes the reference's own
+// kernels/kernelUtils.h and the kernel bodies extracted verbatim from the
+// reference tree into oracle/_ref/frag_*.inc, and exports ref_* launchers that
+// run each kernel over its grid: one-thread-per-element kernels sequentially,
+// one-block kernels with barriers as one host thread per CUDA thread.
 #include <algorithm>
+#include <barrier>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 using std::fabs;
@@ -23,12 +27,39 @@ struct float3 { float x, y, z; };
 struct float4 { float x, y, z, w; };
 static inline float3 make_float3(float a, float b, float c) { float3 r = {a, b, c}; return r; }
 struct uint3_ { unsigned int x, y, z; };
-static uint3_ threadIdx, blockIdx, blockDim, gridDim;
+// per host thread, so that a block's threads can run concurrently
+static thread_local uint3_ threadIdx, blockIdx, blockDim, gridDim;
+typedef unsigned int uint;
 
 #define __global__ static
 #define __device__ static inline
 #define __host__
+// one block at a time: a __shared__ array is a function-level static that the
+// block's host threads share, and __syncthreads is a barrier across them
+#define __shared__ static
+static std::barrier<> *g_block_barrier = nullptr;
+#define __syncthreads() g_block_barrier->arrive_and_wait()
 typedef double doublereal;
+
+// texture<float4, 2> with point sampling, unnormalised coordinates (the
+// reference sets no filter mode): tex2D(t, x, y) is texel (x, y)
+struct RgbdTexShim {
+    const float4 *data = nullptr;
+    int width = 0;
+};
+static RgbdTexShim rgbdTex;
+static inline float4 tex2D(const RgbdTexShim &t, int x, int y) { return t.data[x + y * t.width]; }
+
+// the PhotoTracker method extracted from phototracker.cpp, on its own
+struct PhotoTracker {
+    bool poseDifferenceExceeded(float *dT, float translationThreshold, float rotationThreshold);
+};
+void rot2Quaternion(float *m, int n, float *q);  // basic_math.cpp
+void normalizeQuaternion(float *qr);
+void invertRT4(double *M, double *iM);
+void matrixMult4x4(double *M1, double *M2, double *R);
+void double_precision4(float *m4, double *m4_dbl);
+void float_precision4(double *m4, float *m4_flt);
 
 #include "calib/calib.h"
 #define VERTEXBUFFER_STRIDE 24
@@ -41,7 +72,10 @@ namespace refk {
 #include "frag_d2z.inc"
 #include "frag_rgb2gray.inc"
 #include "frag_downSample2Cuda.inc"
+#include "frag_filterIndex256.inc"
 }  // namespace refk
+
+#include "frag_phototracker.inc"
 
 void expm(float *x, float *Tmotion, float scaleOut);  // tracker/tracker/expm.c:2084 (C++ linkage)
 
@@ -225,5 +259,66 @@ void ref_linearFuse(float *A1, float *b1, float w1, float iN1, float *A2, float 
 }
 
 void ref_expm(float *x, float *T, float scaleOut) { expm(x, T, scaleOut); }
+
+// filterIndices4 (filterIndex256.cu:172-194): seekThreshold256Kernel2 in one
+// thread, then filterIndexKernel4 as one block of 512 threads whose two
+// __syncthreads phases run as barriers across 512 host threads.  hist: the
+// float histogram (overwritten with the threshold and surplus, as the
+// reference does); index: the selected pixel indices, nVertices entries (the
+// reference's index buffer: its surplus trimming skips the last segment, so
+// it can write past entry P).
+void ref_filterIndices4(float *grad, float *hist, int *index, int nVertices, int P, int nbins) {
+    blockIdx = {0, 0, 0};
+    threadIdx = {0, 0, 0};
+    refk::seekThreshold256Kernel2(hist, P, nbins);
+    const int nthreads = 512;
+    int ppt = nVertices / nthreads;
+    std::barrier<> bar(nthreads);
+    g_block_barrier = &bar;
+    std::vector<std::thread> th;
+    th.reserve(nthreads);
+    for (int t = 0; t < nthreads; t++)
+        th.emplace_back([=] {
+            threadIdx = {(unsigned)t, 0, 0};
+            blockIdx = {0, 0, 0};
+            blockDim = {(unsigned)nthreads, 1, 1};
+            gridDim = {1, 1, 1};
+            refk::filterIndexKernel4(grad, hist, index, nthreads, ppt, nbins);
+        });
+    for (auto &x : th) x.join();
+    g_block_barrier = nullptr;
+}
+
+// rgbTex2GrayHdrZKernel / rgbdTex2DepthKernel (rgb2gray.cu:64-87) over the
+// float4 RGBA-D frame bound as the texture
+void ref_rgbTex2GrayHdrZ(float *rgbd, int W, int H, float *calib, float *gray, float *z, float *z2) {
+    rgbdTex.data = (const float4 *)rgbd;
+    rgbdTex.width = W;
+    launch2d(W, H, [&] { refk::rgbTex2GrayHdrZKernel(gray, W, H, z, calib); });
+    launch2d(W, H, [&] { refk::rgbdTex2DepthKernel(W, H, z2, calib); });
+    rgbdTex.data = nullptr;
+}
+
+// PhotoTracker::poseDifferenceExceeded (phototracker.cpp:268-288)
+int ref_poseDifferenceExceeded(float *dT, float dist, float angle) {
+    PhotoTracker p;
+    return p.poseDifferenceExceeded(dT, dist, angle) ? 1 : 0;
+}
+
+// PhotoTracker::applyIncrement's pose arithmetic (phototracker.cpp:514-531)
+// with the reference's basic_math.cpp: T (host, current -> reference, float)
+// and the global pose are updated from the tracked pose Trel.
+void ref_applyIncrement(float *T, double *globalPose, float *Trel) {
+    double TdblPrev[16];
+    double_precision4(T, &TdblPrev[0]);
+    double iTprev[16];
+    invertRT4(&TdblPrev[0], &iTprev[0]);
+    double iTdbl[16], Tdbl[16], Tinc[16];
+    double_precision4(Trel, &iTdbl[0]);
+    invertRT4(&iTdbl[0], &Tdbl[0]);
+    float_precision4(&Tdbl[0], T);
+    matrixMult4x4(&iTprev[0], &Tdbl[0], &Tinc[0]);
+    matrixMult4x4(&globalPose[0], &Tinc[0], &globalPose[0]);
+}
 
 }  // extern "C"

@@ -131,6 +131,10 @@ def lib() -> ctypes.CDLL:
             L.recon_set_mode.argtypes = [vp, i32, f32]
             L.recon_get_relative_pose.argtypes = [vp, vp]
             L.recon_get_global_pose.argtypes = [vp, vp]
+            L.recon_pose_difference_exceeded.argtypes = [vp, f32, f32]
+            L.recon_set_reference_updating.argtypes = [vp, i32, f32, f32]
+            L.recon_reference_outdated.argtypes = [vp]
+            L.recon_batch_reference_outdated.argtypes = [vp, f32, f32, vp]
             L.recon_reset.argtypes = [vp]
             L.recon_batch_track_sequence.argtypes = [vp, i32, vp, vp, i32, vp, vp]
             L.recon_batch_fuse_keyframe.argtypes = [vp, i32, vp, vp, i32, f32]
@@ -509,6 +513,36 @@ class Tracker(Batch):
         g = np.zeros(16, np.float64)
         check(lib().recon_get_global_pose(self.h, _ptr(g)))
         return g.reshape(4, 4)
+
+    def relative_pose(self) -> np.ndarray:
+        """The host relative pose (current -> reference, float), getRelativePose."""
+        T = np.zeros(16, np.float32)
+        check(lib().recon_get_relative_pose(self.h, _ptr(T)))
+        return T.reshape(4, 4)
+
+    def set_reference_updating(self, on: bool, dist_mm: float = 125.0, angle_deg: float = 12.5):
+        check(lib().recon_set_reference_updating(self.h, int(on), dist_mm, angle_deg))
+
+    def reference_outdated(self) -> bool:
+        return bool(check(lib().recon_reference_outdated(self.h)))
+
+    def reset(self):
+        check(lib().recon_reset(self.h))
+
+
+def pose_difference_exceeded(dT, dist_mm: float = 125.0, angle_deg: float = 12.5) -> bool:
+    """poseDifferenceExceeded (recon_pose_difference_exceeded): host code, no GPU needed."""
+    T = np.ascontiguousarray(np.asarray(dT, np.float32).reshape(16))
+    return bool(check(lib().recon_pose_difference_exceeded(_ptr(T), dist_mm, angle_deg)))
+
+
+def _batch_reference_outdated(self, dist_mm: float = 125.0, angle_deg: float = 12.5) -> np.ndarray:
+    out = np.zeros(self.n, np.int32)
+    check(lib().recon_batch_reference_outdated(self.h, dist_mm, angle_deg, _ptr(out)))
+    return out.astype(bool)
+
+
+Batch.reference_outdated = _batch_reference_outdated
 
 
 def render_depth(scene, camera, noise_rel: float, noise_seed: int, frame: int, out, stream=None):

@@ -173,9 +173,13 @@ struct recon_batch {
     int *d_all_active = nullptr;        // [n] ones: the fusion updates every instance
     float *d_fuse_T = nullptr;
     size_t fuse_cap = 0;
-    // host pose bookkeeping for the single-tracker API (applyIncrement)
+    // host pose bookkeeping for the single-tracker API (applyIncrement):
+    // T_host is the reference's host pose T, current -> reference, float
     double global_pose[16];
-    float T_prev[16];
+    float T_host[16];
+    // keyframe policy (setReferenceUpdating / referenceOutdated)
+    bool ref_updating = false;
+    float ref_dist_mm = 125.0f, ref_angle_deg = 12.5f;  // phototracker.cpp:127-128
     // learned initialisation (recon_batch_set_init_net)
     recon_initnet *net = nullptr;
     uint16_t *d_coarse[2] = {nullptr, nullptr};  // coarse images [n][60][80][2] BF16: previous / current frame
@@ -810,7 +814,7 @@ int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs,
     b->cfg.assign(cfgs, cfgs + n);
     b->desc.resize(n);
     identity16d(b->global_pose);
-    identity16(b->T_prev);
+    identity16(b->T_host);
     if (stream) {
         b->stream = (cudaStream_t)stream;
     } else {
@@ -1538,42 +1542,95 @@ int recon_tracker_destroy(recon_tracker *t) { return recon_batch_destroy(t); }
 int recon_set_reference(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device) {
     if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
     int rc = recon_batch_set_reference(t, &gray, &depth, on_device);
-    if (rc == RECON_OK) identity16(t->T_prev);
+    if (rc == RECON_OK) identity16(t->T_host);  // prepareReference clears T (phototracker.cpp:362-368)
     return rc;
 }
 int recon_set_current(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device) {
     return recon_batch_set_current(t, &gray, &depth, on_device);
 }
 
-// applyIncrement, phototracker.cpp:514-531: Tinc = inv(T_prev)^-1 ... in double
-static void apply_increment(recon_tracker *t, const float *Tnew) {
-    // the tracker pose maps reference -> current; the camera motion since the
-    // previous frame is inv(Tprev) composed with Tnew's inverse direction
-    double Tp[16], iTp[16], Tn[16], iTn[16], inc[16], g[16];
-    for (int i = 0; i < 16; i++) { Tp[i] = t->T_prev[i]; Tn[i] = Tnew[i]; }
-    auto inv = [](const double *M, double *Mi) {
-        Mi[0] = M[0]; Mi[1] = M[4]; Mi[2] = M[8];   Mi[3] = -(M[0] * M[3] + M[4] * M[7] + M[8] * M[11]);
-        Mi[4] = M[1]; Mi[5] = M[5]; Mi[6] = M[9];   Mi[7] = -(M[1] * M[3] + M[5] * M[7] + M[9] * M[11]);
-        Mi[8] = M[2]; Mi[9] = M[6]; Mi[10] = M[10]; Mi[11] = -(M[2] * M[3] + M[6] * M[7] + M[10] * M[11]);
-        Mi[12] = 0;   Mi[13] = 0;   Mi[14] = 0;     Mi[15] = 1;
-    };
-    auto mul = [](const double *A, const double *B, double *C) {
-        double t2[16];
-        for (int r = 0; r < 4; r++)
-            for (int c = 0; c < 4; c++) {
-                double s = 0;
-                for (int k = 0; k < 4; k++) s += A[r * 4 + k] * B[k * 4 + c];
-                t2[r * 4 + c] = s;
-            }
-        memcpy(C, t2, sizeof(t2));
-    };
-    inv(Tp, iTp);
-    inv(Tn, iTn);
-    (void)iTp;
-    mul(Tp, iTn, inc);  // previous -> new camera motion
-    mul(t->global_pose, inc, g);
-    memcpy(t->global_pose, g, sizeof(g));
-    memcpy(t->T_prev, Tnew, 16 * sizeof(float));
+// invertRT4 (basic_math.cpp:335-353) in double
+static void invert_rt4d(const double *M, double *Mi) {
+    Mi[0] = M[0]; Mi[1] = M[4]; Mi[2] = M[8];   Mi[3] = -(M[0] * M[3] + M[4] * M[7] + M[8] * M[11]);
+    Mi[4] = M[1]; Mi[5] = M[5]; Mi[6] = M[9];   Mi[7] = -(M[1] * M[3] + M[5] * M[7] + M[9] * M[11]);
+    Mi[8] = M[2]; Mi[9] = M[6]; Mi[10] = M[10]; Mi[11] = -(M[2] * M[3] + M[6] * M[7] + M[10] * M[11]);
+    Mi[12] = 0;   Mi[13] = 0;   Mi[14] = 0;     Mi[15] = 1;
+}
+
+// matrixMult4x4 in double, each entry the left-to-right sum of its four
+// products (basic_math.cpp:183-207); the product may alias an input
+static void mult4x4d(const double *A, const double *B, double *C) {
+    double t2[16];
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++)
+            t2[r * 4 + c] = A[r * 4 + 0] * B[0 * 4 + c] + A[r * 4 + 1] * B[1 * 4 + c] + A[r * 4 + 2] * B[2 * 4 + c] +
+                            A[r * 4 + 3] * B[3 * 4 + c];
+    memcpy(C, t2, sizeof(t2));
+}
+
+// PhotoTracker::applyIncrement (phototracker.cpp:514-531).  Trel is the
+// tracked pose (reference -> current, the device pose).  The host pose T is
+// kept as the reference keeps it: current -> reference, inverted in double
+// and stored as float; the increment from the previous frame is
+// inv(double(T_prev)) * inv(double(Trel)) and is accumulated into the double
+// global pose.
+static void apply_increment(recon_tracker *t, const float *Trel) {
+    double TdblPrev[16], iTprev[16], iTdbl[16], Tdbl[16], Tinc[16];
+    for (int i = 0; i < 16; i++) {
+        TdblPrev[i] = (double)t->T_host[i];
+        iTdbl[i] = (double)Trel[i];
+    }
+    invert_rt4d(TdblPrev, iTprev);
+    invert_rt4d(iTdbl, Tdbl);
+    for (int i = 0; i < 16; i++) t->T_host[i] = (float)Tdbl[i];
+    mult4x4d(iTprev, Tdbl, Tinc);
+    mult4x4d(t->global_pose, Tinc, t->global_pose);
+}
+
+// PhotoTracker::poseDifferenceExceeded (phototracker.cpp:268-288): the
+// translation length of dT, and the rotation angle of dT from its unit
+// quaternion (the identity rotation, to 1e-5 on the diagonal, is angle 0).
+static bool pose_difference_exceeded(const float *dT, float dist_mm, float angle_deg) {
+    double dx = dT[3], dy = dT[7], dz = dT[11];
+    float dist = (float)std::sqrt(dx * dx + dy * dy + dz * dz + 1e-12f);
+    if (dist > dist_mm) return true;
+    float angle = 0.0f;
+    if (std::fabs(dT[0] - 1.0f) > 1e-5 || std::fabs(dT[5] - 1.0f) > 1e-5 || std::fabs(dT[10] - 1.0f) > 1e-5) {
+        // rotation -> unit quaternion (w, x, y, z), branching on the largest
+        // diagonal term for stability (rot2Quaternion, basic_math.cpp:943-973)
+        float q[4];
+        float tr = dT[0] + dT[5] + dT[10];
+        if (tr > 0) {
+            float sc = 0.5f / std::sqrt(tr + 1.0f);
+            q[0] = 0.25f / sc;
+            q[1] = (dT[9] - dT[6]) * sc;
+            q[2] = (dT[2] - dT[8]) * sc;
+            q[3] = (dT[4] - dT[1]) * sc;
+        } else if (dT[0] > dT[5] && dT[0] > dT[10]) {
+            float sc = 2.0f * std::sqrt(1.0f + dT[0] - dT[5] - dT[10]);
+            q[0] = (dT[9] - dT[6]) / sc;
+            q[1] = 0.25f * sc;
+            q[2] = (dT[1] + dT[4]) / sc;
+            q[3] = (dT[2] + dT[8]) / sc;
+        } else if (dT[5] > dT[10]) {
+            float sc = 2.0f * std::sqrt(1.0f + dT[5] - dT[0] - dT[10]);
+            q[0] = (dT[2] - dT[8]) / sc;
+            q[1] = (dT[1] + dT[4]) / sc;
+            q[2] = 0.25f * sc;
+            q[3] = (dT[6] + dT[9]) / sc;
+        } else {
+            float sc = 2.0f * std::sqrt(1.0f + dT[10] - dT[0] - dT[5]);
+            q[0] = (dT[4] - dT[1]) / sc;
+            q[1] = (dT[2] + dT[8]) / sc;
+            q[2] = (dT[6] + dT[9]) / sc;
+            q[3] = 0.25f * sc;
+        }
+        // normalizeQuaternion (basic_math.cpp:1006-1013)
+        float len = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] + 1e-7f);
+        for (int k = 0; k < 4; k++) q[k] /= len;
+        angle = (float)(std::acos((double)q[0]) * 2.0f * 180.0f / 3.141592653f);
+    }
+    return angle > angle_deg;
 }
 
 int recon_track(recon_tracker *t, float T_io[16], recon_track_stats *stats) {
@@ -1594,7 +1651,49 @@ int recon_set_iterations(recon_tracker *t, const int32_t iters[RECON_MAX_LEVELS]
 int recon_set_mode(recon_tracker *t, int32_t mode, float lambda) { return recon_batch_set_mode(t, 0, mode, lambda); }
 int recon_get_relative_pose(recon_tracker *t, float T[16]) {
     if (!t || !T) return fail(RECON_ERR_INVALID_ARG, "null argument");
-    return recon_batch_get_poses(t, T, nullptr);
+    memcpy(T, t->T_host, sizeof(t->T_host));
+    return RECON_OK;
+}
+
+int recon_set_reference_updating(recon_tracker *t, int32_t on, float dist_mm, float angle_deg) {
+    if (!t || !(dist_mm > 0.0f) || !(angle_deg > 0.0f)) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    t->ref_updating = on != 0;
+    t->ref_dist_mm = dist_mm;
+    t->ref_angle_deg = angle_deg;
+    return RECON_OK;
+}
+
+int recon_reference_outdated(recon_tracker *t) {
+    if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
+    if (!t->have_ref) return 1;
+    return (t->ref_updating && pose_difference_exceeded(t->T_host, t->ref_dist_mm, t->ref_angle_deg)) ? 1 : 0;
+}
+
+int recon_pose_difference_exceeded(const float dT[16], float dist_mm, float angle_deg) {
+    if (!dT) return fail(RECON_ERR_INVALID_ARG, "null pose");
+    return pose_difference_exceeded(dT, dist_mm, angle_deg) ? 1 : 0;
+}
+
+int recon_batch_reference_outdated(recon_batch *b, float dist_mm, float angle_deg, int32_t *outdated) {
+    clear_stale_error();
+    if (!b || !outdated || !(dist_mm > 0.0f) || !(angle_deg > 0.0f)) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    if (!b->have_ref) {
+        for (int i = 0; i < b->n; i++) outdated[i] = 1;
+        return RECON_OK;
+    }
+    std::vector<float> T(16 * (size_t)b->n);
+    int rc = recon_batch_get_poses(b, T.data(), nullptr);
+    if (rc) return rc;
+    for (int i = 0; i < b->n; i++) {
+        // the reference tests its host pose T = inv(Trel), inverted in double and stored as float
+        double Td[16], Ti[16];
+        float Tf[16];
+        for (int k = 0; k < 16; k++) Td[k] = (double)T[16 * (size_t)i + k];
+        invert_rt4d(Td, Ti);
+        for (int k = 0; k < 16; k++) Tf[k] = (float)Ti[k];
+        outdated[i] = pose_difference_exceeded(Tf, dist_mm, angle_deg) ? 1 : 0;
+    }
+    return RECON_OK;
 }
 int recon_get_global_pose(recon_tracker *t, double T[16]) {
     if (!t || !T) return fail(RECON_ERR_INVALID_ARG, "null argument");
@@ -1605,7 +1704,7 @@ int recon_reset(recon_tracker *t) {
     clear_stale_error();
     if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
     identity16d(t->global_pose);
-    identity16(t->T_prev);
+    identity16(t->T_host);
     float I[16];
     identity16(I);
     CK(cudaMemcpyAsync(t->desc[0].T, I, sizeof(I), cudaMemcpyHostToDevice, t->stream));

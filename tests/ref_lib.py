@@ -44,5 +44,10 @@ def lib() -> ctypes.CDLL:
         L.ref_conjugateGradient.argtypes = [vp, vp, vp]
         L.ref_linearFuse.argtypes = [vp, vp, f32, f32, vp, vp, f32, f32]
         L.ref_expm.argtypes = [vp, vp, f32]
+        L.ref_filterIndices4.argtypes = [vp, vp, vp, i32, i32, i32]
+        L.ref_rgbTex2GrayHdrZ.argtypes = [vp, i32, i32, vp, vp, vp, vp]
+        L.ref_poseDifferenceExceeded.argtypes = [vp, f32, f32]
+        L.ref_poseDifferenceExceeded.restype = i32
+        L.ref_applyIncrement.argtypes = [vp, vp, vp]
         _lib = L
     return _lib

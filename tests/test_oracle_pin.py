@@ -276,3 +276,132 @@ def test_canonical_reduction_close_to_reference_order():
     np.testing.assert_allclose(A.reshape(6, 6), A_exact, rtol=1e-5, atol=1e-3)
     np.testing.assert_allclose(Af.reshape(6, 6), A_exact, rtol=1e-5, atol=1e-2)
     np.testing.assert_allclose(b, Jm @ r.astype(np.float64), rtol=1e-5, atol=1e-3)
+
+
+def test_selection_matches_reference(frame_pair):
+    """Pixel selection (A5): the oracle's 256-bin histogram and index list
+    equal the reference's extractGradientKernel + seekThreshold256Kernel2 +
+    filterIndexKernel4 (filterIndex256.cu:26-46, 110-169), the latter run as
+    one block of 512 host threads with its two barriers."""
+    fp = frame_pair
+    W, H = fp["W"], fp["H"]
+    z, xyz_o, xyz_r, lv, vd_o, vd_r = _reference_prep(fp)
+    grad = np.ascontiguousarray(vd_o.reshape(-1, 24)[:, 13])
+    grad_r = np.zeros(W * H, np.float32)
+    R.lib().ref_extractGradient(p(vd_r), W * H, p(grad_r))
+    assert np.array_equal(grad.view(np.uint32), grad_r.view(np.uint32))
+    hist = np.zeros(256, np.int32)
+    O.lib().orc_grad_histogram(p(grad), W * H, 256, p(hist))
+    for P in (8192, 4096):
+        idx_o = np.zeros(P, np.int32)
+        n_o = O.lib().orc_filter_indices(p(grad), W * H, p(hist), 256, P, p(idx_o))
+        histf = hist.astype(np.float32)  # cudaHista's float counts
+        # the reference's zero-initialised index buffer holds one entry per
+        # vertex: the kernel never trims the last of its 512 segments, so it
+        # can write past entry P (the tracker then uses the first P)
+        idx_r = np.zeros(W * H, np.int32)
+        R.lib().ref_filterIndices4(p(grad_r), p(histf), p(idx_r), W * H, P, 256)
+        assert np.array_equal(idx_o, idx_r[:P]), P
+        # the count the reference writes, P or more (the untrimmed last segment)
+        assert n_o >= P
+        # the reference's seek wrote the threshold bin and the surplus into hist[0..1]
+        thr = int(histf[0])
+        assert hist[thr + 1:].sum() <= P < hist[thr:].sum()
+
+
+def test_rgbd_float4_conversion_matches_reference():
+    """Float4 RGBA + normalised depth input (A2): orc_rgbd_float4_to_gray_z
+    equals rgbTex2GrayHdrZKernel and rgbdTex2DepthKernel (rgb2gray.cu:64-87)
+    reading the frame through a point-sampled texture with the y-flip."""
+    W, H = 320, 240
+    rng = np.random.default_rng(5)
+    rgbd = rng.random((H, W, 4), dtype=np.float32)
+    rgbd[..., 3] = rng.random((H, W), dtype=np.float32)
+    cal = synth.make_calibration(W, H)
+    calib = np.ascontiguousarray(cal.calib, np.float32)
+    g_o = np.zeros(W * H, np.float32)
+    z_o = np.zeros(W * H, np.float32)
+    O.lib().orc_rgbd_float4_to_gray_z(p(rgbd), W, H, p(calib), p(g_o), p(z_o))
+    g_r = np.zeros(W * H, np.float32)
+    z_r = np.zeros(W * H, np.float32)
+    z2_r = np.zeros(W * H, np.float32)
+    R.lib().ref_rgbTex2GrayHdrZ(p(rgbd), W, H, p(calib), p(g_r), p(z_r), p(z2_r))
+    assert np.array_equal(g_o.view(np.uint32), g_r.view(np.uint32))
+    assert np.array_equal(z_o.view(np.uint32), z_r.view(np.uint32))
+    assert np.array_equal(z_o.view(np.uint32), z2_r.view(np.uint32))
+
+
+def _random_poses(n, seed, max_deg, max_mm):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        deg = float(rng.uniform(0.0, max_deg))
+        mm = float(rng.uniform(0.0, max_mm))
+        out.append(synth.offset_pose(int(rng.integers(1 << 30)), deg, mm).astype(np.float32))
+    return out
+
+
+def test_pose_difference_exceeded_matches_reference():
+    """The keyframe trigger (A20): recon_pose_difference_exceeded equals
+    PhotoTracker::poseDifferenceExceeded (phototracker.cpp:268-288) compiled
+    from the reference, on poses around both thresholds and on identities."""
+    import recon_gb300 as rg
+    poses = _random_poses(400, 17, 25.0, 250.0) + _random_poses(200, 18, 13.0, 1.0)
+    poses += [np.eye(4, dtype=np.float32)]
+    eye = np.eye(4, dtype=np.float32)
+    eye[:3, 3] = [80.0, 90.0, 30.0]
+    poses.append(eye)
+    # rotations near 180 degrees take the quaternion's other branches
+    for ax in range(3):
+        Rm = np.eye(4, dtype=np.float32)
+        i, j = [k for k in range(3) if k != ax]
+        Rm[i, i] = Rm[j, j] = np.float32(-1.0)
+        poses.append(Rm)
+    hits = 0
+    for T in poses:
+        for dist, ang in ((125.0, 12.5), (30.0, 2.0)):
+            Tc = np.ascontiguousarray(T.reshape(16))
+            a = rg.pose_difference_exceeded(Tc, dist, ang)
+            b = bool(R.lib().ref_poseDifferenceExceeded(p(Tc), dist, ang))
+            assert a == b, (T, dist, ang)
+            hits += a
+    assert 0 < hits < 2 * len(poses)
+
+
+def apply_increment_ref_order(T_host, G, Trel):
+    """PhotoTracker::applyIncrement's arithmetic (phototracker.cpp:514-531) in
+    Python floats, in the reference's operation order (invertRT4 and
+    matrixMult4x4 of basic_math.cpp): returns the new host pose (float32,
+    current -> reference) and global pose (float64)."""
+    def inv(M):
+        M = [float(v) for v in M]
+        return [M[0], M[4], M[8], -(M[0] * M[3] + M[4] * M[7] + M[8] * M[11]),
+                M[1], M[5], M[9], -(M[1] * M[3] + M[5] * M[7] + M[9] * M[11]),
+                M[2], M[6], M[10], -(M[2] * M[3] + M[6] * M[7] + M[10] * M[11]),
+                0.0, 0.0, 0.0, 1.0]
+
+    def mul(A, B):
+        return [A[r * 4] * B[c] + A[r * 4 + 1] * B[4 + c] + A[r * 4 + 2] * B[8 + c] + A[r * 4 + 3] * B[12 + c]
+                for r in range(4) for c in range(4)]
+
+    iTprev = inv(np.asarray(T_host, np.float32).reshape(16))
+    Tdbl = inv(np.asarray(Trel, np.float32).reshape(16))
+    T_new = np.asarray(Tdbl, np.float64).astype(np.float32)
+    G_new = mul([float(v) for v in np.asarray(G, np.float64).reshape(16)], mul(iTprev, Tdbl))
+    return T_new.reshape(4, 4), np.asarray(G_new, np.float64).reshape(4, 4)
+
+
+def test_apply_increment_restatement_matches_reference():
+    """The Python restatement of applyIncrement used by the GPU test of the
+    single tracker's global pose equals the reference's own arithmetic bit for
+    bit over a chain of tracked poses."""
+    T = np.eye(4, dtype=np.float32)
+    G = np.eye(4, dtype=np.float64)
+    Tr = np.ascontiguousarray(np.eye(4, dtype=np.float32).reshape(16))
+    Gr = np.ascontiguousarray(np.eye(4, dtype=np.float64).reshape(16))
+    for Trel in _random_poses(40, 23, 3.0, 40.0):
+        T, G = apply_increment_ref_order(T, G, Trel)
+        Trel_c = np.ascontiguousarray(Trel.reshape(16))
+        R.lib().ref_applyIncrement(p(Tr), p(Gr), p(Trel_c))
+        assert np.array_equal(T.reshape(16).view(np.uint32), Tr.view(np.uint32))
+        assert np.array_equal(G.reshape(16).view(np.uint64), Gr.view(np.uint64))
