@@ -1053,6 +1053,75 @@ void orc_icp_residual_jacobian(const float *ref6, const int32_t *select, int nse
     }
 }
 
+/* The tracker's ICP residual and Jacobian over the level's pixel grid (the
+ * GPU's icp_point): weights[idx] per pixel, 0 where the pixel is not a
+ * correspondence.  The projection, bilinear taps and correspondence test are
+ * icpResidualIndexKernel2's expressions (rgb2gray.cu:323-390) without
+ * contraction; the rotated normal, the residual and the Jacobian are
+ * evaluated with fmaf in a fixed order, and the reference's products by exact
+ * zeros and ones of [p]x, [n]x and the unit vectors are left out (for a finite
+ * pose that changes at most the sign of a zero entry).  Against the
+ * reference-ordered orc_icp_residual_jacobian the values agree to a few ulp. */
+void orc_icp_residual_jacobian_grid(const float *ref6, int width, int height, int layer, const float *T,
+                                    const float *calib, const float *cur6, const int32_t *curmask, int npadded,
+                                    float *res, float *J, const float *weights, float optScaleIn) {
+    const float *K = &calib[KL_OFFSET];
+    int divisor = 1 << layer;
+    float a = 1.0f / (float)divisor;
+    float b = 0.5f * (a - 1.0f);
+    int n = width * height;
+#pragma omp parallel for schedule(static)
+    for (int idx = 0; idx < npadded; idx++) {
+        res[idx] = 0.0f;
+        for (int c = 0; c < 6; c++) J[idx + npadded * c] = 0.0f;
+        if (idx >= n) continue;
+        float weight = weights[idx];
+        if (!(weight > 0.0f)) continue;
+        const float *p = &ref6[idx * 6];
+        float p3[3] = {p[0], p[1], p[2]}, rn[3] = {p[3], p[4], p[5]};
+        float q3[3];
+        mul4(T, p3, q3);
+        float q2x = q3[0] / q3[2], q2y = q3[1] / q3[2];
+        float p2x = a * (K[0] * q2x + K[2]) + b;
+        float p2y = a * (K[4] * q2y + K[5]) + b;
+        if (!(p2x >= 0 && p2x < (width - 1) && p2y >= 0 && p2y < (height - 1))) continue;
+        int xdi = ftoi(p2x), ydi = ftoi(p2y);
+        float fx = p2x - xdi, fy = p2y - ydi;
+        int off2 = xdi + ydi * width;
+        float cp[3];
+        bilin6(&cur6[off2 * 6], fx, fy, width * 6, cp);
+        if (!(curmask[off2] && fabsf(cp[2] - q3[2]) < 300.0f)) continue;
+        float rv[3] = {cp[0] - q3[0], cp[1] - q3[1], cp[2] - q3[2]};
+        float cn[3];
+        for (int r = 0; r < 3; r++)
+            cn[r] = fmaf(T[4 * r + 2], rn[2], fmaf(T[4 * r + 1], rn[1], T[4 * r] * rn[0]));
+        res[idx] = optScaleIn * weight * fmaf(rv[2], cn[2], fmaf(rv[1], cn[1], rv[0] * cn[0]));
+        /* columns of R [p]x and R [n]x: R_c1 * s1 + R_c2 * s2 per row */
+        float B[3][3], N[3][3];
+        for (int r = 0; r < 3; r++) {
+            const float *Tr = &T[4 * r];
+            B[0][r] = fmaf(Tr[1], -p3[2], Tr[2] * p3[1]);
+            B[1][r] = fmaf(Tr[0], p3[2], Tr[2] * -p3[0]);
+            B[2][r] = fmaf(Tr[0], -p3[1], Tr[1] * p3[0]);
+            N[0][r] = fmaf(Tr[1], -rn[2], Tr[2] * rn[1]);
+            N[1][r] = fmaf(Tr[0], rn[2], Tr[2] * -rn[0]);
+            N[2][r] = fmaf(Tr[0], -rn[1], Tr[1] * rn[0]);
+        }
+        float so = -optScaleIn * weight;
+        for (int c = 0; c < 3; c++) {
+            float t = -cn[0] * B[c][0];
+            t = fmaf(-cn[1], B[c][1], t);
+            t = fmaf(-cn[2], B[c][2], t);
+            t = fmaf(rv[0], N[c][0], t);
+            t = fmaf(rv[1], N[c][1], t);
+            t = fmaf(rv[2], N[c][2], t);
+            J[idx + npadded * c] = so * t;
+        }
+        for (int c = 0; c < 3; c++)
+            J[idx + npadded * (3 + c)] = -weight * fmaf(-cn[2], T[8 + c], fmaf(-cn[1], T[4 + c], -cn[0] * T[c]));
+    }
+}
+
 /* ------------------------------------------------------------------ */
 /* 6x6 solve and SE(3) exponential                                     */
 /* ------------------------------------------------------------------ */
@@ -1752,9 +1821,9 @@ int orc_track(orc_tracker *t, float *Tio, orc_iter_trace *trace, int max_trace) 
                      * level's pixel grid in 1024-pixel chunks; a pixel that was
                      * not selected has weight 0 and contributes exact zeros. */
                     int npx = wl * hl, np = padded_len(npx);
-                    orc_icp_residual_jacobian(t->ref6[layer], t->all_px, npx, wl, hl, layer, t->T, t->calib,
-                                              t->cur6[layer], t->curmask[layer], np, t->icp_res, t->icp_J, t->icp_wpx,
-                                              t->cfg.opt_scale_in);
+                    orc_icp_residual_jacobian_grid(t->ref6[layer], wl, hl, layer, t->T, t->calib, t->cur6[layer],
+                                                   t->curmask[layer], np, t->icp_res, t->icp_J, t->icp_wpx,
+                                                   t->cfg.opt_scale_in);
                     const float *J6[6];
                     for (int c = 0; c < 6; c++) J6[c] = t->icp_J + (size_t)c * np;
                     orc_fx27 acc;

@@ -133,6 +133,10 @@ void orc_student_t(const float *r2, int n, float *w);
 void orc_icp_residual_jacobian(const float *ref6, const int32_t *select, int nsel, int w, int h, int layer,
                                const float *T, const float *calib, const float *cur6, const int32_t *curmask,
                                int npadded, float *r, float *J, const float *weights, float optScaleIn);
+/* the tracker's form over the pixel grid (fused multiply-adds in the continuous terms) */
+void orc_icp_residual_jacobian_grid(const float *ref6, int w, int h, int layer, const float *T, const float *calib,
+                                    const float *cur6, const int32_t *curmask, int npadded, float *r, float *J,
+                                    const float *weights, float optScaleIn);
 
 /* ---- solve and SE(3) update ---- */
 int orc_solve_cholesky(const double A[36], const double b[6], double x[6]);

@@ -36,7 +36,7 @@ __global__ void k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *
                                        float *store_prev, int begin);
 __global__ void k_icp_student3(const InstDesc *D, int level);
 __global__ void k_icp_prepare(const InstDesc *D, int level);
-__global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta);
+__global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta, int n_inst, int icp_ctas);
 __global__ void k_solve(const InstDesc *D, int level, int it);
 __global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
                                uint16_t *out);
@@ -524,13 +524,14 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
             b->graph_kernels += 2;
         }
         int per_cta = icp_per_cta(b, level, nchunk);
-        int ncta = (nchunk + per_cta - 1) / per_cta;
-        // the photometric cluster, then the ICP CTAs rounded up to whole clusters
-        int gx = kIterCluster + (any_icp ? (ncta + kIterCluster - 1) / kIterCluster * kIterCluster : 0);
+        int ncta = any_icp ? (nchunk + per_cta - 1) / per_cta : 0;
+        // every instance's photometric cluster, then ncta ICP CTAs per
+        // instance, the total rounded up to whole clusters
+        int gx = kIterCluster * n + (n * ncta + kIterCluster - 1) / kIterCluster * kIterCluster;
         for (int it = 0; it < maxit; it++) {
             {
                 TimedScope ts(b, s, TK_ITER, in_graph);
-                CK(launch_pdl(k_iter, dim3(gx, n), dim3(kIterBlock), s, D, level, it, per_cta));
+                CK(launch_pdl(k_iter, dim3(gx, 1), dim3(kIterBlock), s, D, level, it, per_cta, n, ncta));
             }
             {
                 TimedScope ts(b, s, TK_SOLVE, in_graph);

@@ -1062,7 +1062,12 @@ __device__ __forceinline__ void icp_load(const InstDesc &d, int level, int idx, 
 
 // icpResidualIndexKernel2, rgb2gray.cu:323-390, for one pixel of the level.  A
 // pixel that is not a correspondence has weight 0, and the reference's test
-// `weight > 0` then gives zeros.
+// `weight > 0` then gives zeros.  The projection, the bilinear taps and the
+// correspondence test are the reference's expressions without contraction
+// (they decide which pixels count); the rotated normal, the residual and the
+// Jacobian, continuous terms of the normal equations only, are evaluated with
+// fused multiply-adds (one rounding per multiply-add; the oracle's
+// orc_icp_residual_jacobian_grid states the same sequence with fmaf).
 __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int level, float weight, float4 p,
                                           float4 rn, float *j, float &res) {
     res = 0.0f;
@@ -1073,9 +1078,8 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     const float *K = d.calib + RC_KL;
     float a = 1.0f / (float)(1 << level);
     float b = 0.5f * (a - 1.0f);
-    float qx, qy, qz, cnx, cny, cnz;
+    float qx, qy, qz;
     mul4(T, p.x, p.y, p.z, qx, qy, qz);
-    rot4(T, rn.x, rn.y, rn.z, cnx, cny, cnz);
     float q2x = qx / qz, q2y = qy / qz;
     float p2x = a * (K[0] * q2x + K[2]) + b;
     float p2y = a * (K[4] * q2y + K[5]) + b;
@@ -1088,24 +1092,42 @@ __device__ __forceinline__ void icp_point(const InstDesc &d, const float *T, int
     if (!(m0 != 0.0f && fabsf(cz - qz) < 300.0f)) return;
     float optScaleIn = d.opt_in;
     float rvx = cx - qx, rvy = cy - qy, rvz = cz - qz;
-    res = optScaleIn * weight * (rvx * cnx + rvy * cny + rvz * cnz);
+    float cnx = __fmaf_rn(T[2], rn.z, __fmaf_rn(T[1], rn.y, T[0] * rn.x));
+    float cny = __fmaf_rn(T[6], rn.z, __fmaf_rn(T[5], rn.y, T[4] * rn.x));
+    float cnz = __fmaf_rn(T[10], rn.z, __fmaf_rn(T[9], rn.y, T[8] * rn.x));
+    res = optScaleIn * weight * __fmaf_rn(rvz, cnz, __fmaf_rn(rvy, cny, rvx * cnx));
     // The reference rotates the columns of [p]x and [n]x and the unit vectors
     // with full 3x3 products.  The terms it multiplies by an exact 0 or 1 are
     // dropped here: for a finite pose that changes at most the sign of a zero
-    // Jacobian entry, and signed zeros add nothing to the fixed-point sums, so
-    // the normal equations are bit-identical.
-    float b0x = T[1] * (-p.z) + T[2] * p.y, b0y = T[5] * (-p.z) + T[6] * p.y, b0z = T[9] * (-p.z) + T[10] * p.y;
-    float b1x = T[0] * p.z + T[2] * (-p.x), b1y = T[4] * p.z + T[6] * (-p.x), b1z = T[8] * p.z + T[10] * (-p.x);
-    float b2x = T[0] * (-p.y) + T[1] * p.x, b2y = T[4] * (-p.y) + T[5] * p.x, b2z = T[8] * (-p.y) + T[9] * p.x;
-    float n0x = T[1] * (-rn.z) + T[2] * rn.y, n0y = T[5] * (-rn.z) + T[6] * rn.y, n0z = T[9] * (-rn.z) + T[10] * rn.y;
-    float n1x = T[0] * rn.z + T[2] * (-rn.x), n1y = T[4] * rn.z + T[6] * (-rn.x), n1z = T[8] * rn.z + T[10] * (-rn.x);
-    float n2x = T[0] * (-rn.y) + T[1] * rn.x, n2y = T[4] * (-rn.y) + T[5] * rn.x, n2z = T[8] * (-rn.y) + T[9] * rn.x;
+    // Jacobian entry, and signed zeros add nothing to the fixed-point sums.
+    float b0x = __fmaf_rn(T[1], -p.z, T[2] * p.y), b0y = __fmaf_rn(T[5], -p.z, T[6] * p.y),
+          b0z = __fmaf_rn(T[9], -p.z, T[10] * p.y);
+    float b1x = __fmaf_rn(T[0], p.z, T[2] * -p.x), b1y = __fmaf_rn(T[4], p.z, T[6] * -p.x),
+          b1z = __fmaf_rn(T[8], p.z, T[10] * -p.x);
+    float b2x = __fmaf_rn(T[0], -p.y, T[1] * p.x), b2y = __fmaf_rn(T[4], -p.y, T[5] * p.x),
+          b2z = __fmaf_rn(T[8], -p.y, T[9] * p.x);
+    float n0x = __fmaf_rn(T[1], -rn.z, T[2] * rn.y), n0y = __fmaf_rn(T[5], -rn.z, T[6] * rn.y),
+          n0z = __fmaf_rn(T[9], -rn.z, T[10] * rn.y);
+    float n1x = __fmaf_rn(T[0], rn.z, T[2] * -rn.x), n1y = __fmaf_rn(T[4], rn.z, T[6] * -rn.x),
+          n1z = __fmaf_rn(T[8], rn.z, T[10] * -rn.x);
+    float n2x = __fmaf_rn(T[0], -rn.y, T[1] * rn.x), n2y = __fmaf_rn(T[4], -rn.y, T[5] * rn.x),
+          n2z = __fmaf_rn(T[8], -rn.y, T[9] * rn.x);
     float so = -optScaleIn * weight;
-    j[0] = so * (-cnx * b0x - cny * b0y - cnz * b0z + rvx * n0x + rvy * n0y + rvz * n0z);
-    j[1] = so * (-cnx * b1x - cny * b1y - cnz * b1z + rvx * n1x + rvy * n1y + rvz * n1z);
-    j[2] = so * (-cnx * b2x - cny * b2y - cnz * b2z + rvx * n2x + rvy * n2y + rvz * n2z);
+    // -cn . b + rv . n, accumulated left to right
+    auto row = [&](float bx, float by, float bz, float nx, float ny, float nz) {
+        float t = -cnx * bx;
+        t = __fmaf_rn(-cny, by, t);
+        t = __fmaf_rn(-cnz, bz, t);
+        t = __fmaf_rn(rvx, nx, t);
+        t = __fmaf_rn(rvy, ny, t);
+        return __fmaf_rn(rvz, nz, t);
+    };
+    j[0] = so * row(b0x, b0y, b0z, n0x, n0y, n0z);
+    j[1] = so * row(b1x, b1y, b1z, n1x, n1y, n1z);
+    j[2] = so * row(b2x, b2y, b2z, n2x, n2y, n2z);
 #pragma unroll
-    for (int c = 0; c < 3; c++) j[3 + c] = -weight * (-cnx * T[c] - cny * T[4 + c] - cnz * T[8 + c]);
+    for (int c = 0; c < 3; c++)
+        j[3 + c] = -weight * __fmaf_rn(-cnz, T[8 + c], __fmaf_rn(-cny, T[4 + c], -cnx * T[c]));
 }
 
 // The arrays the photometric term reads: FP32, or (mixed precision) the FP16
@@ -1402,13 +1424,17 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
 
 
 // The linearisation of one GN iteration at `level`, iteration `it`, for every
-// instance (blockIdx.y).  blockIdx.x 0..7: the photometric cluster of the
-// instance (updateLinearSystem, phototracker.cpp:505-511); blockIdx.x = 8 + j:
-// ICP chunks [j K, (j+1) K) of 1024 pixels, K = icp_per_cta
-// (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).  Every CTA adds
-// its fixed-point sums to the instance's with integer atomics, so the result
-// does not depend on K or on the order in which CTAs finish; k_solve then
-// fuses, solves and updates the pose.
+// instance.  The grid is one row: blocks [0, 8n) are the photometric clusters
+// of the n instances (cluster i = instance i; updateLinearSystem,
+// phototracker.cpp:505-511), then icp_ctas blocks per instance, block j of an
+// instance taking ICP chunks [j K, (j+1) K) of 1024 pixels, K = icp_per_cta
+// (ShapeTracker::updateLinearSystem, shapetracker.cpp:376-381).  The
+// photometric clusters, the longest dependent chains of the iteration
+// (residuals, a cluster-wide histogram, then the weighted sums), come first so
+// that they all start in the first wave and the short ICP CTAs fill in around
+// them.  Every CTA adds its fixed-point sums to the instance's with integer
+// atomics, so the result does not depend on K or on the order in which CTAs
+// finish; k_solve then fuses, solves and updates the pose.
 //
 // Even iterations visit the instances, and the chunks within each, in reverse
 // order (CTAs start roughly in block order): a level-0 pass streams several
@@ -1418,11 +1444,22 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
 #define RECON_ITER_MIN_BLOCKS 4
 #endif
 __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads, RECON_ITER_MIN_BLOCKS)
-    k_iter(const InstDesc *D, int level, int it, int icp_per_cta) {
+    k_iter(const InstDesc *D, int level, int it, int icp_per_cta, int n_inst, int icp_ctas) {
     pdl_trigger();
-    __shared__ InstDesc sd;
     const bool rev = (it & 1) == 0;
-    load_desc(sd, D + (rev ? gridDim.y - 1 - blockIdx.y : blockIdx.y));
+    int slot, role;  // instance slot of the block, and its role within the instance
+    if ((int)blockIdx.x < kCluster * n_inst) {
+        slot = blockIdx.x / kCluster;
+        role = blockIdx.x % kCluster;
+    } else {
+        int j = blockIdx.x - kCluster * n_inst;
+        if (icp_ctas <= 0) return;
+        slot = j / icp_ctas;
+        role = kCluster + j % icp_ctas;
+        if (slot >= n_inst) return;  // rounding of the grid to whole clusters
+    }
+    __shared__ InstDesc sd;
+    load_desc(sd, D + (rev ? n_inst - 1 - slot : slot));
     __syncthreads();
     const InstDesc &d = sd;
     if (level >= d.L) return;
@@ -1434,7 +1471,6 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
     int npix = (d.W >> level) * (d.H >> level);
     int nchunks = (npix + kChunk - 1) / kChunk;
     int nicp = nsel > 0 ? (nchunks + icp_per_cta - 1) / icp_per_cta : 0;
-    int role = blockIdx.x;
     int set;  // which sums this CTA adds to: 0 photometric, 1 ICP
     if (role < kCluster) {
         if (!use_ph) return;

@@ -112,6 +112,7 @@ def lib() -> ctypes.CDLL:
             L.orc_downsample_cloud6.argtypes = [vp, vp, i32, i32, vp, vp]
             L.orc_icp_residual_mask.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, i32, vp, vp]
             L.orc_icp_residual_jacobian.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, i32, vp, vp, vp, f32]
+            L.orc_icp_residual_jacobian_grid.argtypes = [vp, i32, i32, i32, vp, vp, vp, vp, i32, vp, vp, vp, f32]
             L.orc_compact.argtypes = [vp, i32, vp]
             L.orc_compact.restype = i32
             L.orc_generate_weights.restype = i32

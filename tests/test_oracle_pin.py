@@ -230,6 +230,23 @@ def test_icp_stages_match_reference(frame_pair):
                              p(er), p(jr), p(w_o), 1e-3)
         assert np.array_equal(eo.view(np.uint32), er.view(np.uint32)), f"icp residual level {l}"
         assert np.array_equal(jo.view(np.uint32), jr.view(np.uint32)), f"icp jacobian level {l}"
+        # the tracker's form over the pixel grid (fused multiply-adds in the
+        # continuous terms): the same pixels are correspondences, and every
+        # residual and Jacobian entry is within 1e-5 of the reference's,
+        # relative to the largest entry of its column at the level
+        wpx = np.zeros(w * h, np.float32)
+        wpx[sel[:n]] = w_o
+        gpad = ((w * h + 1023) // 1024) * 1024
+        jg, eg = np.zeros(6 * gpad, np.float32), np.zeros(gpad, np.float32)
+        lib.orc_icp_residual_jacobian_grid(p(refs[l][0]), w, h, l, p(T), p(calib), p(curs[l][0]), p(curs[l][1]),
+                                           gpad, p(eg), p(jg), p(wpx), 1e-3)
+        assert np.array_equal(eg[sel[:n]] != 0, er[:n] != 0), f"icp correspondences level {l}"
+        scale = np.abs(er[:n]).max()
+        np.testing.assert_allclose(eg[sel[:n]], er[:n], rtol=0, atol=1e-5 * scale)
+        for c in range(6):
+            col_g = jg[c * gpad:(c + 1) * gpad][sel[:n]]
+            col_r = jr[c * npad:c * npad + n]
+            np.testing.assert_allclose(col_g, col_r, rtol=0, atol=1e-5 * np.abs(col_r).max(), err_msg=f"J{c} l{l}")
 
 
 def test_cg_solver_matches_reference():
