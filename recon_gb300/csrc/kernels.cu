@@ -334,6 +334,36 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
         return;
     }
     float px3 = ((float)xi - cx) * z / fx, py3 = ((float)yi - cy) * z / fy, pz3 = z;
+    // The frames are independent until they are averaged: every frame's
+    // projection and depth tap is issued first, then every colour sample, so
+    // that the gathers of all frames are in flight together; the running means
+    // then add the frames in order.
+    constexpr int kF = 8;
+    float qx[kF], qy[kF], qz[kF], zf[kF], csample[kF];
+    int xd[kF], yd[kF];
+    bool hit[kF];
+#pragma unroll
+    for (int f = 0; f < kF; f++) {
+        hit[f] = false;
+        zf[f] = 0.0f;
+        if (f >= nframes) continue;
+        mul4(sT[f], px3, py3, pz3, qx[f], qy[f], qz[f]);
+        float q2x = qx[f] / qz[f], q2y = qy[f] / qz[f];
+        float pxl = KL[0] * q2x + KL[1] * q2y + KL[2];
+        float pyl = KL[3] * q2x + KL[4] * q2y + KL[5];
+        xd[f] = ftoi(pxl + 0.5f);
+        yd[f] = ftoi(pyl + 0.5f);
+        if (xd[f] < 0 || yd[f] < 0 || xd[f] >= W || yd[f] >= H) continue;
+        uint16_t dm = __ldg(depth[(size_t)f * n_inst + blockIdx.y] + xd[f] + yd[f] * W);
+        zf[f] = dm ? -(float)dm : 0.0f;
+        hit[f] = true;
+    }
+    if (colour) {
+#pragma unroll
+        for (int f = 0; f < kF; f++)
+            csample[f] = hit[f] ? rgb_sample(d.calib, qx[f], qy[f], qz[f], gray[(size_t)f * n_inst + blockIdx.y], W, H)
+                                : -1.0f;
+    }
     float zsum = z, wsum = 1.0f;
     float csum = 0.0f, cw = 0.0f;
     if (colour) {
@@ -343,30 +373,20 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
             cw = 1.0f;
         }
     }
-    for (int f = 0; f < nframes && f < 8; f++) {
-        float qx, qy, qz;
-        mul4(sT[f], px3, py3, pz3, qx, qy, qz);
-        float q2x = qx / qz, q2y = qy / qz;
-        float pxl = KL[0] * q2x + KL[1] * q2y + KL[2];
-        float pyl = KL[3] * q2x + KL[4] * q2y + KL[5];
-        int xd = ftoi(pxl + 0.5f), yd = ftoi(pyl + 0.5f);
-        if (xd < 0 || yd < 0 || xd >= W || yd >= H) continue;
-        uint16_t dm = depth[(size_t)f * n_inst + blockIdx.y][xd + yd * W];
-        float zf = dm ? -(float)dm : 0.0f;
-        if (!(zf < -minDist && zf > -maxDist)) continue;
-        float mx = ((float)xd - cx) * zf / fx, my = ((float)yd - cy) * zf / fy, mz = zf;
+#pragma unroll
+    for (int f = 0; f < kF; f++) {
+        if (!hit[f]) continue;
+        if (!(zf[f] < -minDist && zf[f] > -maxDist)) continue;
+        float mx = ((float)xd[f] - cx) * zf[f] / fx, my = ((float)yd[f] - cy) * zf[f] / fy, mz = zf[f];
         float kx, ky, kz;
         mul4(sTi[f], mx, my, mz, kx, ky, kz);
         float dz = kz - z;
         if (fabsf(dz) < gate) {
             zsum += kz;
             wsum += 1.0f;
-            if (colour) {
-                float c = rgb_sample(d.calib, qx, qy, qz, gray[(size_t)f * n_inst + blockIdx.y], W, H);
-                if (c >= 0.0f) {
-                    csum += c;
-                    cw += 1.0f;
-                }
+            if (colour && csample[f] >= 0.0f) {
+                csum += csample[f];
+                cw += 1.0f;
             }
         }
     }
@@ -1269,12 +1289,40 @@ __device__ bool photo_cluster(const InstDesc &d, IterShared &sh, int level, int 
     return rank < nph;
 }
 
+// L2 prefetch of [p, p + bytes) (cp.async.bulk.prefetch.L2: a 16-byte aligned
+// global address and a multiple of 16 bytes; a smaller tail is left out).  A
+// prefetch changes no value anywhere, it only brings lines into L2 early.
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+    bytes &= ~15u;
+    if (bytes == 0) return;
+    unsigned long long g;
+    asm("cvta.to.global.u64 %0, %1;\n" : "=l"(g) : "l"(p));
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(g), "r"(bytes) : "memory");
+}
+
+// Prefetches what ICP chunk c of the level reads: its reference points,
+// normals and weights (contiguous streams) and the rows of the current point
+// cloud that its bilinear taps read at small motion (the chunk's own rows and
+// the one below).  Issued by one thread, a chunk ahead of its use.
+__device__ __forceinline__ void icp_prefetch_chunk(const InstDesc &d, int level, int c, int npix) {
+    int i0 = c * kChunk;
+    if (c < 0 || i0 >= npix) return;
+    int n = min(kChunk, npix - i0);
+    prefetch_l2(d.ref_pts[level] + i0, (unsigned)n * 16u);
+    prefetch_l2(d.ref_nrm[level] + i0, (unsigned)n * 16u);
+    prefetch_l2(d.icp_w + i0, (unsigned)n * 4u);
+    int w = d.W >> level, h = d.H >> level;
+    int y0 = i0 / w, y1 = min((i0 + n - 1) / w + 1, h - 1);
+    prefetch_l2(d.cur_pts[level] + (size_t)y0 * w, (unsigned)((y1 - y0 + 1) * w) * 16u);
+}
+
 // ICP chunks [c0, c1) of 1024 pixels of the level: lane t evaluates pixels
 // t + 256m of each chunk (icpResidualIndexKernel2 and the reference's per-point
 // Jacobian), the warp totals of each chunk go into the CTA's fixed-point sums.
 __device__ void icp_chunks(const InstDesc &d, IterShared &sh, int level, int c0, int c1, int npix) {
     int t = threadIdx.x, lane = t & 31;
     for (int c = c0; c < c1; c++) {
+        if (t == 0 && c + 1 < c1) icp_prefetch_chunk(d, level, c + 1, npix);
         // Phase 1: the lane's four pixels with no accumulators live; each
         // result goes to the lane's own shared slots.
 #pragma unroll
@@ -1464,6 +1512,13 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
     const InstDesc &d = sd;
     if (level >= d.L) return;
     if (it >= d.iters[d.L - 1 - level]) return;
+    if (role >= kCluster && threadIdx.x == 0 && d.mode != RECON_PHOTOMETRIC) {
+        // the first chunk's inputs, while the previous kernel finishes
+        int np = (d.W >> level) * (d.H >> level);
+        int nall = ((np + kChunk - 1) / kChunk + icp_per_cta - 1) / icp_per_cta;
+        int jj = role - kCluster;
+        if (jj < nall) icp_prefetch_chunk(d, level, (rev ? nall - 1 - jj : jj) * icp_per_cta, np);
+    }
     pdl_wait();
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
