@@ -334,36 +334,6 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
         return;
     }
     float px3 = ((float)xi - cx) * z / fx, py3 = ((float)yi - cy) * z / fy, pz3 = z;
-    // The frames are independent until they are averaged: every frame's
-    // projection and depth tap is issued first, then every colour sample, so
-    // that the gathers of all frames are in flight together; the running means
-    // then add the frames in order.
-    constexpr int kF = 8;
-    float qx[kF], qy[kF], qz[kF], zf[kF], csample[kF];
-    int xd[kF], yd[kF];
-    bool hit[kF];
-#pragma unroll
-    for (int f = 0; f < kF; f++) {
-        hit[f] = false;
-        zf[f] = 0.0f;
-        if (f >= nframes) continue;
-        mul4(sT[f], px3, py3, pz3, qx[f], qy[f], qz[f]);
-        float q2x = qx[f] / qz[f], q2y = qy[f] / qz[f];
-        float pxl = KL[0] * q2x + KL[1] * q2y + KL[2];
-        float pyl = KL[3] * q2x + KL[4] * q2y + KL[5];
-        xd[f] = ftoi(pxl + 0.5f);
-        yd[f] = ftoi(pyl + 0.5f);
-        if (xd[f] < 0 || yd[f] < 0 || xd[f] >= W || yd[f] >= H) continue;
-        uint16_t dm = __ldg(depth[(size_t)f * n_inst + blockIdx.y] + xd[f] + yd[f] * W);
-        zf[f] = dm ? -(float)dm : 0.0f;
-        hit[f] = true;
-    }
-    if (colour) {
-#pragma unroll
-        for (int f = 0; f < kF; f++)
-            csample[f] = hit[f] ? rgb_sample(d.calib, qx[f], qy[f], qz[f], gray[(size_t)f * n_inst + blockIdx.y], W, H)
-                                : -1.0f;
-    }
     float zsum = z, wsum = 1.0f;
     float csum = 0.0f, cw = 0.0f;
     if (colour) {
@@ -373,20 +343,30 @@ __global__ void k_fuse_depth(const InstDesc *D, int nframes, int n_inst, const u
             cw = 1.0f;
         }
     }
-#pragma unroll
-    for (int f = 0; f < kF; f++) {
-        if (!hit[f]) continue;
-        if (!(zf[f] < -minDist && zf[f] > -maxDist)) continue;
-        float mx = ((float)xd[f] - cx) * zf[f] / fx, my = ((float)yd[f] - cy) * zf[f] / fy, mz = zf[f];
+    for (int f = 0; f < nframes && f < 8; f++) {
+        float qx, qy, qz;
+        mul4(sT[f], px3, py3, pz3, qx, qy, qz);
+        float q2x = qx / qz, q2y = qy / qz;
+        float pxl = KL[0] * q2x + KL[1] * q2y + KL[2];
+        float pyl = KL[3] * q2x + KL[4] * q2y + KL[5];
+        int xd = ftoi(pxl + 0.5f), yd = ftoi(pyl + 0.5f);
+        if (xd < 0 || yd < 0 || xd >= W || yd >= H) continue;
+        uint16_t dm = depth[(size_t)f * n_inst + blockIdx.y][xd + yd * W];
+        float zf = dm ? -(float)dm : 0.0f;
+        if (!(zf < -minDist && zf > -maxDist)) continue;
+        float mx = ((float)xd - cx) * zf / fx, my = ((float)yd - cy) * zf / fy, mz = zf;
         float kx, ky, kz;
         mul4(sTi[f], mx, my, mz, kx, ky, kz);
         float dz = kz - z;
         if (fabsf(dz) < gate) {
             zsum += kz;
             wsum += 1.0f;
-            if (colour && csample[f] >= 0.0f) {
-                csum += csample[f];
-                cw += 1.0f;
+            if (colour) {
+                float c = rgb_sample(d.calib, qx, qy, qz, gray[(size_t)f * n_inst + blockIdx.y], W, H);
+                if (c >= 0.0f) {
+                    csum += c;
+                    cw += 1.0f;
+                }
             }
         }
     }
