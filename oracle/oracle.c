@@ -1141,7 +1141,7 @@ int orc_solve_cholesky(const double A[36], const double b[6], double x[6]) {
         double sv[6];
         for (int i = j; i < 6; i++) {
             double v = A[i * 6 + j];
-            for (int k = 0; k < j; k++) v = v - L[i * 6 + k] * U[j * 6 + k];
+            for (int k = 0; k < j; k++) v = fma(-L[i * 6 + k], U[j * 6 + k], v);
             sv[i] = v;
         }
         if (!(sv[j] > 0.0)) {
@@ -1157,10 +1157,10 @@ int orc_solve_cholesky(const double A[36], const double b[6], double x[6]) {
     double z[6];
     for (int i = 0; i < 6; i++) z[i] = b[i];
     for (int k = 0; k < 6; k++)
-        for (int i = k + 1; i < 6; i++) z[i] = z[i] - L[i * 6 + k] * z[k];
+        for (int i = k + 1; i < 6; i++) z[i] = fma(-L[i * 6 + k], z[k], z[i]);
     for (int i = 0; i < 6; i++) z[i] = z[i] * inv[i];
     for (int k = 5; k >= 0; k--)
-        for (int i = 0; i < k; i++) z[i] = z[i] - L[k * 6 + i] * z[k];
+        for (int i = 0; i < k; i++) z[i] = fma(-L[k * 6 + i], z[k], z[i]);
     for (int i = 0; i < 6; i++) x[i] = z[i];
     return 0;
 }
@@ -1203,8 +1203,9 @@ static void mat4d(const double *M1, const double *M2, double *R) {
     double t[16];
     for (int r = 0; r < 4; r++)
         for (int c = 0; c < 4; c++)
-            t[r * 4 + c] = M1[r * 4 + 0] * M2[0 * 4 + c] + M1[r * 4 + 1] * M2[1 * 4 + c] +
-                           M1[r * 4 + 2] * M2[2 * 4 + c] + M1[r * 4 + 3] * M2[3 * 4 + c];
+            t[r * 4 + c] = fma(M1[r * 4 + 3], M2[3 * 4 + c],
+                               fma(M1[r * 4 + 2], M2[2 * 4 + c], fma(M1[r * 4 + 1], M2[1 * 4 + c],
+                                                                     M1[r * 4 + 0] * M2[0 * 4 + c])));
     memcpy(R, t, sizeof(t));
 }
 
@@ -1215,23 +1216,23 @@ static void normalize_mat4_safe(double *T) {
     double u[3] = {T[0], T[4], T[8]};
     double v[3] = {T[1], T[5], T[9]};
     double w[3] = {T[2], T[6], T[10]};
-    double lenU = (double)sqrtf((float)(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
-    double lenW = (double)sqrtf((float)(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]));
+    double lenU = (double)sqrtf((float)fma(u[2], u[2], fma(u[1], u[1], u[0] * u[0])));
+    double lenW = (double)sqrtf((float)fma(w[2], w[2], fma(w[1], w[1], w[0] * w[0])));
     if (lenW > 1e-8f) {
         double iw = 1.0 / lenW;
         w[0] = w[0] * iw; w[1] = w[1] * iw; w[2] = w[2] * iw;
     } else { w[0] = 0; w[1] = 0; w[2] = 1; }
     /* crossproductReal(v, w, u), expmCuda.cu:1934-1938 */
-    u[0] = v[1] * w[2] - v[2] * w[1];
-    u[1] = -(v[0] * w[2] - v[2] * w[0]);
-    u[2] = v[0] * w[1] - v[1] * w[0];
+    u[0] = fma(v[1], w[2], -(v[2] * w[1]));
+    u[1] = -fma(v[0], w[2], -(v[2] * w[0]));
+    u[2] = fma(v[0], w[1], -(v[1] * w[0]));
     if (lenU > 1e-8f) {
         double iu = 1.0 / lenU;
         u[0] = u[0] * iu; u[1] = u[1] * iu; u[2] = u[2] * iu;
     } else { u[0] = 1; u[1] = 0; u[2] = 0; }
-    v[0] = w[1] * u[2] - w[2] * u[1];
-    v[1] = -(w[0] * u[2] - w[2] * u[0]);
-    v[2] = w[0] * u[1] - w[1] * u[0];
+    v[0] = fma(w[1], u[2], -(w[2] * u[1]));
+    v[1] = -fma(w[0], u[2], -(w[2] * u[0]));
+    v[2] = fma(w[0], u[1], -(w[1] * u[0]));
     T[0] = u[0]; T[4] = u[1]; T[8] = u[2];
     T[1] = v[0]; T[5] = v[1]; T[9] = v[2];
     T[2] = w[0]; T[6] = w[1]; T[10] = w[2];
@@ -1274,14 +1275,14 @@ static int solve4(double *D, double *N) {
         inv[k] = 1.0 / D[k * 4 + k];
         for (int i = k + 1; i < 3; i++) {
             double f = D[i * 4 + k] * inv[k];
-            for (int c = k + 1; c < 4; c++) D[i * 4 + c] = D[i * 4 + c] - f * D[k * 4 + c];
-            for (int c = 0; c < 4; c++) N[i * 4 + c] = N[i * 4 + c] - f * N[k * 4 + c];
+            for (int c = k + 1; c < 4; c++) D[i * 4 + c] = fma(-f, D[k * 4 + c], D[i * 4 + c]);
+            for (int c = 0; c < 4; c++) N[i * 4 + c] = fma(-f, N[k * 4 + c], N[i * 4 + c]);
         }
     }
     for (int k = 3; k >= 1; k--) {
         for (int c = 0; c < 4; c++) {
             double xk = N[k * 4 + c];
-            for (int i = 0; i < k; i++) N[i * 4 + c] = N[i * 4 + c] - D[i * 4 + k] * xk;
+            for (int i = 0; i < k; i++) N[i * 4 + c] = fma(-D[i * 4 + k], xk, N[i * 4 + c]);
         }
         for (int c = 0; c < 4; c++) N[(k - 1) * 4 + c] = N[(k - 1) * 4 + c] * inv[k - 1];
     }
@@ -1313,8 +1314,8 @@ void orc_expm_twist(const double A[16], double E[16]) {
     double U0[16], U[16], V[16];
     for (int i = 0; i < 16; i++) {
         double I = (i % 5 == 0) ? 1.0 : 0.0;
-        U0[i] = ((c[1] * I + c[3] * X2[i]) + c[5] * X4[i]) + 0.0 * X6[i];
-        V[i] = ((c[0] * I + c[2] * X2[i]) + c[4] * X4[i]) + c[6] * X6[i];
+        U0[i] = fma(0.0, X6[i], fma(c[5], X4[i], fma(c[3], X2[i], c[1] * I)));
+        V[i] = fma(c[6], X6[i], fma(c[4], X4[i], fma(c[2], X2[i], c[0] * I)));
     }
     mat4d(X, U0, U);
     double Nm[16], Dm[16];
@@ -1361,8 +1362,8 @@ void orc_linear_fuse(double A1[36], double b1[6], double w1, int N1, const doubl
                      double w2, int N2) {
     double c1 = w1 / (double)N1;
     double c2 = w2 / (double)N2;
-    for (int i = 0; i < 36; i++) A1[i] = c1 * A1[i] + c2 * A2[i];
-    for (int i = 0; i < 6; i++) b1[i] = c1 * b1[i] + c2 * b2[i];
+    for (int i = 0; i < 36; i++) A1[i] = fma(c1, A1[i], c2 * A2[i]);
+    for (int i = 0; i < 6; i++) b1[i] = fma(c1, b1[i], c2 * b2[i]);
 }
 
 /* ------------------------------------------------------------------ */

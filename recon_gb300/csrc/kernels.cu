@@ -1400,7 +1400,7 @@ __device__ __noinline__ void finalize_iter(const InstDesc &d, SolveShared &sh, i
         double v;
         if (d.mode == RECON_PHOTOMETRIC) v = aph;
         else if (d.mode == RECON_GEOMETRIC) v = aic;
-        else v = ok ? d.fuse_c1 * aph + sh.fuse_c2 * aic : aph;  // (1-lambda)/P * photo + lambda/N * icp
+        else v = ok ? __fma_rn(d.fuse_c1, aph, sh.fuse_c2 * aic) : aph;  // (1-lambda)/P * photo + lambda/N * icp
         if (t < 36) S.A[t] = v;
         else S.b[t - 36] = v;
         if (tr) {

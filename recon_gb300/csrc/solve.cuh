@@ -6,9 +6,10 @@
 // On GB300 an FP64 warp instruction occupies its SM sub-partition for about 64
 // cycles whether or not it depends on the previous one, and a divide or square
 // root costs about ten of them.  The layout below therefore keeps the serial
-// FP64 chain short: one reciprocal per pivot instead of a divide per element,
-// lane-parallel substitutions, and comparisons of magnitudes on the integer
-// bit patterns instead of FP64 compares.
+// FP64 chain short: every product added to a sum is one fused multiply-add
+// (the oracle's fma, one rounding), one reciprocal per pivot instead of a
+// divide per element, lane-parallel substitutions, and comparisons of
+// magnitudes on the integer bit patterns instead of FP64 compares.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -35,13 +36,16 @@ __device__ __constant__ const double kPade[7] = {0x1.0000000000000p+0, 0x1.00000
 __device__ __forceinline__ long long abs_bits(double v) { return __double_as_longlong(v) & 0x7fffffffffffffffLL; }
 constexpr long long kInfBits = 0x7ff0000000000000LL;
 
-// 4x4 product R = M1 * M2 (matrixMult4Real, expmCuda.cu:1894-1917); R may alias.
+// 4x4 product R = M1 * M2 (matrixMult4Real, expmCuda.cu:1894-1917), each entry
+// the first product then three fused multiply-adds; R may alias.
 __device__ __forceinline__ void wmat4(const double *M1, const double *M2, double *R, int lane) {
     double t = 0.0;
     if (lane < 16) {
         int r = lane >> 2, c = lane & 3;
-        t = M1[r * 4 + 0] * M2[0 * 4 + c] + M1[r * 4 + 1] * M2[1 * 4 + c] + M1[r * 4 + 2] * M2[2 * 4 + c] +
-            M1[r * 4 + 3] * M2[3 * 4 + c];
+        t = M1[r * 4 + 0] * M2[0 * 4 + c];
+        t = __fma_rn(M1[r * 4 + 1], M2[1 * 4 + c], t);
+        t = __fma_rn(M1[r * 4 + 2], M2[2 * 4 + c], t);
+        t = __fma_rn(M1[r * 4 + 3], M2[3 * 4 + c], t);
     }
     __syncwarp();
     if (lane < 16) R[lane] = t;
@@ -56,7 +60,7 @@ __device__ __forceinline__ void wnormalize(double *T, int lane) {
     if (lane < 2) {
         int c = lane ? 2 : 0;
         double a = T[c], b = T[4 + c], e = T[8 + c];
-        len = (double)sqrtf((float)(a * a + b * b + e * e));
+        len = (double)sqrtf((float)__fma_rn(e, e, __fma_rn(b, b, a * a)));
     }
     double lenU = __shfl_sync(kFull, len, 0), lenW = __shfl_sync(kFull, len, 1);
     bool okU = lenU > 1e-8f, okW = lenW > 1e-8f;
@@ -70,11 +74,11 @@ __device__ __forceinline__ void wnormalize(double *T, int lane) {
     int ia = (i == 0) ? 1 : 0, ib = (i == 2) ? 1 : 2;
     double w_a = __shfl_sync(kFull, wi, ia), w_b = __shfl_sync(kFull, wi, ib);
     double v_a = __shfl_sync(kFull, vi, ia), v_b = __shfl_sync(kFull, vi, ib);
-    double r = v_a * w_b - v_b * w_a;
+    double r = __fma_rn(v_a, w_b, -(v_b * w_a));
     double ui = (i == 1) ? -r : r;
     ui = okU ? ui * iu : (i == 0 ? 1.0 : 0.0);
     double u_a = __shfl_sync(kFull, ui, ia), u_b = __shfl_sync(kFull, ui, ib);
-    double r2 = w_a * u_b - w_b * u_a;
+    double r2 = __fma_rn(w_a, u_b, -(w_b * u_a));
     double vn = (i == 1) ? -r2 : r2;
     __syncwarp();
     if (lane < 3) {
@@ -131,7 +135,7 @@ static __device__ void wexpm_twist(SolveScratch &S, const double *A, int lane) {
         double ca = isV ? kPade[0] : kPade[1], cb = isV ? kPade[2] : kPade[3];
         double cc = isV ? kPade[4] : kPade[5], cd = isV ? kPade[6] : 0.0;
         double I = (e % 5 == 0) ? 1.0 : 0.0;
-        double o = ((ca * I + cb * X2[e]) + cc * X4[e]) + cd * X6[e];
+        double o = __fma_rn(cd, X6[e], __fma_rn(cc, X4[e], __fma_rn(cb, X2[e], ca * I)));
         (isV ? V : U0)[e] = o;
     }
     __syncwarp();
@@ -179,8 +183,8 @@ static __device__ void wexpm_twist(SolveScratch &S, const double *A, int lane) {
         bool act = (row > k && row < 3) && (col >= 4 || col >= k + 1);
         if (act) {
             double f = Dm[row * 4 + k] * inv;
-            if (col < 4) nv = Dm[row * 4 + col] - f * Dm[k * 4 + col];
-            else nv = Nm[row * 4 + col - 4] - f * Nm[k * 4 + col - 4];
+            if (col < 4) nv = __fma_rn(-f, Dm[k * 4 + col], Dm[row * 4 + col]);
+            else nv = __fma_rn(-f, Nm[k * 4 + col - 4], Nm[row * 4 + col - 4]);
         }
         __syncwarp();
         if (act) {
@@ -195,7 +199,7 @@ static __device__ void wexpm_twist(SolveScratch &S, const double *A, int lane) {
     for (int k = 3; k >= 1; k--) {
         double nv = 0.0;
         bool act = (col >= 4) && (row < k);
-        if (act) nv = Nm[row * 4 + c] - Dm[row * 4 + k] * Nm[k * 4 + c];
+        if (act) nv = __fma_rn(-Dm[row * 4 + k], Nm[k * 4 + c], Nm[row * 4 + c]);
         __syncwarp();
         if (act) Nm[row * 4 + c] = nv;
         __syncwarp();
@@ -259,7 +263,7 @@ static __device__ int wcholesky(SolveScratch &S, int lane) {
         double v = 0.0;
         if (i >= j && i < 6) {
             v = A[i * 6 + j];
-            for (int k = 0; k < j; k++) v = v - L[i * 6 + k] * U[j * 6 + k];
+            for (int k = 0; k < j; k++) v = __fma_rn(-L[i * 6 + k], U[j * 6 + k], v);
         }
         double dj = __shfl_sync(kFull, v, j);
         if (!(dj > 0.0)) return -1;
@@ -274,12 +278,12 @@ static __device__ int wcholesky(SolveScratch &S, int lane) {
     double z = (i < 6) ? S.b[i] : 0.0;
     for (int k = 0; k < 6; k++) {
         double zk = __shfl_sync(kFull, z, k);
-        if (i > k && i < 6) z = z - L[i * 6 + k] * zk;
+        if (i > k && i < 6) z = __fma_rn(-L[i * 6 + k], zk, z);
     }
     if (i < 6) z = z * S.inv[i];
     for (int k = 5; k >= 0; k--) {
         double zk = __shfl_sync(kFull, z, k);
-        if (i < k) z = z - L[k * 6 + i] * zk;
+        if (i < k) z = __fma_rn(-L[k * 6 + i], zk, z);
     }
     if (i < 6) S.x[i] = z;
     __syncwarp();
