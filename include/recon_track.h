@@ -201,10 +201,10 @@ int recon_batch_get_trace(recon_batch *b, int32_t inst, recon_iter_trace *out, i
 
 /* Measurement hooks (used by the benchmark).  Timing brackets every launch of
  * the schedule with CUDA events on the batch's stream; totals per kernel kind
- * (0 GN iteration: linearisation, solve and pose update, 1 ICP mask, 2
- * Student-t passes, 3 current-frame preparation, 4 reference preparation, 5
- * ICP preparation of a small level in one launch, 6 keyframe fusion)
- * accumulate in
+ * (0 GN iteration linearisation, 1 ICP mask, 2 Student-t passes, 3
+ * current-frame preparation, 4 reference preparation, 5 GN iteration solve and
+ * pose update, 6 ICP preparation of a small level in one launch, 7 keyframe
+ * fusion) accumulate in
  * recon_batch_get_poses and are read with recon_batch_get_timing.  Work
  * counters: per instance [photometric point-iterations, ICP point-iterations,
  * ICP mask pixels, 0]. */

@@ -450,8 +450,8 @@ class Batch:
         return out[: n // out.itemsize]
 
 
-TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_student_t", "prep_current", "prep_reference", "icp_prepare",
-                "keyframe_fusion"]
+TIMING_KINDS = ["gn_iteration", "icp_mask", "icp_student_t", "prep_current", "prep_reference", "gn_solve",
+                "icp_prepare", "keyframe_fusion"]
 
 
 def launch_count() -> int:

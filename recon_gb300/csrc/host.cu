@@ -37,6 +37,7 @@ __global__ void k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *
 __global__ void k_icp_student3(const InstDesc *D, int level);
 __global__ void k_icp_prepare(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta, int n_inst, int icp_ctas);
+__global__ void k_solve(const InstDesc *D, int level, int it);
 __global__ void k_render_depth(recon_scene sc, recon_camera cam, float noise_rel, uint32_t seed, uint32_t frame,
                                uint16_t *out);
 __global__ void k_render_gray(recon_scene sc, recon_camera cam, uint8_t *out);
@@ -341,7 +342,7 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
 dim3 grid_pix(int pix, int n, int block = 256) { return dim3((pix + block - 1) / block, n, 1); }
 
 enum TimingKind {
-    TK_ITER = 0, TK_ICP_MASK, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_ICP_PREP, TK_FUSE, TK_COUNT
+    TK_ITER = 0, TK_ICP_MASK, TK_ICP_STUDENT, TK_PREP_CUR, TK_PREP_REF, TK_SOLVE, TK_ICP_PREP, TK_FUSE, TK_COUNT
 };
 static_assert(TK_COUNT <= 8, "timing slots");
 
@@ -532,7 +533,11 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
                 TimedScope ts(b, s, TK_ITER, in_graph);
                 CK(launch_pdl(k_iter, dim3(gx, 1), dim3(kIterBlock), s, D, level, it, per_cta, n, ncta));
             }
-            b->graph_kernels += 1;
+            {
+                TimedScope ts(b, s, TK_SOLVE, in_graph);
+                CK(launch_pdl(k_solve, dim3(n), dim3(kSolveThreads), s, D, level, it));
+            }
+            b->graph_kernels += 2;
         }
     }
     CK(cudaGetLastError());
@@ -729,7 +734,7 @@ __global__ void k_begin_track(const InstDesc *D, const float *T_init, int have_i
     if (have_init && t < 16) d.T[t] = T_init[16 * blockIdx.y + t];
     if (t < ST_COUNT) d.stats[t] = 0;
     if (t == 0) {
-        d.counter[0] = d.counter[1] = 0u;
+        *d.counter = 0u;
         if (d.trace_count) *d.trace_count = 0;
     }
     for (int k = t; k < 2 * 27 * kFxLimbs; k += blockDim.x) d.fx[k] = 0ull;

@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256) k_prep_current_pyramid(const InstDesc *D,
         if (begin) {
             if (t < ST_COUNT) d.stats[t] = 0;
             if (t == 0) {
-                d.counter[0] = d.counter[1] = 0u;
+                *d.counter = 0u;
                 if (d.trace_count) *d.trace_count = 0;
             }
             for (int k = t; k < 2 * 27 * kFxLimbs; k += blockDim.x) d.fx[k] = 0ull;
@@ -1351,7 +1351,7 @@ __device__ __forceinline__ int packed_index(int r, int c) {
 // the optional trace.  Every global value it reads is loaded in one round trip
 // at the start (threads 54..63 fetch the scalars), since the FP64 solve that
 // follows is a long serial chain.
-__device__ __noinline__ void finalize_iter(const InstDesc &d, SolveShared &sh, int level, int it, bool use_ph,
+__device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh, int level, int it, bool use_ph,
                                               bool use_icp) {
     int t = threadIdx.x;
     SolveScratch &S = sh.S;
@@ -1462,8 +1462,7 @@ __device__ __noinline__ void finalize_iter(const InstDesc &d, SolveShared &sh, i
 // that they all start in the first wave and the short ICP CTAs fill in around
 // them.  Every CTA adds its fixed-point sums to the instance's with integer
 // atomics, so the result does not depend on K or on the order in which CTAs
-// finish; the instance's last CTA to finish then fuses, solves and updates
-// the pose.
+// finish; k_solve then fuses, solves and updates the pose.
 //
 // Even iterations visit the instances, and the chunks within each, in reverse
 // order (CTAs start roughly in block order): a level-0 pass streams several
@@ -1507,48 +1506,48 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
     int npix = (d.W >> level) * (d.H >> level);
     int nchunks = (npix + kChunk - 1) / kChunk;
     int nicp = nsel > 0 ? (nchunks + icp_per_cta - 1) / icp_per_cta : 0;
-    int set = -1;  // which sums this CTA adds to: 0 photometric, 1 ICP, -1 none
+    int set;  // which sums this CTA adds to: 0 photometric, 1 ICP
     if (role < kCluster) {
-        if (use_ph) set = 0;
+        if (!use_ph) return;
+        set = 0;
     } else {
-        if (role - kCluster < nicp) set = 1;
+        if (role - kCluster >= nicp) return;
+        set = 1;
     }
-    // the iteration's scratch, and afterwards the solve's in the same memory
-    __shared__ union IterSolveShared {
-        IterShared it;
-        SolveShared so;
-    } u;
-    IterShared &sh = u.it;
-    if (set >= 0) {
-        if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
-        fx_clear(sh);
-        __syncthreads();
-        bool had = true;
-        if (set == 0) {
-            had = d.precision == RECON_PRECISION_MIXED ? photo_cluster<true>(d, sh, level, role)
-                                                       : photo_cluster<false>(d, sh, level, role);
-        } else {
-            int j = role - kCluster;
-            int c0 = (rev ? nicp - 1 - j : j) * icp_per_cta;
-            icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), npix);
-        }
-        __syncthreads();
-        if (had) fx_flush(sh, d.fx + set * kFxTerms, d.fx_bad + set);
+    __shared__ IterShared sh;
+    if (threadIdx.x < 16) sh.T[threadIdx.x] = __ldcg(d.T + threadIdx.x);
+    fx_clear(sh);
+    __syncthreads();
+    if (set == 0) {
+        bool had = d.precision == RECON_PRECISION_MIXED ? photo_cluster<true>(d, sh, level, role)
+                                                        : photo_cluster<false>(d, sh, level, role);
+        if (!had) return;
+    } else {
+        int j = role - kCluster;
+        int c0 = (rev ? nicp - 1 - j : j) * icp_per_cta;
+        icp_chunks(d, sh, level, c0, min(c0 + icp_per_cta, nchunks), npix);
     }
-    // Every CTA of the instance (8 + icp_ctas, with or without work) takes a
-    // ticket once its sums are in; the last one completes the iteration: the
-    // normal equations from the sums, fusion, solve and SE(3) update
-    // (estimateIncrement, phototracker.cpp:646-664; linearFuse,
-    // shapetracker.cpp:392-394), while other instances' CTAs still stream.
-    __shared__ bool s_last;
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(d.counter + 1, 1u) == (unsigned int)(kCluster + icp_ctas - 1);
+    fx_flush(sh, d.fx + set * kFxTerms, d.fx_bad + set);
+}
+
+// The rest of a GN iteration, one CTA per instance after k_iter: the normal
+// equations from the fixed-point sums, fusion, solve and SE(3) update
+// (estimateIncrement, phototracker.cpp:646-664; linearFuse,
+// shapetracker.cpp:392-394).
+__global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int level, int it) {
+    pdl_trigger();
+    __shared__ InstDesc sd;
+    load_desc(sd, D + blockIdx.x);
     __syncthreads();
-    if (!s_last) return;
-    __threadfence();  // every other CTA's sums are visible
-    if (threadIdx.x == 0) d.counter[1] = 0u;
-    finalize_iter(d, u.so, level, it, use_ph, use_icp);
+    const InstDesc &d = sd;
+    if (level >= d.L) return;
+    if (it >= d.iters[d.L - 1 - level]) return;
+    pdl_wait();
+    bool use_ph = d.mode != RECON_GEOMETRIC;
+    bool use_icp = d.mode != RECON_PHOTOMETRIC;
+    __shared__ SolveShared sh;
+    finalize_iter(d, sh, level, it, use_ph, use_icp);
 }
 
 // The three Student-t passes of a level in one launch (updateWeightsKernel /

@@ -18,6 +18,7 @@ constexpr int kVtxPlanes = 9;    // x y z px py gx gy gmag gray
 constexpr int kIterCluster = 8;  // CTAs of the photometric cluster of the GN iteration kernel
 constexpr int kIterBlock = 256;  // threads of a GN iteration CTA
 constexpr int kIterCtaSlots = 4 * 152;  // GN iteration CTAs resident on a 152-SM GB300
+constexpr int kSolveThreads = 64;        // threads of the per-instance solve CTA
 constexpr int kFxLimbs = 4;      // limbs of a fixed-point sum (fx.cuh)
 constexpr int kNetW = 80, kNetH = 60;  // coarse image of the learned initialisation
 
@@ -69,7 +70,7 @@ struct InstDesc {
     unsigned long long *fx;
     int *fx_bad;             // 2: an accumulated value was out of range
     unsigned long long *work; // [0] photometric point-iterations, [1] ICP point-iterations, [2] ICP mask pixels
-    unsigned int *counter;   // [1]: CTAs of the current GN iteration that finished (k_iter's ticket)
+    unsigned int *counter;
     float *T;                // 16, device pose (reference IR -> current IR)
     int *stats;              // ST_COUNT
     recon_iter_trace *trace;
