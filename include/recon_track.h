@@ -27,7 +27,7 @@ extern "C" {
 #define RECON_ERR_INVALID_ARG -1
 #define RECON_ERR_NOT_ENOUGH_POINTS -2 /* shapetracker.cpp:365 "not enough points" */
 #define RECON_ERR_NON_SPD -3           /* a Cholesky pivot was not positive; pose kept */
-#define RECON_ERR_TIMEOUT -4
+#define RECON_ERR_TIMEOUT -4           /* reserved: no kernel of this library waits on a flag */
 #define RECON_ERR_CUDA -5
 #define RECON_ERR_STATE -6             /* reference or current frame missing */
 #define RECON_ERR_NO_DEVICE -7
@@ -62,7 +62,9 @@ typedef struct recon_config {
 } recon_config;
 
 typedef struct recon_track_stats {
-    int32_t status;                   /* RECON_OK or the first error of the frame */
+    int32_t status;                   /* RECON_OK; RECON_ERR_NON_SPD if a solve was rejected; else
+                                         RECON_ERR_NOT_ENOUGH_POINTS if an iteration was skipped for
+                                         lack of ICP correspondences (the pose is kept in both cases) */
     int32_t iterations;               /* GN iterations executed */
     int32_t solves;                   /* iterations that updated the pose */
     int32_t icp_selected[RECON_MAX_LEVELS]; /* valid ICP correspondences per level (0 if unused) */

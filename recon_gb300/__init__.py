@@ -19,6 +19,9 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "librecon_track.so")
 
 GEOMETRIC, PHOTOMETRIC, BIOBJECTIVE = 0, 1, 2
+# status codes (include/recon_track.h)
+OK, ERR_INVALID_ARG, ERR_NOT_ENOUGH_POINTS, ERR_NON_SPD, ERR_TIMEOUT, ERR_CUDA, ERR_STATE, ERR_NO_DEVICE = \
+    0, -1, -2, -3, -4, -5, -6, -7
 SOLVER_CHOLESKY, SOLVER_CG = 0, 1
 PRECISION_FP32, PRECISION_MIXED = 0, 1
 CALIB_SIZE = 96
@@ -499,15 +502,41 @@ class Tracker(Batch):
     def __init__(self, config: Config, calib, stream=None):
         super().__init__([config], [calib], stream)
 
+    def _frame(self, gray, depth):
+        if isinstance(gray, np.ndarray):
+            gray = np.ascontiguousarray(gray, np.uint8)
+            depth = np.ascontiguousarray(depth, np.uint16)
+        if _on_device(gray) != _on_device(depth):
+            raise ValueError("mix of host and device inputs")
+        return gray, depth, _on_device(gray)
+
     def set_reference(self, gray, depth):
-        super().set_reference([gray], [depth])
+        """recon_set_reference: the new keyframe; the relative pose restarts at the identity."""
+        g, d, dev = self._frame(gray, depth)
+        check(lib().recon_set_reference(self.h, _ptr(g), _ptr(d), dev))
 
     def set_current(self, gray, depth):
-        super().set_current([gray], [depth])
+        g, d, dev = self._frame(gray, depth)
+        self._keep = [g, d]
+        check(lib().recon_set_current(self.h, _ptr(g), _ptr(d), dev))
 
     def track(self, T_init=None):
-        T, st = super().track(None if T_init is None else np.asarray(T_init).reshape(1, 16))
-        return T[0], st[0]
+        """recon_track: the schedule from T_init (None: the tracker's pose) and
+        the host pose bookkeeping (applyIncrement).  Returns the tracked pose
+        (reference -> current) and the frame's statistics; a frame whose status
+        is RECON_ERR_NON_SPD or RECON_ERR_NOT_ENOUGH_POINTS keeps its pose and
+        is reported in the statistics, not raised."""
+        stats = (TrackStats * 1)()
+        T = None
+        if T_init is not None:
+            T = np.ascontiguousarray(np.asarray(T_init, np.float32).reshape(16))
+        rc = lib().recon_track(self.h, None if T is None else _ptr(T), ctypes.cast(stats, ctypes.c_void_p))
+        if rc < 0 and rc not in (ERR_NON_SPD, ERR_NOT_ENOUGH_POINTS):
+            check(rc)
+        if T is None:
+            T = np.zeros(16, np.float32)
+            check(lib().recon_batch_get_poses(self.h, _ptr(T), None))
+        return T.reshape(4, 4), stats[0]
 
     def global_pose(self) -> np.ndarray:
         g = np.zeros(16, np.float64)

@@ -1045,9 +1045,11 @@ int recon_batch_get_poses(recon_batch *b, float *T_out, recon_track_stats *stats
             o.non_spd = s[ST_NONSPD];
             o.photo_median_bin = s[ST_MEDIAN];
             for (int l = 0; l < RECON_MAX_LEVELS; l++) o.icp_selected[l] = s[ST_ICPSEL0 + l];
-            o.status = o.non_spd ? RECON_ERR_NON_SPD : RECON_OK;
-            if (b->cfg[i].mode == RECON_GEOMETRIC && o.solves == 0 && o.iterations == 0)
-                o.status = RECON_ERR_NOT_ENOUGH_POINTS;
+            // a rejected pivot first; else an iteration skipped for lack of ICP
+            // correspondences (ShapeTracker's "not enough points",
+            // shapetracker.cpp:365); the pose is kept in both cases
+            o.status = o.non_spd ? RECON_ERR_NON_SPD
+                                 : (o.solves < o.iterations ? RECON_ERR_NOT_ENOUGH_POINTS : RECON_OK);
         }
     }
     return RECON_OK;

@@ -200,6 +200,12 @@ class OracleTracker:
         d = np.ascontiguousarray(depth, np.uint16)
         self.L.orc_set_reference(self.h, ptr(g), ptr(d))
 
+    def set_reference_float(self, gray: np.ndarray, z: np.ndarray):
+        """A reference given as float gray in [0, 1] and z = -mm (0 or NaN: invalid)."""
+        g = np.ascontiguousarray(gray, np.float32).reshape(-1)
+        zz = np.ascontiguousarray(z, np.float32).reshape(-1)
+        self.L.orc_set_reference_float(self.h, ptr(g), ptr(zz))
+
     def set_current(self, gray: np.ndarray, depth: np.ndarray):
         g = np.ascontiguousarray(gray, np.uint8)
         d = np.ascontiguousarray(depth, np.uint16)
