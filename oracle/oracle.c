@@ -1224,14 +1224,14 @@ static void normalize_mat4_safe(double *T) {
     } else { w[0] = 0; w[1] = 0; w[2] = 1; }
     /* crossproductReal(v, w, u), expmCuda.cu:1934-1938 */
     u[0] = fma(v[1], w[2], -(v[2] * w[1]));
-    u[1] = -fma(v[0], w[2], -(v[2] * w[0]));
+    u[1] = fma(-v[0], w[2], v[2] * w[0]);  /* no fused result is negated (signed zeros) */
     u[2] = fma(v[0], w[1], -(v[1] * w[0]));
     if (lenU > 1e-8f) {
         double iu = 1.0 / lenU;
         u[0] = u[0] * iu; u[1] = u[1] * iu; u[2] = u[2] * iu;
     } else { u[0] = 1; u[1] = 0; u[2] = 0; }
     v[0] = fma(w[1], u[2], -(w[2] * u[1]));
-    v[1] = -fma(w[0], u[2], -(w[2] * u[0]));
+    v[1] = fma(-w[0], u[2], w[2] * u[0]);
     v[2] = fma(w[0], u[1], -(w[1] * u[0]));
     T[0] = u[0]; T[4] = u[1]; T[8] = u[2];
     T[1] = v[0]; T[5] = v[1]; T[9] = v[2];

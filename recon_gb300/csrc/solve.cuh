@@ -74,12 +74,12 @@ __device__ __forceinline__ void wnormalize(double *T, int lane) {
     int ia = (i == 0) ? 1 : 0, ib = (i == 2) ? 1 : 2;
     double w_a = __shfl_sync(kFull, wi, ia), w_b = __shfl_sync(kFull, wi, ib);
     double v_a = __shfl_sync(kFull, vi, ia), v_b = __shfl_sync(kFull, vi, ib);
-    double r = __fma_rn(v_a, w_b, -(v_b * w_a));
-    double ui = (i == 1) ? -r : r;
+    // component 1 is v0 w2 - v2 w0 negated: written as -v0 w2 + v2 w0 so that
+    // no fused result is negated (a negated zero sum would flip its sign)
+    double ui = (i == 1) ? __fma_rn(-v_a, w_b, v_b * w_a) : __fma_rn(v_a, w_b, -(v_b * w_a));
     ui = okU ? ui * iu : (i == 0 ? 1.0 : 0.0);
     double u_a = __shfl_sync(kFull, ui, ia), u_b = __shfl_sync(kFull, ui, ib);
-    double r2 = __fma_rn(w_a, u_b, -(w_b * u_a));
-    double vn = (i == 1) ? -r2 : r2;
+    double vn = (i == 1) ? __fma_rn(-w_a, u_b, w_b * u_a) : __fma_rn(w_a, u_b, -(w_b * u_a));
     __syncwarp();
     if (lane < 3) {
         T[4 * i] = ui;
