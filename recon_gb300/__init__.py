@@ -529,7 +529,8 @@ class Tracker(Batch):
         stats = (TrackStats * 1)()
         T = None
         if T_init is not None:
-            T = np.ascontiguousarray(np.asarray(T_init, np.float32).reshape(16))
+            # a copy: recon_track writes the result into its pose argument
+            T = np.array(T_init, dtype=np.float32).reshape(16).copy()
         rc = lib().recon_track(self.h, None if T is None else _ptr(T), ctypes.cast(stats, ctypes.c_void_p))
         if rc < 0 and rc not in (ERR_NON_SPD, ERR_NOT_ENOUGH_POINTS):
             check(rc)
