@@ -13,6 +13,9 @@
  * accept either host (0) or device (1) image pointers.  All device work of one
  * tracker/batch runs on the stream given at creation (NULL = the library's own
  * stream); the reference's second GPU becomes a second stream (fusion).
+ * Device inputs are read on that stream: work that writes them on another
+ * stream must be ordered before the call (an event the batch's stream,
+ * recon_batch_stream, waits for, or a synchronisation).
  */
 #pragma once
 #include <stddef.h>
@@ -238,9 +241,13 @@ int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, in
  * larger n_points is rejected with RECON_ERR_INVALID_ARG.  Every call shares
  * that array, so calls that overlap on the GPU (other streams or host threads)
  * race and must be serialised by the caller.  The first call on a device looks
- * up the array's device address; make that first call before any stream
- * capture.  All pointers in the view and T_dev are device memory; the result
- * equals one iteration of recon_batch_track in PHOTOMETRIC mode. */
+ * up the array's device address and keeps it; make that first call before any
+ * stream capture, and do not call it again on a device after cudaDeviceReset
+ * (the kept address belongs to the reset context).  All pointers in the view
+ * and T_dev are device memory; the result equals one iteration of
+ * recon_batch_track in PHOTOMETRIC mode.  A solve whose pivot is not positive
+ * leaves T_dev where it was (re-orthonormalised) and is not reported here;
+ * the batch entry point counts it in recon_track_stats.non_spd. */
 #define RECON_NOALLOC_MAX_POINTS 16384
 typedef struct recon_photo_view {
     int32_t n_points;                 /* selected points P, multiple of 1024, <= RECON_NOALLOC_MAX_POINTS */

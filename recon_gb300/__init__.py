@@ -177,6 +177,14 @@ def _on_device(a) -> int:
     return int(hasattr(a, "is_cuda") and a.is_cuda)
 
 
+def _order_after_torch(batch) -> None:
+    """The batch reads device inputs on its own stream: make that stream wait
+    for the work already queued on torch's current stream (which may still be
+    writing the tensors being passed).  An event and a wait, no host stall."""
+    import torch
+    torch.cuda.ExternalStream(batch.stream()).wait_stream(torch.cuda.current_stream())
+
+
 class Batch:
     """Several tracker instances served by the same launches (recon_batch_*)."""
 
@@ -231,6 +239,8 @@ class Batch:
                 raise ValueError("mix of host and device inputs")
             g[i] = _ptr(gi).value
             d[i] = _ptr(di).value
+        if dev:
+            _order_after_torch(self)
         return g, d, int(dev or 0), keep
 
     def _stack_table(self, stack, index, itemsize):
@@ -258,6 +268,8 @@ class Batch:
         if idx.size and (idx.min() < 0 or idx.max() >= F):
             raise IndexError("frame index out of the stack")
         table = np.uint64(base) + idx.astype(np.uint64) * np.uint64(H * W * itemsize)
+        if dev:
+            _order_after_torch(self)
         return np.ascontiguousarray(table, np.uint64), dev
 
     def _stack_tables(self, grays, depths, index, shape):
@@ -310,10 +322,14 @@ class Batch:
 
     def set_reference_rgbd_float4(self, inst: int, rgbd):
         a = np.ascontiguousarray(rgbd, np.float32) if isinstance(rgbd, np.ndarray) else rgbd
+        if _on_device(a):
+            _order_after_torch(self)
         check(lib().recon_batch_set_reference_rgbd_float4(self.h, inst, _ptr(a), _on_device(a)))
 
     def set_current_rgbd_float4(self, inst: int, rgbd):
         a = np.ascontiguousarray(rgbd, np.float32) if isinstance(rgbd, np.ndarray) else rgbd
+        if _on_device(a):
+            _order_after_torch(self)
         check(lib().recon_batch_set_current_rgbd_float4(self.h, inst, _ptr(a), _on_device(a)))
 
     def track(self, T_init=None):
@@ -351,6 +367,8 @@ class Batch:
                     raise ValueError("mix of host and device inputs")
                 g[f * self.n + i] = _ptr(gi).value
                 d[f * self.n + i] = _ptr(di).value
+        if dev:
+            _order_after_torch(self)
         T = np.zeros((nf, self.n, 16), np.float32)
         stats = (TrackStats * self.n)()
         check(lib().recon_batch_track_sequence(self.h, nf, ctypes.cast(g, ctypes.c_void_p),
@@ -384,6 +402,8 @@ class Batch:
                     if _on_device(gi) != od:
                         raise ValueError("mix of host and device inputs")
                     g[f * self.n + i] = _ptr(gi).value
+        if dev:
+            _order_after_torch(self)
         Tn = np.ascontiguousarray(np.asarray(T, np.float32).reshape(nf * self.n, 16))
         check(lib().recon_batch_fuse_keyframe_rgbd(self.h, nf, None if g is None else ctypes.cast(g, ctypes.c_void_p),
                                                    ctypes.cast(d, ctypes.c_void_p), _ptr(Tn), int(dev or 0), gate_mm))
@@ -508,6 +528,8 @@ class Tracker(Batch):
             depth = np.ascontiguousarray(depth, np.uint16)
         if _on_device(gray) != _on_device(depth):
             raise ValueError("mix of host and device inputs")
+        if _on_device(gray):
+            _order_after_torch(self)
         return gray, depth, _on_device(gray)
 
     def set_reference(self, gray, depth):

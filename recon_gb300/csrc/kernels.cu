@@ -2034,7 +2034,6 @@ extern "C" int recon_photometric_iteration_noalloc(const recon_photo_view *v, fl
         v->img_height != (v->depth_height >> v->level))
         return noalloc_reject("recon_photometric_iteration_noalloc: img must be the depth size >> level");
     if (v->solver < 0 || v->solver > 1) return noalloc_reject("recon_photometric_iteration_noalloc: bad solver");
-    (void)cudaGetLastError();
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
         rt::set_last_error("recon_photometric_iteration_noalloc: no current CUDA device");
@@ -2055,8 +2054,14 @@ extern "C" int recon_photometric_iteration_noalloc(const recon_photo_view *v, fl
         }
         ptr = g_noalloc_ptr[dev];
     }
-    rt::k_photo_iter_noalloc<<<1, rt::kLanes, 0, (cudaStream_t)stream>>>(*v, (float *)ptr, T_dev);
-    if (cudaGetLastError() != cudaSuccess) {
+    // the launch status comes from the launch call itself, so an error the
+    // caller's own earlier work left pending is neither cleared nor taken for ours
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(rt::kLanes);
+    cfg.stream = (cudaStream_t)stream;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, rt::k_photo_iter_noalloc, *v, (float *)ptr, T_dev);
+    if (e != cudaSuccess) {
         rt::set_last_error("recon_photometric_iteration_noalloc: kernel launch failed");
         return RECON_ERR_CUDA;
     }
