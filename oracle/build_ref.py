@@ -46,6 +46,12 @@ FRAGMENTS = {
     "tracker/kernels/downSample2Cuda.cu": ["fastDownSampleHdrKernel"],
     # one-block kernels with shared memory and __syncthreads (run as 512 host threads)
     "tracker/kernels/filterIndex256.cu": ["seekThreshold256Kernel2", "filterIndexKernel4"],
+    # the reconstruction stream: TSDF update, ray cast, shading, resampling
+    "tracker/kernels/VoxelGrid_cuda.cu": [
+        "transformRT3CUDA", "resetKernel", "initRay", "intersectVoxelGridCuda", "voxelize", "trilinearDensity",
+        "trilinearWeight", "estimateLinearZero", "traverseVoxelsCuda", "rayCastVoxelsKernel", "filter3",
+        "shadingKernel", "resampleVoxelsKernel", "updateVoxelsKernel", "reconstructionKernel",
+    ],
     # host code: the keyframe trigger's pose test
     "tracker/tracker/phototracker.cpp": ["bool PhotoTracker::poseDifferenceExceeded"],
 }
@@ -89,9 +95,15 @@ def main() -> int:
         base = os.path.splitext(os.path.basename(rel))[0]
         with open(os.path.join(OUT, f"frag_{base}.inc"), "w") as f:
             f.write(f"// extracted from {rel}: {', '.join(names)}\n" + body)
+    # particles_kernel.cuh includes the CUDA header vector_types.h; the shim
+    # defines the vector types itself, so an empty stand-in satisfies it
+    stub = os.path.join(OUT, "stub")
+    os.makedirs(stub, exist_ok=True)
+    with open(os.path.join(stub, "vector_types.h"), "w") as f:
+        f.write("// empty: the vector types come from ref_shim.cpp\n")
     cxx = os.environ.get("CXX", "g++")
     flags = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w", "-std=c++20", "-pthread"]
-    inc = ["-I" + OUT, "-I" + os.path.join(ref, "tracker"), "-I" + os.path.join(ref, "tracker", "kernels"),
+    inc = ["-I" + OUT, "-I" + stub, "-I" + os.path.join(ref, "tracker"), "-I" + os.path.join(ref, "tracker", "kernels"),
            "-I" + os.path.join(ref, "tracker", "tracker")]
     objs = []
     shim_o = os.path.join(OUT, "ref_shim.o")

@@ -186,6 +186,24 @@ void orc64_get_pose(const orc64_tracker *t, double T[16]);
 void orc64_set_pose(orc64_tracker *t, const double T[16]);
 int orc64_get_array(orc64_tracker *t, const char *name, int level, void *dst, int64_t nbytes);
 
+/* ---- reconstruction stream (oracle_tsdf.c): TSDF fusion and ray cast,
+ * tracker/kernels/VoxelGrid_cuda.cu; grid = R^3 float2 (tsdf, weight), x fastest ---- */
+typedef struct orc_tsdf_params {
+    int32_t R;           /* voxels per side (SimParams.gridResolution) */
+    float origin[3];     /* SimParams.cubeOrigin */
+    float dim[3];        /* SimParams.cubeDim: half the side length */
+    int32_t W, H;        /* SimParams.winWidth / winHeight */
+    float min_dist, max_dist;
+} orc_tsdf_params;
+void orc_tsdf_invert_rt4(const float *M, float *Mi);
+void orc_tsdf_reset(float *grid, int64_t nvox);
+void orc_tsdf_dist_from_rgbd(const float *rgbd, int W, int H, float min_dist, float max_dist, float *dist);
+void orc_tsdf_update(float *grid, const orc_tsdf_params *p, const float *dist, const float Tcur[16], const float K[9]);
+void orc_tsdf_raycast(const float *grid, const orc_tsdf_params *p, const float Tcur[16], const float K[9],
+                      int filtering, float *xyz);
+void orc_tsdf_shade(const float *xyz, int W, int H, float *shaded, float *normal);
+void orc_tsdf_resample(float *dst, const float *src, const orc_tsdf_params *p, const float Tcur[16]);
+
 /* ---- procedural scene (CPU twin of the GPU renderer) ---- */
 struct recon_scene;
 struct recon_camera;

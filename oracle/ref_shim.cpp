@@ -77,6 +77,49 @@ namespace refk {
 
 #include "frag_phototracker.inc"
 
+// ---- tracker/kernels/VoxelGrid_cuda.cu (reconstruction stream) ----
+// The voxel kernels use the CUDA samples' helper_math.h vector operators
+// (componentwise float3 / float4 arithmetic, dot, clamp), restated here, the
+// reference's SimParams (kernels/particles_kernel.cuh, included as is) in a
+// global `params`, and uint3 values converted from float the way the GPU does
+// it: truncation that saturates (negative and NaN give 0), also for the
+// `uint += float` steps of the voxel traversal.
+void invertRT4(float *M, float *Mi);  // basic_math.cpp:355-368
+#include <cfloat>
+namespace refv {
+using refk::normalize3Cuda;
+using refk::rotate3Cuda;
+static inline unsigned gpu_f2u(float v) {
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 4294967296.0f) return 0xffffffffu;
+    return (unsigned)v;
+}
+struct SatU {
+    unsigned v;
+    operator unsigned() const { return v; }
+    SatU &operator+=(float f) { v = gpu_f2u((float)v + f); return *this; }
+};
+struct uint3 { SatU x, y, z; };
+static inline uint3 make_uint3(float a, float b, float c) {
+    uint3 r = {{gpu_f2u(a)}, {gpu_f2u(b)}, {gpu_f2u(c)}};
+    return r;
+}
+static inline float4 make_float4(float a, float b, float c, float d) { float4 r = {a, b, c, d}; return r; }
+static inline float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline float3 operator*(float3 a, float3 b) { return make_float3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+static inline float3 operator/(float s, float3 a) { return make_float3(s / a.x, s / a.y, s / a.z); }
+static inline float4 operator-(float4 a, float4 b) { return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+static inline float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline float clamp(float f, float a, float b) { return fmaxf(a, fminf(f, b)); }
+static inline float max(float a, float b) { return fmaxf(a, b); }
+static inline float min(float a, float b) { return fminf(a, b); }
+#include "particles_kernel.cuh"
+static SimParams params;
+#include "frag_VoxelGrid_cuda.inc"
+}  // namespace refv
+
 void expm(float *x, float *Tmotion, float scaleOut);  // tracker/tracker/expm.c:2084 (C++ linkage)
 
 namespace {
@@ -319,6 +362,82 @@ void ref_applyIncrement(float *T, double *globalPose, float *Trel) {
     float_precision4(&Tdbl[0], T);
     matrixMult4x4(&iTprev[0], &Tdbl[0], &Tinc[0]);
     matrixMult4x4(&globalPose[0], &Tinc[0], &globalPose[0]);
+}
+
+}  // extern "C"
+
+// ---- reconstruction stream launchers: every kernel over its whole grid ----
+// SimParams as VoxelGrid's constructor and setCameraParams fill it
+// (VoxelGrid.cpp:48-106, 266-273): voxelSize = cubeDim / gridResolution,
+// T = invertRT4(Tcur) (world -> camera), iT = Tcur, K normalised.
+static void ref_tsdf_params(int R, const float *origin, const float *dim, int W, int H, float min_dist, float max_dist,
+                            const float *Tcur, const float *K) {
+    refv::SimParams &p = refv::params;
+    memset(&p, 0, sizeof(p));
+    p.maxDist = max_dist;
+    p.minDist = min_dist;
+    p.winWidth = W;
+    p.winHeight = H;
+    p.cubeOrigin = make_float3(origin[0], origin[1], origin[2]);
+    p.cubeDim = make_float3(dim[0], dim[1], dim[2]);
+    p.gridResolution = R;
+    p.voxelSize = make_float3(p.cubeDim.x / R, p.cubeDim.y / R, p.cubeDim.z / R);
+    if (Tcur) {
+        float Tc[16], iTc[16];
+        memcpy(Tc, Tcur, sizeof(Tc));
+        invertRT4(Tc, iTc);
+        memcpy(p.T.m, iTc, sizeof(iTc));
+        memcpy(p.iT.m, Tc, sizeof(Tc));
+    }
+    if (K) memcpy(p.K.m, K, 9 * sizeof(float));
+}
+
+template <class F> static void launch3d(int R, F f) {
+    blockDim = {1, 1, 1};
+    gridDim = {(unsigned)R, (unsigned)R, (unsigned)R};
+    threadIdx = {0, 0, 0};
+    for (int z = 0; z < R; z++)
+        for (int y = 0; y < R; y++)
+            for (int x = 0; x < R; x++) {
+                blockIdx = {(unsigned)x, (unsigned)y, (unsigned)z};
+                f();
+            }
+}
+
+extern "C" {
+
+void ref_tsdf_reset(float *grid, int nvox) {
+    launch1d(nvox, 1024, [&] { refv::resetKernel((float2 *)grid, 1.0f, 0.0f); });
+}
+
+void ref_tsdf_reconstruction(float *rgbd, int W, int H, float min_dist, float max_dist, float *dist) {
+    ref_tsdf_params(8, (const float[3]){0, 0, 0}, (const float[3]){1, 1, 1}, W, H, min_dist, max_dist, nullptr,
+                    nullptr);
+    rgbdTex.data = (const float4 *)rgbd;
+    rgbdTex.width = W;
+    launch2d(W, H, [&] { refv::reconstructionKernel(dist, W, H); });
+    rgbdTex.data = nullptr;
+}
+
+void ref_tsdf_update(float *grid, int R, float *origin, float *dim, int W, int H, float min_dist, float max_dist,
+                     float *Tcur, float *K, float *dist) {
+    ref_tsdf_params(R, origin, dim, W, H, min_dist, max_dist, Tcur, K);
+    launch3d(R, [&] { refv::updateVoxelsKernel((float2 *)grid, dist); });
+}
+
+void ref_tsdf_raycast(float *grid, int R, float *origin, float *dim, int W, int H, float min_dist, float max_dist,
+                      float *Tcur, float *K, int filtering, float *xyz) {
+    ref_tsdf_params(R, origin, dim, W, H, min_dist, max_dist, Tcur, K);
+    launch2d(W, H, [&] { refv::rayCastVoxelsKernel((float2 *)grid, W, H, filtering != 0, (float4 *)xyz); });
+}
+
+void ref_tsdf_shade(float *xyz, int W, int H, float *shaded, float *normal) {
+    launch2d(W, H, [&] { refv::shadingKernel((float4 *)xyz, W, H, (float4 *)shaded, (float4 *)normal); });
+}
+
+void ref_tsdf_resample(float *dst, float *src, int R, float *origin, float *dim, float *Tcur) {
+    ref_tsdf_params(R, origin, dim, 8, 8, 0, 1, Tcur, nullptr);
+    launch3d(R, [&] { refv::resampleVoxelsKernel((float2 *)dst, (float2 *)src); });
 }
 
 }  // extern "C"

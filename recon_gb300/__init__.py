@@ -152,8 +152,37 @@ def lib() -> ctypes.CDLL:
             L.recon_render_depth.argtypes = [vp, vp, f32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
             L.recon_render_gray.argtypes = [vp, vp, vp, vp]
             L.recon_selftest_exact_arith.argtypes = [vp]
+            L.recon_tsdf_default_params.argtypes = [i32, i32, i32, f32, f32, ctypes.POINTER(TsdfParams)]
+            L.recon_tsdf_default_params.restype = None
+            L.recon_tsdf_create.argtypes = [ctypes.POINTER(TsdfParams), vp, ctypes.POINTER(vp)]
+            L.recon_tsdf_destroy.argtypes = [vp]
+            L.recon_tsdf_reset.argtypes = [vp]
+            L.recon_tsdf_set_dist_map.argtypes = [vp, vp, i32]
+            L.recon_tsdf_set_dist_rgbd_float4.argtypes = [vp, vp, i32]
+            L.recon_tsdf_set_dist_depth16.argtypes = [vp, vp, i32]
+            L.recon_tsdf_update.argtypes = [vp, vp, vp]
+            L.recon_tsdf_raycast.argtypes = [vp, vp, vp, i32]
+            L.recon_tsdf_resample.argtypes = [vp, vp, vp]
+            L.recon_tsdf_device_array.argtypes = [vp, ctypes.c_char_p]
+            L.recon_tsdf_device_array.restype = vp
+            L.recon_tsdf_get.argtypes = [vp, ctypes.c_char_p, vp, i64]
+            L.recon_tsdf_get.restype = i64
+            L.recon_tsdf_set_grid.argtypes = [vp, vp, i32]
+            L.recon_tsdf_stream.argtypes = [vp]
+            L.recon_tsdf_stream.restype = vp
+            L.recon_tsdf_enable_timing.argtypes = [vp, i32]
+            L.recon_tsdf_get_timing.argtypes = [vp, vp, vp, i32]
+            L.recon_tsdf_enable_counting.argtypes = [vp, i32]
+            L.recon_tsdf_get_counts.argtypes = [vp, vp, i32]
             _lib = L
     return _lib
+
+
+class TsdfParams(ctypes.Structure):
+    """recon_tsdf_params (include/recon_tsdf.h)."""
+    _fields_ = [("grid_resolution", ctypes.c_int32), ("cube_origin", ctypes.c_float * 3),
+                ("cube_dim", ctypes.c_float * 3), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("min_dist", ctypes.c_float), ("max_dist", ctypes.c_float)]
 
 
 def check(rc: int) -> int:
@@ -606,3 +635,141 @@ def render_depth(scene, camera, noise_rel: float, noise_seed: int, frame: int, o
 def render_gray(scene, camera, out, stream=None):
     check(lib().recon_render_gray(ctypes.byref(scene), ctypes.byref(camera), _ptr(out),
                                   ctypes.c_void_p(stream) if stream else None))
+
+
+# ---- reconstruction stream (include/recon_tsdf.h) ----
+
+TSDF_TIMING_KINDS = ("update", "raycast", "shading", "distance_map", "reset_resample")
+
+
+def tsdf_params(grid_resolution: int, width: int, height: int, min_dist: float = 400.0, max_dist: float = 4500.0,
+                cube_origin=None, cube_dim=None) -> TsdfParams:
+    """VoxelGrid's parameters; the reference's grid placement unless given."""
+    p = TsdfParams()
+    lib().recon_tsdf_default_params(grid_resolution, width, height, min_dist, max_dist, ctypes.byref(p))
+    if cube_origin is not None:
+        p.cube_origin[:] = [float(v) for v in cube_origin]
+    if cube_dim is not None:
+        p.cube_dim[:] = [float(v) for v in cube_dim]
+    return p
+
+
+def normalized_K(K_pix, width: int, height: int) -> np.ndarray:
+    """getNormalizedK (main.cpp:878-882): pixel intrinsics over width / height, in float."""
+    K = np.asarray(K_pix, np.float32).reshape(-1)
+    out = np.zeros(9, np.float32)
+    out[0] = K[0] / np.float32(width)
+    out[2] = K[2] / np.float32(width)
+    out[4] = K[4] / np.float32(height)
+    out[5] = K[5] / np.float32(height)
+    out[8] = 1.0
+    return out
+
+
+class TSDF:
+    """A voxel grid of the reconstruction stream (VoxelGrid, recon_tsdf_*).
+
+    Poses are 4x4 camera -> world; K is the normalised 3x3 intrinsic matrix.
+    Device inputs (torch tensors) are read on the grid's stream after the work
+    queued on torch's current stream."""
+
+    def __init__(self, params: TsdfParams, stream=None):
+        self.params = params
+        h = ctypes.c_void_p()
+        check(lib().recon_tsdf_create(ctypes.byref(params), ctypes.c_void_p(stream) if stream else None,
+                                      ctypes.byref(h)))
+        self.h = h
+        self.R = params.grid_resolution
+        self.W, self.H = params.width, params.height
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().recon_tsdf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stream(self) -> int:
+        return lib().recon_tsdf_stream(self.h)
+
+    def _inputs_ready(self, a):
+        if _on_device(a):
+            _order_after_torch(self)
+
+    def reset(self):
+        check(lib().recon_tsdf_reset(self.h))
+
+    def set_dist_map(self, dist):
+        self._inputs_ready(dist)
+        check(lib().recon_tsdf_set_dist_map(self.h, _ptr(dist), _on_device(dist)))
+
+    def set_dist_rgbd_float4(self, rgbd):
+        self._inputs_ready(rgbd)
+        check(lib().recon_tsdf_set_dist_rgbd_float4(self.h, _ptr(rgbd), _on_device(rgbd)))
+
+    def set_dist_depth16(self, depth):
+        self._inputs_ready(depth)
+        check(lib().recon_tsdf_set_dist_depth16(self.h, _ptr(depth), _on_device(depth)))
+
+    @staticmethod
+    def _f32(a, n):
+        a = np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1))
+        assert a.size == n
+        return a
+
+    def update(self, T, K):
+        T = self._f32(T, 16)
+        K = self._f32(K, 9)
+        check(lib().recon_tsdf_update(self.h, _ptr(T), _ptr(K)))
+
+    def raycast(self, T, K, cubic_filter: bool = True):
+        T = self._f32(T, 16)
+        K = self._f32(K, 9)
+        check(lib().recon_tsdf_raycast(self.h, _ptr(T), _ptr(K), int(cubic_filter)))
+
+    def resample_from(self, src: "TSDF", T):
+        T = self._f32(T, 16)
+        check(lib().recon_tsdf_resample(self.h, src.h, _ptr(T)))
+
+    def device_array(self, name: str) -> int:
+        p = lib().recon_tsdf_device_array(self.h, name.encode())
+        if not p:
+            raise ReconError(ERR_INVALID_ARG, f"unknown array {name}")
+        return p
+
+    def get(self, name: str) -> np.ndarray:
+        if name == "tsdf":
+            out = np.empty(2 * self.R ** 3, np.float32)
+        elif name == "dist":
+            out = np.empty(self.W * self.H, np.float32)
+        elif name == "flags":
+            out = np.empty((self.R // 8) ** 3, np.uint8)
+        else:
+            out = np.empty(4 * self.W * self.H, np.float32)
+        check(lib().recon_tsdf_get(self.h, name.encode(), _ptr(out), out.nbytes))
+        return out
+
+    def set_grid(self, grid):
+        self._inputs_ready(grid)
+        check(lib().recon_tsdf_set_grid(self.h, _ptr(grid), _on_device(grid)))
+
+    def enable_timing(self, on: bool = True):
+        check(lib().recon_tsdf_enable_timing(self.h, int(on)))
+
+    def timing(self, reset: bool = True) -> dict:
+        ms = np.zeros(5, np.float64)
+        n = np.zeros(5, np.int64)
+        check(lib().recon_tsdf_get_timing(self.h, _ptr(ms), _ptr(n), int(reset)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(TSDF_TIMING_KINDS)}
+
+    def enable_counting(self, on: bool = True):
+        check(lib().recon_tsdf_enable_counting(self.h, int(on)))
+
+    def counts(self, reset: bool = True) -> np.ndarray:
+        c = np.zeros(3, np.int64)
+        check(lib().recon_tsdf_get_counts(self.h, _ptr(c), int(reset)))
+        return c

@@ -97,6 +97,7 @@ void clear_stale_error() { (void)cudaGetLastError(); }
 namespace rt {
 // lets other translation units of the library report a message through recon_last_error
 void set_last_error(const char *msg) { g_last_error = msg; }
+void add_launches(long long n) { g_launches += n; }
 }  // namespace rt
 
 namespace {

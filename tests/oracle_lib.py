@@ -45,6 +45,12 @@ class OrcIterTrace(ctypes.Structure):
     ]
 
 
+class OrcTsdfParams(ctypes.Structure):
+    _fields_ = [("R", ctypes.c_int32), ("origin", ctypes.c_float * 3), ("dim", ctypes.c_float * 3),
+                ("W", ctypes.c_int32), ("H", ctypes.c_int32), ("min_dist", ctypes.c_float),
+                ("max_dist", ctypes.c_float)]
+
+
 def _build() -> None:
     src = [os.path.join(ORACLE_DIR, f) for f in ("oracle.c", "oracle_fp64.c", "oracle.h", "initnet_oracle.c",
                                                  "Makefile")]
@@ -140,6 +146,13 @@ def lib() -> ctypes.CDLL:
             L.orc_init_gate.restype = i32
             L.orc_set_pose.argtypes = [vp, vp]
             L.orc_get_pose.argtypes = [vp, vp]
+            L.orc_tsdf_invert_rt4.argtypes = [vp, vp]
+            L.orc_tsdf_reset.argtypes = [vp, ctypes.c_int64]
+            L.orc_tsdf_dist_from_rgbd.argtypes = [vp, i32, i32, f32, f32, vp]
+            L.orc_tsdf_update.argtypes = [vp, ctypes.POINTER(OrcTsdfParams), vp, vp, vp]
+            L.orc_tsdf_raycast.argtypes = [vp, ctypes.POINTER(OrcTsdfParams), vp, vp, i32, vp]
+            L.orc_tsdf_shade.argtypes = [vp, i32, i32, vp, vp]
+            L.orc_tsdf_resample.argtypes = [vp, vp, ctypes.POINTER(OrcTsdfParams), vp]
             L.orc_num_threads.restype = i32
             L.orc_set_threads.argtypes = [i32]
             _lib = L
@@ -315,3 +328,64 @@ def render_pair(scene, cam_ir, cam_rgb, noise_rel=0.01, noise_seed=1, frame=0):
     L.orc_render_depth(ctypes.byref(scene), ctypes.byref(cam_ir), noise_rel, noise_seed, frame, ptr(d))
     L.orc_render_gray(ctypes.byref(scene), ctypes.byref(cam_rgb), ptr(g))
     return g, d
+
+
+# ---- reconstruction stream (oracle_tsdf.c) ----
+# the reference's grid placement (VoxelGrid.cpp:62-65: kinect8 test)
+TSDF_ORIGIN = (0.0, 0.01, -1600.01)
+TSDF_DIM = (1500.0, 1500.0, 1500.0)
+
+
+def tsdf_params(R, W, H, min_dist=400.0, max_dist=4500.0, origin=TSDF_ORIGIN, dim=TSDF_DIM) -> OrcTsdfParams:
+    p = OrcTsdfParams()
+    p.R, p.W, p.H = R, W, H
+    p.origin[:] = list(origin)
+    p.dim[:] = list(dim)
+    p.min_dist, p.max_dist = min_dist, max_dist
+    return p
+
+
+def normalized_K(K_pix, W, H) -> np.ndarray:
+    """getNormalizedK (main.cpp:878-882): pixel intrinsics over width / height, in float."""
+    K = np.asarray(K_pix, np.float32).reshape(-1)
+    out = np.zeros(9, np.float32)
+    out[0] = K[0] / np.float32(W)
+    out[2] = K[2] / np.float32(W)
+    out[4] = K[4] / np.float32(H)
+    out[5] = K[5] / np.float32(H)
+    out[8] = 1.0
+    return out
+
+
+class OracleTSDF:
+    """The CPU oracle's voxel grid: reset, update, ray cast, shading, resampling."""
+
+    def __init__(self, params: OrcTsdfParams):
+        self.p = params
+        self.grid = np.zeros(2 * params.R ** 3, np.float32)
+        lib().orc_tsdf_reset(ptr(self.grid), params.R ** 3)
+
+    def update(self, dist, Tcur, K):
+        d = np.ascontiguousarray(dist, np.float32).reshape(-1)
+        T = np.ascontiguousarray(Tcur, np.float32).reshape(-1)
+        Kn = np.ascontiguousarray(K, np.float32).reshape(-1)
+        lib().orc_tsdf_update(ptr(self.grid), ctypes.byref(self.p), ptr(d), ptr(T), ptr(Kn))
+
+    def raycast(self, Tcur, K, filtering=True):
+        xyz = np.zeros(4 * self.p.W * self.p.H, np.float32)
+        T = np.ascontiguousarray(Tcur, np.float32).reshape(-1)
+        Kn = np.ascontiguousarray(K, np.float32).reshape(-1)
+        lib().orc_tsdf_raycast(ptr(self.grid), ctypes.byref(self.p), ptr(T), ptr(Kn), int(filtering), ptr(xyz))
+        return xyz
+
+    def shade(self, xyz):
+        shaded = np.zeros_like(xyz)
+        normal = np.zeros_like(xyz)
+        lib().orc_tsdf_shade(ptr(xyz), self.p.W, self.p.H, ptr(shaded), ptr(normal))
+        return shaded, normal
+
+    def resampled(self, Tcur):
+        dst = np.zeros_like(self.grid)
+        T = np.ascontiguousarray(Tcur, np.float32).reshape(-1)
+        lib().orc_tsdf_resample(ptr(dst), ptr(self.grid), ctypes.byref(self.p), ptr(T))
+        return dst

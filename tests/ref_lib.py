@@ -49,5 +49,11 @@ def lib() -> ctypes.CDLL:
         L.ref_poseDifferenceExceeded.argtypes = [vp, f32, f32]
         L.ref_poseDifferenceExceeded.restype = i32
         L.ref_applyIncrement.argtypes = [vp, vp, vp]
+        L.ref_tsdf_reset.argtypes = [vp, i32]
+        L.ref_tsdf_reconstruction.argtypes = [vp, i32, i32, f32, f32, vp]
+        L.ref_tsdf_update.argtypes = [vp, i32, vp, vp, i32, i32, f32, f32, vp, vp, vp]
+        L.ref_tsdf_raycast.argtypes = [vp, i32, vp, vp, i32, i32, f32, f32, vp, vp, i32, vp]
+        L.ref_tsdf_shade.argtypes = [vp, i32, i32, vp, vp]
+        L.ref_tsdf_resample.argtypes = [vp, vp, i32, vp, vp, vp]
         _lib = L
     return _lib

@@ -1,5 +1,5 @@
 """C-ABI checks that need no GPU: the library loads, exports every function that
-include/recon_track.h declares, and its host-only entry points behave."""
+the headers under include/ declare, and its host-only entry points behave."""
 import ctypes
 import os
 import re
@@ -20,19 +20,29 @@ def L():
     return rg.lib()
 
 
-def declared_functions():
-    src = open(os.path.join(ROOT, "include", "recon_track.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s*(recon_[a-z0-9_]+)\s*\(", src, flags=re.M)
-    return sorted(set(names))
+def declared_functions(header=None):
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for h in sorted(os.listdir(inc)) if header is None else [header]:
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(inc, h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s*(recon_[a-z0-9_]+)\s*\(", src,
+                                flags=re.M))
+    return sorted(names)
 
 
 def test_header_declares_the_operator_api():
-    names = declared_functions()
+    names = declared_functions("recon_track.h")
     for required in ["recon_tracker_create", "recon_set_reference", "recon_set_current", "recon_track",
                      "recon_set_iterations", "recon_set_mode", "recon_reset", "recon_get_global_pose",
                      "recon_batch_create", "recon_batch_track", "recon_calib_setup"]:
         assert required in names
+    tsdf = declared_functions("recon_tsdf.h")
+    for required in ["recon_tsdf_create", "recon_tsdf_reset", "recon_tsdf_update", "recon_tsdf_raycast",
+                     "recon_tsdf_resample", "recon_tsdf_set_dist_rgbd_float4", "recon_tsdf_device_array"]:
+        assert required in tsdf
 
 
 def test_library_exports_every_declared_symbol(L):
