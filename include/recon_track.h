@@ -114,6 +114,20 @@ int recon_batch_size(const recon_batch *b);
  * gray[i] / depth[i] may be NULL to leave instance i unchanged. */
 int recon_batch_set_reference(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
                               int32_t on_device);
+/* The filtered reference (setFilteredReference(true); PhotoTracker::
+ * setReferencePoints and ShapeTracker::setReferencePoints, phototracker.cpp:
+ * 310-337, shapetracker.cpp:195-212): the photometric reference from gray and
+ * depth as recon_batch_set_reference, the ICP reference from oriented points
+ * -- points[i] and normals[i] are width x height float4 maps in instance i's
+ * depth-camera frame, typically the ray cast of a fused volume
+ * (recon_tsdf_device_array "xyz" and "normal"); a pixel whose point has z < 0
+ * and whose normal is not zero becomes an ICP point with that normal
+ * (genOrientedPoints6Kernel, d2z.cu:471-501), coarser levels are 2x2 means
+ * as for a raw reference.  points / normals may hold NULL for instances that
+ * take the raw path (normals from the depth).  A later keyframe fusion
+ * rebuilds the ICP reference from the fused depth. */
+int recon_batch_set_reference_oriented(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
+                                       const float *const *points, const float *const *normals, int32_t on_device);
 /* Reference given as the reference's float4 RGBA + normalised depth frame
  * (rgbTex2GrayHdrZKernel, rgb2gray.cu:64-76; rows stored bottom-up). */
 int recon_batch_set_reference_rgbd_float4(recon_batch *b, int32_t inst, const float *rgbd, int32_t on_device);
@@ -278,6 +292,8 @@ typedef recon_batch recon_tracker;
 int recon_tracker_create(const recon_config *cfg, const float *calib, void *stream, recon_tracker **out);
 int recon_tracker_destroy(recon_tracker *t);
 int recon_set_reference(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device);
+int recon_set_reference_oriented(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, const float *points,
+                                 const float *normals, int32_t on_device);
 int recon_set_current(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device);
 int recon_track(recon_tracker *t, float T_io[16], recon_track_stats *stats);
 int recon_set_iterations(recon_tracker *t, const int32_t iters[RECON_MAX_LEVELS]);
@@ -307,6 +323,28 @@ int recon_pose_difference_exceeded(const float dT[16], float dist_mm, float angl
 int recon_set_reference_updating(recon_tracker *t, int32_t on, float dist_mm, float angle_deg);
 int recon_reference_outdated(recon_tracker *t);
 int recon_batch_reference_outdated(recon_batch *b, float dist_mm, float angle_deg, int32_t *outdated);
+
+/* ---- result files (tracker/calib/ResultTxt.cpp:17-76, TrackingParams.cpp:50-95) ----
+ * recon_trajectory_save: ResultTxt::save -- n poses (n x 16 float, row-major,
+ * e.g. the global poses of successive frames as float, main.cpp:942) are
+ * left-multiplied by the inverse of the first (canonize, float arithmetic in
+ * the reference's order) and written one per line as "i: " and 16 values in
+ * %e; transpose / inverse as ResultTxt::save's flags (the reference writes
+ * transpose 1, inverse 0: the row-major matrix; main.cpp:383).  At most 10000
+ * poses are written (MAX_POSE_COUNT).
+ * recon_trajectory_load: reads such a file back (transpose as it was written);
+ * returns the number of poses.
+ * recon_track_params_load: TrackingParams::init -- lines "frame mode error",
+ * mode geometric (lambda 1), photometric (lambda 0) or biobjective-lambda<x>;
+ * returns the number of entries (all are counted, max_n are stored) or an
+ * error naming the line of an unknown mode.
+ * recon_track_params_lookup: TrackingParams::getParams -- index of the entry
+ * whose frame is nearest to `frame` (the first on ties), -1 without entries
+ * (the reference then uses GEOMETRIC). */
+int recon_trajectory_save(const char *path, const float *poses, int32_t n, int32_t transpose, int32_t inverse);
+int32_t recon_trajectory_load(const char *path, float *poses, int32_t max_n, int32_t transpose);
+int32_t recon_track_params_load(const char *path, int32_t *frames, int32_t *modes, float *lambdas, int32_t max_n);
+int32_t recon_track_params_lookup(const int32_t *frames, int32_t n, int32_t frame);
 
 /* ---- procedural RGB-D renderer (inputs for tests and benchmarks) ----
  * scene / camera: the recon_scene / recon_camera structs of

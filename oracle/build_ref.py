@@ -11,8 +11,10 @@ they use are provided.  This script
     oracle/_ref/frag_<file>.inc,
   * compiles oracle/ref_shim.cpp, which includes those fragments and the
     reference's kernels/kernelUtils.h under a small host shim, together with the
-    reference's CPU SE(3) exponential tracker/tracker/expm.c and its 4x4 /
-    quaternion helpers tracker/tracker/basic_math.cpp,
+    reference's CPU SE(3) exponential tracker/tracker/expm.c, its 4x4 /
+    quaternion helpers tracker/tracker/basic_math.cpp and its result-file
+    classes tracker/calib/ResultTxt.cpp and TrackingParams.cpp (wrapped by
+    oracle/ref_files.cpp),
   * writes everything only below oracle/_ref/ (git-ignored).
 
 Usage: python oracle/build_ref.py REFERENCE_ROOT   (or $RECON_REFERENCE)
@@ -37,6 +39,7 @@ FRAGMENTS = {
     "tracker/kernels/d2z.cu": [
         "xyz2CloudKernel", "genPointsCloud6Kernel", "computeNormalsCudaKernel", "downSampleCloud6Kernel",
         "extractGradientKernel", "addVertexAttributesWithoutNormalsKernel3", "addVertexAttributesWithoutNormalsKernel4",
+        "genOrientedPoints6Kernel",
     ],
     "tracker/kernels/rgb2gray.cu": [
         "icpResidualKernel2", "icpResidualIndexKernel2", "packIndexKernel", "initWeightsKernel",
@@ -101,6 +104,11 @@ def main() -> int:
     os.makedirs(stub, exist_ok=True)
     with open(os.path.join(stub, "vector_types.h"), "w") as f:
         f.write("// empty: the vector types come from ref_shim.cpp\n")
+    # TrackingParams.h includes tracker/phototracker.h (CUDA headers) for the
+    # TrackMode enum alone; the stand-in declares that enum
+    os.makedirs(os.path.join(stub, "tracker"), exist_ok=True)
+    with open(os.path.join(stub, "tracker", "phototracker.h"), "w") as f:
+        f.write("#pragma once\nenum TrackMode { GEOMETRIC, PHOTOMETRIC, BIOBJECTIVE };\n")
     cxx = os.environ.get("CXX", "g++")
     flags = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w", "-std=c++20", "-pthread"]
     inc = ["-I" + OUT, "-I" + stub, "-I" + os.path.join(ref, "tracker"), "-I" + os.path.join(ref, "tracker", "kernels"),
@@ -117,6 +125,13 @@ def main() -> int:
     subprocess.run([cxx, *flags, *inc, "-c", os.path.join(ref, "tracker", "tracker", "basic_math.cpp"), "-o", bm_o],
                    check=True)
     objs.append(bm_o)
+    # the result files: ResultTxt and TrackingParams as they are, and their wrappers
+    for src, obj in ((os.path.join(ref, "tracker", "calib", "ResultTxt.cpp"), "ResultTxt.o"),
+                     (os.path.join(ref, "tracker", "calib", "TrackingParams.cpp"), "TrackingParams.o"),
+                     (os.path.join(HERE, "ref_files.cpp"), "ref_files.o")):
+        o = os.path.join(OUT, obj)
+        subprocess.run([cxx, *flags, *inc, "-c", src, "-o", o], check=True)
+        objs.append(o)
     subprocess.run([cxx, "-shared", "-pthread", "-o", os.path.join(OUT, "libreconref.so"), *objs], check=True)
     print("built", os.path.join(OUT, "libreconref.so"))
     return 0

@@ -1653,6 +1653,41 @@ int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0)
     return prepare_reference(t, gray0, z0, 1);
 }
 
+/* genOrientedPoints6Kernel (d2z.cu:471-501): an ICP point and normal from a
+ * ray-cast point image and its normals (float4 each) where z < 0 and the
+ * normal is not zero, else zeros */
+void orc_gen_oriented_points6(const float *xyz4, const float *nrm4, int W, int H, float *pts6, int32_t *mask) {
+    for (int i = 0; i < W * H; i++) {
+        const float *v = xyz4 + 4 * i, *n = nrm4 + 4 * i;
+        float *o = pts6 + 6 * i;
+        float len = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+        if (v[2] < 0 && len > 1e-7f) {
+            o[0] = v[0]; o[1] = v[1]; o[2] = v[2];
+            o[3] = n[0]; o[4] = n[1]; o[5] = n[2];
+            mask[i] = 1;
+        } else {
+            for (int k = 0; k < 6; k++) o[k] = 0;
+            mask[i] = 0;
+        }
+    }
+}
+
+/* The filtered reference (PhotoTracker::setReferencePoints with
+ * setFilteredReference(true), phototracker.cpp:310-337; ShapeTracker::
+ * setReferencePoints, shapetracker.cpp:195-212): photometric reference from
+ * the frame, ICP level 0 from the oriented points, coarser levels by
+ * downSampleCloud6 (shapetracker.cpp:276-288). */
+int orc_set_reference_oriented(orc_tracker *t, const uint8_t *gray, const uint16_t *depth, const float *xyz4,
+                               const float *nrm4) {
+    int rc = orc_set_reference(t, gray, depth);
+    if (rc) return rc;
+    int W = t->W, H = t->H;
+    orc_gen_oriented_points6(xyz4, nrm4, W, H, t->ref6[0], t->refmask[0]);
+    for (int l = 1; l < t->L; l++)
+        orc_downsample_cloud6(t->ref6[l - 1], t->refmask[l - 1], W >> l, H >> l, t->ref6[l], t->refmask[l]);
+    return 0;
+}
+
 /* Keyframe fusion of nframes depth maps (uint16 mm) with their tracked poses
  * (keyframe -> frame), then the reference is rebuilt from the fused depth
  * with the keyframe's gray image; the current pose is kept. */

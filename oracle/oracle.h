@@ -159,6 +159,9 @@ void orc_destroy(orc_tracker *t);
 int orc_set_reference(orc_tracker *t, const uint8_t *gray, const uint16_t *depth);
 int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0);
 int orc_set_current(orc_tracker *t, const uint8_t *gray, const uint16_t *depth);
+void orc_gen_oriented_points6(const float *xyz4, const float *nrm4, int W, int H, float *pts6, int32_t *mask);
+int orc_set_reference_oriented(orc_tracker *t, const uint8_t *gray, const uint16_t *depth, const float *xyz4,
+                               const float *nrm4);
 int orc_fuse_keyframe(orc_tracker *t, int nframes, const uint16_t *const *depth, const float *Tframes, float gate);
 int orc_fuse_keyframe_rgbd(orc_tracker *t, int nframes, const uint8_t *const *gray, const uint16_t *const *depth,
                            const float *Tframes, float gate);

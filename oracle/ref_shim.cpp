@@ -215,6 +215,10 @@ void ref_genPointsCloud6(float *z, int W, int H, float *calib, float *pts, int *
     launch2d(W, H, [&] { refk::genPointsCloud6Kernel(z, W, H, calib, pts, mask); });
 }
 
+void ref_genOrientedPoints6(float *xyz4, float *nrm4, int W, int H, float *calib, float *pts, int *mask) {
+    launch2d(W, H, [&] { refk::genOrientedPoints6Kernel((float4 *)xyz4, (float4 *)nrm4, W, H, calib, pts, mask); });
+}
+
 void ref_computeNormals(float *pts, int *mask, int W, int H) {
     launch2d(W, H, [&] { refk::computeNormalsCudaKernel(pts, mask, W, H); });
 }

@@ -108,6 +108,8 @@ def lib() -> ctypes.CDLL:
             L.recon_batch_size.argtypes = [vp]
             L.recon_batch_set_reference.argtypes = [vp, vp, vp, i32]
             L.recon_batch_set_reference_rgbd_float4.argtypes = [vp, i32, vp, i32]
+            L.recon_batch_set_reference_oriented.argtypes = [vp, vp, vp, vp, vp, i32]
+            L.recon_set_reference_oriented.argtypes = [vp, vp, vp, vp, vp, i32]
             L.recon_batch_set_current.argtypes = [vp, vp, vp, i32]
             L.recon_batch_set_current_rgbd_float4.argtypes = [vp, i32, vp, i32]
             L.recon_batch_track.argtypes = [vp, vp, vp]
@@ -152,6 +154,13 @@ def lib() -> ctypes.CDLL:
             L.recon_render_depth.argtypes = [vp, vp, f32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
             L.recon_render_gray.argtypes = [vp, vp, vp, vp]
             L.recon_selftest_exact_arith.argtypes = [vp]
+            L.recon_trajectory_save.argtypes = [ctypes.c_char_p, vp, i32, i32, i32]
+            L.recon_trajectory_load.argtypes = [ctypes.c_char_p, vp, i32, i32]
+            L.recon_trajectory_load.restype = i32
+            L.recon_track_params_load.argtypes = [ctypes.c_char_p, vp, vp, vp, i32]
+            L.recon_track_params_load.restype = i32
+            L.recon_track_params_lookup.argtypes = [vp, i32, i32]
+            L.recon_track_params_lookup.restype = i32
             L.recon_tsdf_default_params.argtypes = [i32, i32, i32, f32, f32, ctypes.POINTER(TsdfParams)]
             L.recon_tsdf_default_params.restype = None
             L.recon_tsdf_create.argtypes = [ctypes.POINTER(TsdfParams), vp, ctypes.POINTER(vp)]
@@ -212,6 +221,38 @@ def _order_after_torch(batch) -> None:
     writing the tensors being passed).  An event and a wait, no host stall."""
     import torch
     torch.cuda.ExternalStream(batch.stream()).wait_stream(torch.cuda.current_stream())
+
+
+class DeviceView:
+    """A device array owned by the library (no copy): the address, shape and
+    the stream that writes it, with enough of the tensor interface for these
+    wrappers (and __cuda_array_interface__ for torch.as_tensor)."""
+
+    is_cuda = True
+
+    def __init__(self, ptr: int, shape, typestr: str, stream: int, owner):
+        self.ptr, self.shape, self.typestr, self.stream, self.owner = ptr, tuple(shape), typestr, stream, owner
+
+    def data_ptr(self) -> int:
+        return self.ptr
+
+    def is_contiguous(self) -> bool:
+        return True
+
+    @property
+    def __cuda_array_interface__(self):
+        return {"shape": self.shape, "typestr": self.typestr, "data": (self.ptr, False), "version": 3,
+                "stream": None}
+
+
+def _after_producer(consumer, a) -> None:
+    """Orders the consumer's stream after the work that produces `a`: the
+    owning library stream of a DeviceView, else torch's current stream."""
+    if isinstance(a, DeviceView):
+        import torch
+        torch.cuda.ExternalStream(consumer.stream()).wait_stream(torch.cuda.ExternalStream(a.stream))
+    elif _on_device(a):
+        _order_after_torch(consumer)
 
 
 class Batch:
@@ -348,6 +389,31 @@ class Batch:
         self._keep = keep
         check(lib().recon_batch_set_current(self.h, ctypes.cast(g, ctypes.c_void_p),
                                             ctypes.cast(d, ctypes.c_void_p), dev))
+
+    def set_reference_oriented(self, grays, depths, points, normals):
+        """The filtered reference (recon_batch_set_reference_oriented): ICP
+        level 0 of instance i from the float4 maps points[i] / normals[i]
+        (e.g. TSDF.view("xyz") / TSDF.view("normal")), None for the raw path."""
+        g, d, dev, keep = self._ptr_tables(grays, depths)
+        p = (ctypes.c_void_p * self.n)()
+        q = (ctypes.c_void_p * self.n)()
+        for i in range(self.n):
+            if points[i] is None or normals[i] is None:
+                continue
+            pi, ni = points[i], normals[i]
+            if isinstance(pi, np.ndarray):
+                pi = np.ascontiguousarray(pi, np.float32)
+                ni = np.ascontiguousarray(ni, np.float32)
+            if _on_device(pi) != bool(dev) or _on_device(ni) != bool(dev):
+                raise ValueError("mix of host and device inputs")
+            _after_producer(self, pi)
+            _after_producer(self, ni)
+            keep += [pi, ni]
+            p[i] = _ptr(pi).value
+            q[i] = _ptr(ni).value
+        check(lib().recon_batch_set_reference_oriented(self.h, ctypes.cast(g, ctypes.c_void_p),
+                                                       ctypes.cast(d, ctypes.c_void_p), ctypes.cast(p, ctypes.c_void_p),
+                                                       ctypes.cast(q, ctypes.c_void_p), dev))
 
     def set_reference_rgbd_float4(self, inst: int, rgbd):
         a = np.ascontiguousarray(rgbd, np.float32) if isinstance(rgbd, np.ndarray) else rgbd
@@ -566,6 +632,20 @@ class Tracker(Batch):
         g, d, dev = self._frame(gray, depth)
         check(lib().recon_set_reference(self.h, _ptr(g), _ptr(d), dev))
 
+    def set_reference_oriented(self, gray, depth, points, normals):
+        """recon_set_reference_oriented: the filtered reference (ICP points and
+        normals from float4 maps, e.g. a TSDF ray cast); the relative pose
+        restarts at the identity."""
+        g, d, dev = self._frame(gray, depth)
+        if isinstance(points, np.ndarray):
+            points = np.ascontiguousarray(points, np.float32)
+            normals = np.ascontiguousarray(normals, np.float32)
+        if _on_device(points) != bool(dev) or _on_device(normals) != bool(dev):
+            raise ValueError("mix of host and device inputs")
+        _after_producer(self, points)
+        _after_producer(self, normals)
+        check(lib().recon_set_reference_oriented(self.h, _ptr(g), _ptr(d), _ptr(points), _ptr(normals), dev))
+
     def set_current(self, gray, depth):
         g, d, dev = self._frame(gray, depth)
         self._keep = [g, d]
@@ -741,6 +821,13 @@ class TSDF:
             raise ReconError(ERR_INVALID_ARG, f"unknown array {name}")
         return p
 
+    def view(self, name: str) -> DeviceView:
+        """A no-copy view of a device array ("xyz", "normal", "shaded": H x W x 4
+        float; "dist": H x W float; "tsdf": R x R x R x 2 float)."""
+        shape = {"xyz": (self.H, self.W, 4), "normal": (self.H, self.W, 4), "shaded": (self.H, self.W, 4),
+                 "dist": (self.H, self.W), "tsdf": (self.R, self.R, self.R, 2)}[name]
+        return DeviceView(self.device_array(name), shape, "<f4", self.stream(), self)
+
     def get(self, name: str) -> np.ndarray:
         if name == "tsdf":
             out = np.empty(2 * self.R ** 3, np.float32)
@@ -773,3 +860,46 @@ class TSDF:
         c = np.zeros(3, np.int64)
         check(lib().recon_tsdf_get_counts(self.h, _ptr(c), int(reset)))
         return c
+
+
+# ---- result files (ResultTxt, TrackingParams) ----
+
+class Trajectory:
+    """ResultTxt: poses added one per frame, saved canonized (relative to the
+    first) in the reference's text format.  add_identity starts the list with
+    the identity, as ResultTxt::init(fn, true) does (main.cpp:1189)."""
+
+    def __init__(self, add_identity: bool = True):
+        self.poses = [np.eye(4, dtype=np.float32)] if add_identity else []
+
+    def add_pose(self, T):
+        self.poses.append(np.asarray(T, np.float32).reshape(4, 4).copy())
+
+    def save(self, path: str, transpose: int = 1, inverse: int = 0):
+        P = np.ascontiguousarray(np.stack(self.poses) if self.poses else np.zeros((0, 4, 4), np.float32), np.float32)
+        check(lib().recon_trajectory_save(os.fsencode(path), _ptr(P), len(self.poses), transpose, inverse))
+
+
+def load_trajectory(path: str, transpose: int = 1, max_poses: int = 10000) -> np.ndarray:
+    out = np.zeros((max_poses, 4, 4), np.float32)
+    n = check(lib().recon_trajectory_load(os.fsencode(path), _ptr(out), max_poses, transpose))
+    return out[:n]
+
+
+def load_track_params(path: str, max_n: int = 100000):
+    """TrackingParams::init: [(frame, mode, lambda)] of a mode file."""
+    fr = np.zeros(max_n, np.int32)
+    md = np.zeros(max_n, np.int32)
+    la = np.zeros(max_n, np.float32)
+    n = check(lib().recon_track_params_load(os.fsencode(path), _ptr(fr), _ptr(md), _ptr(la), max_n))
+    n = min(n, max_n)
+    return [(int(fr[i]), int(md[i]), float(la[i])) for i in range(n)]
+
+
+def track_params_for(params, frame: int):
+    """TrackingParams::getParams: the entry nearest to `frame` (the first on
+    ties); (frame, GEOMETRIC, 1.0)-like default when there are none."""
+    if not params:
+        return (frame, GEOMETRIC, 1.0)
+    fr = np.ascontiguousarray([p[0] for p in params], np.int32)
+    return params[lib().recon_track_params_lookup(_ptr(fr), len(params), frame)]

@@ -24,6 +24,7 @@ __global__ void k_convert_level0(const InstDesc *D, const uint8_t *const *in_gra
                                  const float *const *in_rgbd);
 __global__ void k_downsample(const InstDesc *D, int level, const int *active);
 __global__ void k_normals(const InstDesc *D, const int *active);
+__global__ void k_oriented_points(const InstDesc *D, const float *const *in_pts, const float *const *in_nrm);
 __global__ void k_xyz2cloud(const InstDesc *D, const int *active);
 __global__ void k_seg_count(const InstDesc *D, const int *active);
 __global__ void k_seg_scan(const InstDesc *D, const int *active);
@@ -122,7 +123,8 @@ struct recon_batch {
     std::vector<InstDesc> desc;
     std::vector<void *> arenas;
     InstDesc *d_desc = nullptr;
-    // input pointer tables (3 x n) and staging for host uploads
+    // input pointer tables (5 x n: gray, depth, float4 RGB-D, oriented points,
+    // their normals) and staging for host uploads
     const void **d_inptr = nullptr;
     std::vector<const void *> h_inptr;
     int *d_active = nullptr;
@@ -291,9 +293,9 @@ int ensure_stage(recon_batch *b, size_t bytes) {
 
 // uploads host images to staging (if needed) and fills the device pointer table
 int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth, const float *const *rgbd,
-                 int on_device) {
+                 int on_device, const float *const *opts = nullptr, const float *const *onrm = nullptr) {
     int n = b->n;
-    b->h_inptr.assign(3 * (size_t)n, nullptr);
+    b->h_inptr.assign(5 * (size_t)n, nullptr);
     std::vector<int> active(n, 0);
     size_t need = 0;
     if (!on_device) {
@@ -301,6 +303,7 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
             size_t px = (size_t)b->cfg[i].width * b->cfg[i].height;
             if (rgbd && rgbd[i]) need += align256(px * 16);
             else if (gray && depth && gray[i] && depth[i]) need += align256(px) + align256(px * 2);
+            if (opts && onrm && opts[i] && onrm[i]) need += 2 * align256(px * 16);
         }
         int rc = ensure_stage(b, need ? need : 256);
         if (rc) return rc;
@@ -331,8 +334,21 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
             b->h_inptr[(size_t)n + i] = pd;
             active[i] = 1;
         }
+        if (active[i] && opts && onrm && opts[i] && onrm[i]) {
+            const void *pp = opts[i], *pn = onrm[i];
+            if (!on_device) {
+                CK(cudaMemcpyAsync(b->d_stage + off, opts[i], px * 16, cudaMemcpyHostToDevice, b->stream));
+                pp = b->d_stage + off;
+                off += align256(px * 16);
+                CK(cudaMemcpyAsync(b->d_stage + off, onrm[i], px * 16, cudaMemcpyHostToDevice, b->stream));
+                pn = b->d_stage + off;
+                off += align256(px * 16);
+            }
+            b->h_inptr[3 * (size_t)n + i] = pp;
+            b->h_inptr[4 * (size_t)n + i] = pn;
+        }
     }
-    CK(cudaMemcpyAsync(b->d_inptr, b->h_inptr.data(), 3 * (size_t)n * sizeof(void *), cudaMemcpyHostToDevice,
+    CK(cudaMemcpyAsync(b->d_inptr, b->h_inptr.data(), 5 * (size_t)n * sizeof(void *), cudaMemcpyHostToDevice,
                        b->stream));
     CK(cudaMemcpyAsync(b->d_active, active.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
     // the pageable source vectors must stay valid until the copies complete
@@ -405,7 +421,7 @@ void collect_events(recon_batch *b, std::vector<std::pair<int, std::pair<cudaEve
 // reference preparation; from_inputs: convert the staged images (else rebuild
 // from the current ref_z, keeping the keyframe gray); reset_pose: T <- I
 int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose = true,
-                      cudaStream_t st = nullptr, const int *active_flags = nullptr) {
+                      cudaStream_t st = nullptr, const int *active_flags = nullptr, bool oriented = false) {
     cudaStream_t s = st ? st : b->stream;
     TimedScope ts(b, s, TK_PREP_REF, false);
     int n = b->n;
@@ -418,6 +434,11 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
     else
         k_ref_from_z<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
     k_normals<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
+    if (oriented) {
+        k_oriented_points<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, (const float *const *)(in + 3 * n),
+                                                                   (const float *const *)(in + 4 * n));
+        g_launches += 1;
+    }
     for (int l = 1; l < b->max_L; l++)
         k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, active);
     k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, active);
@@ -672,7 +693,8 @@ int fuse_prepare(recon_batch *b, size_t cnt) {
     return RECON_OK;
 }
 
-int prepare_reference(recon_batch *b, bool from_inputs, bool reset_pose, cudaStream_t st, const int *active_flags);
+int prepare_reference(recon_batch *b, bool from_inputs, bool reset_pose, cudaStream_t st, const int *active_flags,
+                      bool oriented);
 
 // The fusion kernel and the reference rebuild on the second stream, reading
 // the device table d_fuse_ptr (depth, then gray) and poses Tdev; the pose
@@ -861,7 +883,7 @@ int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs,
         b->max_P = std::max(b->max_P, c.n_select);
     }
     cudaError_t e = cudaMalloc(&b->d_desc, n * sizeof(InstDesc));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_inptr, 3 * (size_t)n * sizeof(void *));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_inptr, 5 * (size_t)n * sizeof(void *));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_active, n * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_Tinit, 16 * (size_t)n * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_results, 32 * (size_t)n * sizeof(int));
@@ -953,6 +975,21 @@ int recon_batch_set_reference(recon_batch *b, const uint8_t *const *gray, const 
     int rc = stage_inputs(b, gray, depth, nullptr, on_device);
     if (rc) return rc;
     rc = prepare_reference(b);
+    if (rc) return rc;
+    rc = learned_keyframe(b);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    b->have_ref = true;
+    return RECON_OK;
+}
+
+int recon_batch_set_reference_oriented(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth,
+                                       const float *const *points, const float *const *normals, int32_t on_device) {
+    clear_stale_error();
+    if (!b || !gray || !depth || !points || !normals) return fail(RECON_ERR_INVALID_ARG, "null argument");
+    int rc = stage_inputs(b, gray, depth, nullptr, on_device, points, normals);
+    if (rc) return rc;
+    rc = prepare_reference(b, true, true, nullptr, nullptr, true);
     if (rc) return rc;
     rc = learned_keyframe(b);
     if (rc) return rc;
@@ -1547,6 +1584,13 @@ int recon_set_reference(recon_tracker *t, const uint8_t *gray, const uint16_t *d
     if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
     int rc = recon_batch_set_reference(t, &gray, &depth, on_device);
     if (rc == RECON_OK) identity16(t->T_host);  // prepareReference clears T (phototracker.cpp:362-368)
+    return rc;
+}
+int recon_set_reference_oriented(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, const float *points,
+                                 const float *normals, int32_t on_device) {
+    if (!t) return fail(RECON_ERR_INVALID_ARG, "null tracker");
+    int rc = recon_batch_set_reference_oriented(t, &gray, &depth, &points, &normals, on_device);
+    if (rc == RECON_OK) identity16(t->T_host);
     return rc;
 }
 int recon_set_current(recon_tracker *t, const uint8_t *gray, const uint16_t *depth, int32_t on_device) {

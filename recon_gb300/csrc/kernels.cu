@@ -395,6 +395,28 @@ __global__ void k_ref_from_z(const InstDesc *D, const int *active) {
     d.ref_pts[0][i] = o;
 }
 
+// genOrientedPoints6Kernel (d2z.cu:471-501): the filtered reference's level-0
+// ICP points and normals from a ray-cast point image and its normals (float4
+// maps of the keyframe's pixels, camera frame); replaces what k_normals wrote
+// for the instances whose point pointer is set
+__global__ void k_oriented_points(const InstDesc *D, const float *const *in_pts, const float *const *in_nrm) {
+    INST_DESC;
+    const float4 *pts = reinterpret_cast<const float4 *>(in_pts[blockIdx.y]);
+    const float4 *nrm = reinterpret_cast<const float4 *>(in_nrm[blockIdx.y]);
+    if (!pts || !nrm) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.W * d.H) return;
+    const float4 v = pts[i], n = nrm[i];
+    const float len = n.x * n.x + n.y * n.y + n.z * n.z;
+    if (v.z < 0 && len > 1e-7f) {
+        d.ref_pts[0][i] = make_float4(v.x, v.y, v.z, 1.0f);
+        d.ref_nrm[0][i] = make_float4(n.x, n.y, n.z, 0.0f);
+    } else {
+        d.ref_pts[0][i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        d.ref_nrm[0][i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
 // computeNormalsCudaKernel, d2z.cu:503-537 (reference level 0)
 __global__ void k_normals(const InstDesc *D, const int *active) {
     INST_DESC;

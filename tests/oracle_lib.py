@@ -146,6 +146,8 @@ def lib() -> ctypes.CDLL:
             L.orc_init_gate.restype = i32
             L.orc_set_pose.argtypes = [vp, vp]
             L.orc_get_pose.argtypes = [vp, vp]
+            L.orc_gen_oriented_points6.argtypes = [vp, vp, i32, i32, vp, vp]
+            L.orc_set_reference_oriented.argtypes = [vp, vp, vp, vp, vp]
             L.orc_tsdf_invert_rt4.argtypes = [vp, vp]
             L.orc_tsdf_reset.argtypes = [vp, ctypes.c_int64]
             L.orc_tsdf_dist_from_rgbd.argtypes = [vp, i32, i32, f32, f32, vp]
@@ -212,6 +214,14 @@ class OracleTracker:
         g = np.ascontiguousarray(gray, np.uint8)
         d = np.ascontiguousarray(depth, np.uint16)
         self.L.orc_set_reference(self.h, ptr(g), ptr(d))
+
+    def set_reference_oriented(self, gray, depth, points, normals):
+        """The filtered reference: ICP level 0 from float4 point and normal maps."""
+        g = np.ascontiguousarray(gray, np.uint8)
+        d = np.ascontiguousarray(depth, np.uint16)
+        p = np.ascontiguousarray(points, np.float32).reshape(-1)
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1)
+        self.L.orc_set_reference_oriented(self.h, ptr(g), ptr(d), ptr(p), ptr(n))
 
     def set_reference_float(self, gray: np.ndarray, z: np.ndarray):
         """A reference given as float gray in [0, 1] and z = -mm (0 or NaN: invalid)."""
