@@ -55,6 +55,11 @@ FRAGMENTS = {
         "trilinearWeight", "estimateLinearZero", "traverseVoxelsCuda", "rayCastVoxelsKernel", "filter3",
         "shadingKernel", "resampleVoxelsKernel", "updateVoxelsKernel", "reconstructionKernel",
     ],
+    # the Kinect pre-processing (host routines of the capture path)
+    "tracker/multicore/multicore.cpp": [
+        "void OMPFunctions::d2Z", "void OMPFunctions::d2ZLow", "void OMPFunctions::convert2Gray",
+        "void OMPFunctions::undistort", "void OMPFunctions::undistortLookup",
+    ],
     # host code: the keyframe trigger's pose test
     "tracker/tracker/phototracker.cpp": ["bool PhotoTracker::poseDifferenceExceeded"],
 }
@@ -125,10 +130,12 @@ def main() -> int:
     subprocess.run([cxx, *flags, *inc, "-c", os.path.join(ref, "tracker", "tracker", "basic_math.cpp"), "-o", bm_o],
                    check=True)
     objs.append(bm_o)
-    # the result files: ResultTxt and TrackingParams as they are, and their wrappers
+    # the result files (ResultTxt and TrackingParams as they are) and the
+    # wrappers of the result files and of the Kinect routines
     for src, obj in ((os.path.join(ref, "tracker", "calib", "ResultTxt.cpp"), "ResultTxt.o"),
                      (os.path.join(ref, "tracker", "calib", "TrackingParams.cpp"), "TrackingParams.o"),
-                     (os.path.join(HERE, "ref_files.cpp"), "ref_files.o")):
+                     (os.path.join(HERE, "ref_files.cpp"), "ref_files.o"),
+                     (os.path.join(HERE, "ref_multicore.cpp"), "ref_multicore.o")):
         o = os.path.join(OUT, obj)
         subprocess.run([cxx, *flags, *inc, "-c", src, "-o", o], check=True)
         objs.append(o)

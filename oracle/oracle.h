@@ -207,6 +207,15 @@ void orc_tsdf_raycast(const float *grid, const orc_tsdf_params *p, const float T
 void orc_tsdf_shade(const float *xyz, int W, int H, float *shaded, float *normal);
 void orc_tsdf_resample(float *dst, const float *src, const orc_tsdf_params *p, const float Tcur[16]);
 
+/* ---- Kinect pre-processing (oracle_kinect.c, tracker/multicore/multicore.cpp) ---- */
+void orc_kinect_d2z(const uint16_t *disp, int W, int H, float c0, float c1, float min_dist, float max_dist,
+                    float x_off, float y_off, float *z);
+void orc_kinect_d2z_low(const uint16_t *disp, int Wl, int Hl, float c0, float c1, float min_dist, float max_dist,
+                        float x_off, float y_off, float *z);
+void orc_kinect_rgb2gray(const uint8_t *rgb, int W, int H, uint8_t *gray);
+void orc_kinect_undistort(const uint8_t *src, int W, int H, const float *K, const float *iK, const float *kc,
+                          uint8_t *dst);
+
 /* ---- procedural scene (CPU twin of the GPU renderer) ---- */
 struct recon_scene;
 struct recon_camera;

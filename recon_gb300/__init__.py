@@ -154,6 +154,9 @@ def lib() -> ctypes.CDLL:
             L.recon_render_depth.argtypes = [vp, vp, f32, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
             L.recon_render_gray.argtypes = [vp, vp, vp, vp]
             L.recon_selftest_exact_arith.argtypes = [vp]
+            L.recon_kinect_disparity_to_depth.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, i32, vp, vp]
+            L.recon_kinect_rgb_to_gray.argtypes = [vp, i32, i32, vp, vp]
+            L.recon_kinect_undistort_gray.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp]
             L.recon_trajectory_save.argtypes = [ctypes.c_char_p, vp, i32, i32, i32]
             L.recon_trajectory_load.argtypes = [ctypes.c_char_p, vp, i32, i32]
             L.recon_trajectory_load.restype = i32
@@ -903,3 +906,47 @@ def track_params_for(params, frame: int):
         return (frame, GEOMETRIC, 1.0)
     fr = np.ascontiguousarray([p[0] for p in params], np.int32)
     return params[lib().recon_track_params_lookup(_ptr(fr), len(params), frame)]
+
+
+# ---- Kinect pre-processing (include/recon_kinect.h); torch CUDA tensors in and out ----
+
+def _stream_now():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def kinect_disparity_to_depth(disp, c0: float, c1: float, min_dist: float, max_dist: float, x_off: float = 0.0,
+                              y_off: float = 0.0, half_resolution: bool = False, out=None):
+    """OMPFunctions::d2Z / d2ZLow on the GPU: uint16 disparity [H, W] (a CUDA
+    tensor, int16 or uint16 storage) -> float depth in mm, on torch's current stream."""
+    import torch
+    H, W = disp.shape
+    shape = (H // 2, W // 2) if half_resolution else (H, W)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float32, device=disp.device)
+    check(lib().recon_kinect_disparity_to_depth(_ptr(disp), W, H, c0, c1, min_dist, max_dist, x_off, y_off,
+                                                int(half_resolution), _ptr(out), _stream_now()))
+    return out
+
+
+def kinect_rgb_to_gray(rgb, out=None):
+    """OMPFunctions::convert2Gray on the GPU: uint8 [H, W, 3] -> uint8 [H, W]."""
+    import torch
+    H, W = rgb.shape[:2]
+    if out is None:
+        out = torch.zeros((H, W), dtype=torch.uint8, device=rgb.device)
+    check(lib().recon_kinect_rgb_to_gray(_ptr(rgb), W, H, _ptr(out), _stream_now()))
+    return out
+
+
+def kinect_undistort_gray(src, K, iK, kc, out=None):
+    """OMPFunctions::undistort (lookup form) on the GPU: uint8 [H, W] -> uint8 [H, W]."""
+    import torch
+    H, W = src.shape
+    if out is None:
+        out = torch.zeros((H, W), dtype=torch.uint8, device=src.device)
+    Kf = np.ascontiguousarray(np.asarray(K, np.float32).reshape(9))
+    iKf = np.ascontiguousarray(np.asarray(iK, np.float32).reshape(9))
+    kcf = np.ascontiguousarray(np.asarray(kc, np.float32).reshape(-1)[:5])
+    check(lib().recon_kinect_undistort_gray(_ptr(src), W, H, _ptr(Kf), _ptr(iKf), _ptr(kcf), _ptr(out), _stream_now()))
+    return out

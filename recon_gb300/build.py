@@ -1,6 +1,7 @@
 """Builds librecon_track.so (sm_103a) in-tree with nvcc.
 
-Seven translation units (kernels.cu, host.cu, refshim.cu, initnet.cu, selftest.cu, tsdf.cu, trajio.cu) compiled in parallel and linked
+Eight translation units (kernels.cu, host.cu, refshim.cu, initnet.cu, selftest.cu, tsdf.cu, trajio.cu,
+kinect.cu) compiled in parallel and linked
 into recon_gb300/librecon_track.so.  -fmad=false keeps every floating-point
 multiply and add separately rounded (the bit-exactness contract of the
 kernels); -lineinfo keeps source lines for profiling.
@@ -19,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librecon_track.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-UNITS = ["kernels.cu", "host.cu", "refshim.cu", "initnet.cu", "selftest.cu", "tsdf.cu", "trajio.cu"]
+UNITS = ["kernels.cu", "host.cu", "refshim.cu", "initnet.cu", "selftest.cu", "tsdf.cu", "trajio.cu", "kinect.cu"]
 HEADERS = ["scene.h", "fx.cuh", "solve.cuh", "track_kernels.cuh", "track_math.cuh", "exact_arith.cuh"]
 
 
@@ -36,6 +37,7 @@ def _sources():
     srcs.append(os.path.join(ROOT, "include", "recon_ref_shim.h"))
     srcs.append(os.path.join(ROOT, "include", "recon_initnet.h"))
     srcs.append(os.path.join(ROOT, "include", "recon_tsdf.h"))
+    srcs.append(os.path.join(ROOT, "include", "recon_kinect.h"))
     srcs.append(os.path.abspath(__file__))
     return srcs
 

@@ -146,6 +146,10 @@ def lib() -> ctypes.CDLL:
             L.orc_init_gate.restype = i32
             L.orc_set_pose.argtypes = [vp, vp]
             L.orc_get_pose.argtypes = [vp, vp]
+            L.orc_kinect_d2z.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, vp]
+            L.orc_kinect_d2z_low.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, vp]
+            L.orc_kinect_rgb2gray.argtypes = [vp, i32, i32, vp]
+            L.orc_kinect_undistort.argtypes = [vp, i32, i32, vp, vp, vp, vp]
             L.orc_gen_oriented_points6.argtypes = [vp, vp, i32, i32, vp, vp]
             L.orc_set_reference_oriented.argtypes = [vp, vp, vp, vp, vp]
             L.orc_tsdf_invert_rt4.argtypes = [vp, vp]

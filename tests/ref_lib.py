@@ -50,6 +50,10 @@ def lib() -> ctypes.CDLL:
         L.ref_poseDifferenceExceeded.restype = i32
         L.ref_applyIncrement.argtypes = [vp, vp, vp]
         L.ref_genOrientedPoints6.argtypes = [vp, vp, i32, i32, vp, vp, vp]
+        L.ref_d2Z.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, vp]
+        L.ref_d2ZLow.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, vp]
+        L.ref_convert2Gray.argtypes = [vp, i32, i32, vp]
+        L.ref_undistort.argtypes = [vp, i32, i32, vp, vp, vp, i32, vp]
         L.ref_result_save.argtypes = [ctypes.c_char_p, vp, i32, i32, i32, i32]
         L.ref_track_params_get.argtypes = [ctypes.c_char_p, i32, vp, vp, vp]
         L.ref_tsdf_reset.argtypes = [vp, i32]
