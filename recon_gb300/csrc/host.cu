@@ -434,6 +434,10 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
     else
         k_ref_from_z<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
     k_normals<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
+    // the photometric vertex records take the level-0 points of the depth
+    // (both reference paths); only then may oriented points replace them for ICP
+    k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, active);
+    k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
     if (oriented) {
         k_oriented_points<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, (const float *const *)(in + 3 * n),
                                                                    (const float *const *)(in + 4 * n));
@@ -441,8 +445,6 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
     }
     for (int l = 1; l < b->max_L; l++)
         k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, active);
-    k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, active);
-    k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
     k_seg_count<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, active);
     k_seg_scan<<<dim3(1, n), 32, 0, s>>>(D, active);
     k_seg_scatter<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, active);
