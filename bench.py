@@ -532,7 +532,7 @@ def profiled_traffic():
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
                 return float(line.split(":")[1])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
 
