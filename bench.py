@@ -738,6 +738,70 @@ def tsdf_arm(args, torch, seed=77):
     }
 
 
+def kinect_arm(args, torch, seed=91, frames=30):
+    """Kinect pre-processing (multicore.cpp routines) on the GPU: per frame the
+    disparity -> depth conversion (full resolution, the (-4, -3) shift), RGB ->
+    gray and the gray undistortion of a 640x480 frame, device buffers, CUDA
+    events on torch's stream; the oracle's per-frame time beside it and the
+    last frame checked bit for bit against it."""
+    import recon_gb300 as rg
+    from recon_gb300 import synth
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    rng = np.random.default_rng(seed)
+    cal = synth.make_calibration(W, H, distortion=True)
+    c0, c1 = float(cal.calib[61]), float(cal.calib[42])
+    disp = rng.integers(280, 1040, (frames, H, W)).astype(np.uint16)
+    disp[rng.random((frames, H, W)) < 0.05] = 2047
+    rgb = rng.integers(0, 256, (frames, H, W, 3)).astype(np.uint8)
+    K = np.ascontiguousarray(cal.calib[0:9], np.float32)
+    iK = np.ascontiguousarray(cal.calib[9:18], np.float32)
+    kc = np.ascontiguousarray(cal.calib[18:23], np.float32)
+    d_disp = torch.from_numpy(disp.view(np.int16)).cuda()
+    d_rgb = torch.from_numpy(rgb).cuda()
+    z = torch.empty((frames, H, W), dtype=torch.float32, device="cuda")
+    gray = torch.zeros((frames, H, W), dtype=torch.uint8, device="cuda")
+    und = torch.zeros((frames, H, W), dtype=torch.uint8, device="cuda")
+
+    def step():
+        for f in range(frames):
+            rg.kinect_disparity_to_depth(d_disp[f], c0, c1, cal.min_dist, cal.max_dist, -4.0, -3.0, out=z[f])
+            rg.kinect_rgb_to_gray(d_rgb[f], out=gray[f])
+            rg.kinect_undistort_gray(gray[f], K, iK, kc, out=und[f])
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps / frames
+    # the oracle on the last frame (and its time per frame, one thread)
+    f = frames - 1
+    t0 = time.perf_counter()
+    zo = np.zeros((H, W), np.float32)
+    dispf = np.ascontiguousarray(disp[f])
+    O.lib().orc_kinect_d2z(O.ptr(dispf), W, H, c0, c1, cal.min_dist, cal.max_dist, -4.0, -3.0, O.ptr(zo))
+    go = np.zeros((H, W), np.uint8)
+    rgbf = np.ascontiguousarray(rgb[f])
+    O.lib().orc_kinect_rgb2gray(O.ptr(rgbf), W, H, O.ptr(go))
+    uo = np.zeros((H, W), np.uint8)
+    O.lib().orc_kinect_undistort(O.ptr(go), W, H, O.ptr(K), O.ptr(iK), O.ptr(kc), O.ptr(uo))
+    cpu_ms = 1000.0 * (time.perf_counter() - t0)
+    same = (np.array_equal(z[f].cpu().numpy().view(np.uint32), zo.view(np.uint32))
+            and np.array_equal(gray[f].cpu().numpy(), go) and np.array_equal(und[f].cpu().numpy(), uo))
+    return {"workload": f"{frames} frames of 640x480: 11-bit disparity -> depth (shift -4, -3), RGB -> gray, gray "
+                        "undistortion (radial), device buffers",
+            "frames_per_s": 1000.0 / ms, "us_per_frame": 1000.0 * ms,
+            "bytes_per_frame": W * H * (2 + 4 + 3 + 1 + 1 + 1),
+            "bit_identical_to_oracle": bool(same),
+            "cpu_baseline": {"kind": "port", "cores": 1, "ms_per_frame": cpu_ms,
+                             "sample": "the oracle's three routines on one frame, one thread"}}
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -753,10 +817,12 @@ def main():
     seed = rank_seed(rank)
     if args.tsdf_only:
         out = tsdf_arm(args, torch)
+        kin = kinect_arm(args, torch)
         if rank == 0:
             print(json.dumps({"metric": "reconstruction frames/s (TSDF update + ray cast), 256^3 grid, 640x480",
                               "unit": "frames/s", "value": out["frames_per_s"], "n_gpus": world,
-                              "steps": args.steps, "warmup": args.warmup, "tsdf": out}), flush=True)
+                              "steps": args.steps, "warmup": args.warmup, "tsdf": out,
+                              "kinect_preprocessing": kin}), flush=True)
         if world > 1:
             torch.distributed.destroy_process_group()
         return 0
@@ -966,6 +1032,7 @@ def main():
         batched = batch_arm(args, torch, world, rank, 5000 + 7919 * rank)
     c1 = config1_arm(args, torch) if rank == 0 and not args.no_cpu else None
     recon_stream = tsdf_arm(args, torch) if rank == 0 and not args.no_tsdf else None
+    kinect = kinect_arm(args, torch) if rank == 0 and not args.no_tsdf else None
     clk.__exit__(None, None, None)
     if net is not None:
         batch.set_init_net(None)
@@ -1038,6 +1105,7 @@ def main():
             "mixed_precision": mixed,
             "config1": c1,
             "reconstruction": recon_stream,
+            "kinect_preprocessing": kinect,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

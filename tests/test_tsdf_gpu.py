@@ -138,3 +138,22 @@ def test_tsdf_argument_errors():
     assert np.all(v.get("tsdf")[0::2] == 1.0)
     other.close()
     v.close()
+
+
+def test_tsdf_traversal_edge_cases_match_oracle():
+    """A camera inside the grid, axis-aligned poses and rays with an exactly
+    zero direction component (the traversal's FLT_MAX inverse) on the GPU."""
+    import recon_gb300 as rg
+    from test_tsdf_oracle import edge_case_setup
+    s, K, poses, p = edge_case_setup()
+    o = O.OracleTSDF(p)
+    v = rg.TSDF(rg.tsdf_params(p.R, p.W, p.H, cube_origin=tuple(p.origin), cube_dim=tuple(p.dim)))
+    for f in range(3):
+        v.set_dist_map(s.dist[f])
+        v.update(poses[f], K)
+        o.update(s.dist[f], poses[f], K)
+    assert np.array_equal(bits(v.get("tsdf")), bits(o.grid))
+    for f in range(3):
+        v.raycast(poses[f], K)
+        assert np.array_equal(bits(v.get("xyz")), bits(o.raycast(poses[f], K))), f
+    v.close()

@@ -176,3 +176,56 @@ def test_invert_rt4_is_the_reference_formula():
         t = T[:3, 3]
         expect = np.float32(0) - (R[0, 0] * t[0] + R[1, 0] * t[1] + R[2, 0] * t[2])
         assert Ti[3] == expect
+
+
+def edge_case_setup(R=64, W=160, H=120):
+    """A camera inside the grid, axis-aligned poses and intrinsics whose
+    principal point falls on a pixel centre: the rays of that column / row
+    have an exactly zero direction component (the traversal's FLT_MAX
+    inverse), and rays start inside the grid (entry parameter 0)."""
+    s = depth_sequence(W, H, 3, seed=12, noise=0.0)
+    # a wall 1.5 m ahead of the first pose, seen by all three
+    s.dist = [np.full((H, W), 1500.0, np.float32) for _ in range(3)]
+    K = s.K.copy()
+    K[2] = np.float32(80.0) / np.float32(W)  # column 80 looks straight ahead
+    K[5] = np.float32(60.0) / np.float32(H)  # row 60 too
+    poses = [np.eye(4, dtype=np.float32)]
+    Ry = np.eye(4, dtype=np.float32)
+    Ry[:3, :3] = np.array([[0, 0, 1], [0, 1, 0], [-1, 0, 0]], np.float32)  # 90 degrees about y
+    poses.append(Ry)
+    T = np.eye(4, dtype=np.float32)
+    T[:3, 3] = [40.0, -25.0, -60.0]
+    poses.append(T)
+    p = O.tsdf_params(R, W, H, origin=(0.0, 0.0, -1000.0), dim=(1500.0, 1500.0, 1500.0))
+    return s, K, poses, p
+
+
+@needs_ref
+def test_traversal_edge_cases_match_reference():
+    s, K, poses, p = edge_case_setup()
+    W, H, R = p.W, p.H, p.R
+    o = O.OracleTSDF(p)
+    L = RL.lib()
+    ref = np.zeros_like(o.grid)
+    L.ref_tsdf_reset(O.ptr(ref), R ** 3)
+    org = np.array(p.origin, np.float32)
+    dm = np.array(p.dim, np.float32)
+    Kc = np.ascontiguousarray(K)
+    for f in range(3):
+        Tf = np.ascontiguousarray(poses[f].reshape(-1))
+        d = np.ascontiguousarray(s.dist[f].reshape(-1))
+        o.update(d, Tf, Kc)
+        L.ref_tsdf_update(O.ptr(ref), R, O.ptr(org), O.ptr(dm), W, H, p.min_dist, p.max_dist, O.ptr(Tf), O.ptr(Kc),
+                          O.ptr(d))
+        assert np.array_equal(bits(ref), bits(o.grid)), f
+    for f in range(3):
+        Tf = np.ascontiguousarray(poses[f].reshape(-1))
+        xyz = o.raycast(Tf, Kc)
+        xr = np.zeros_like(xyz)
+        L.ref_tsdf_raycast(O.ptr(ref), R, O.ptr(org), O.ptr(dm), W, H, p.min_dist, p.max_dist, O.ptr(Tf), O.ptr(Kc),
+                           1, O.ptr(xr))
+        assert np.array_equal(bits(xyz), bits(xr)), f
+        if f != 1:
+            # the straight-ahead column and row hit the wall (their rays have a zero component)
+            img = xyz.reshape(H, W, 4)
+            assert img[3:-3, 80, 3].all() and img[60, 3:-3, 3].all(), f
