@@ -772,10 +772,22 @@ def kinect_arm(args, torch, seed=91, frames=30):
     for _ in range(max(args.warmup, 1)):
         step()
     torch.cuda.synchronize()
+    # the 90 launches of a step captured once and replayed, so that the time is
+    # the device's and not the Python loop's
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph):
+            step()
+    torch.cuda.synchronize()
+    for _ in range(max(args.warmup, 1)):
+        graph.replay()
+    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.steps):
-        step()
+        graph.replay()
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps / frames
@@ -794,7 +806,7 @@ def kinect_arm(args, torch, seed=91, frames=30):
     same = (np.array_equal(z[f].cpu().numpy().view(np.uint32), zo.view(np.uint32))
             and np.array_equal(gray[f].cpu().numpy(), go) and np.array_equal(und[f].cpu().numpy(), uo))
     return {"workload": f"{frames} frames of 640x480: 11-bit disparity -> depth (shift -4, -3), RGB -> gray, gray "
-                        "undistortion (radial), device buffers",
+                        "undistortion (radial), device buffers, the step's launches replayed as a CUDA graph",
             "frames_per_s": 1000.0 / ms, "us_per_frame": 1000.0 * ms,
             "bytes_per_frame": W * H * (2 + 4 + 3 + 1 + 1 + 1),
             "bit_identical_to_oracle": bool(same),
