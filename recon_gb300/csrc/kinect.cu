@@ -133,14 +133,22 @@ int fail(int code, const char *msg) {
     return code;
 }
 
-int launched() {
-    rt::add_launches(1);
-    cudaError_t e = cudaGetLastError();
+// Launches through cudaLaunchKernelEx, whose return value is the launch's own
+// status: an error another part of the process left pending is neither
+// reported as this library's nor cleared.
+template <typename... KArgs, typename... Args>
+int launch(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = s;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
     if (e != cudaSuccess) {
         std::string m = std::string("kernel launch: ") + cudaGetErrorString(e);
         rt::set_last_error(m.c_str());
         return RECON_ERR_CUDA;
     }
+    rt::add_launches(1);
     return RECON_OK;
 }
 
@@ -156,42 +164,35 @@ int recon_kinect_disparity_to_depth(const uint16_t *disp, int32_t width, int32_t
     if (!disp || !z || width < 2 || height < 2 || width > 16384 || height > 16384)
         return fail(RECON_ERR_INVALID_ARG, "bad argument");
     if (half_resolution && (width % 2 || height % 2)) return fail(RECON_ERR_INVALID_ARG, "odd disparity size");
-    (void)cudaGetLastError();
     cudaStream_t s = (cudaStream_t)stream;
     dim3 blk(32, 8);
     if (half_resolution) {
         const int Wl = width / 2, Hl = height / 2;
-        k_d2z_low<<<dim3((Wl + 31) / 32, (Hl + 7) / 8), blk, 0, s>>>(disp, Wl, Hl, c0, c1, min_dist, max_dist, x_off,
-                                                                      y_off, z);
-    } else {
-        k_d2z<<<dim3((width + 31) / 32, (height + 7) / 8), blk, 0, s>>>(disp, width, height, c0, c1, min_dist, max_dist,
-                                                                         x_off, y_off, z);
+        return launch(k_d2z_low, dim3((Wl + 31) / 32, (Hl + 7) / 8), blk, s, disp, Wl, Hl, c0, c1, min_dist, max_dist,
+                      x_off, y_off, z);
     }
-    return launched();
+    return launch(k_d2z, dim3((width + 31) / 32, (height + 7) / 8), blk, s, disp, width, height, c0, c1, min_dist,
+                  max_dist, x_off, y_off, z);
 }
 
 int recon_kinect_rgb_to_gray(const uint8_t *rgb, int32_t width, int32_t height, uint8_t *gray, void *stream) {
     if (!rgb || !gray || width < 1 || height < 1) return fail(RECON_ERR_INVALID_ARG, "bad argument");
-    (void)cudaGetLastError();
     const int n = 4 * width * (height / 4);
     if (n == 0) return RECON_OK;
-    k_rgb2gray<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(rgb, n, gray);
-    return launched();
+    return launch(k_rgb2gray, dim3((n + 255) / 256), dim3(256), (cudaStream_t)stream, rgb, n, gray);
 }
 
 int recon_kinect_undistort_gray(const uint8_t *src, int32_t width, int32_t height, const float K[9], const float iK[9],
                                 const float kc[5], uint8_t *dst, void *stream) {
     if (!src || !dst || !K || !iK || !kc || width < 4 || height < 6) return fail(RECON_ERR_INVALID_ARG, "bad argument");
-    (void)cudaGetLastError();
     KinectUndistort u;
     for (int i = 0; i < 9; i++) {
         u.K[i] = K[i];
         u.iK[i] = iK[i];
     }
     for (int i = 0; i < 5; i++) u.kc[i] = kc[i];
-    k_undistort<<<dim3((width + 31) / 32, (6 * (height / 6) + 7) / 8), dim3(32, 8), 0, (cudaStream_t)stream>>>(
-        src, width, height, u, dst);
-    return launched();
+    return launch(k_undistort, dim3((width + 31) / 32, (6 * (height / 6) + 7) / 8), dim3(32, 8), (cudaStream_t)stream, src,
+                  width, height, u, dst);
 }
 
 }  // extern "C"

@@ -762,10 +762,18 @@ struct Timed {
     }
 };
 
-int launched(int n) {
-    rt::add_launches(n);
-    cudaError_t e = cudaGetLastError();
+// Launches through cudaLaunchKernelEx, whose return value is the launch's own
+// status: an error another part of the process left pending is neither
+// reported as this library's nor cleared.
+template <typename... KArgs, typename... Args>
+int launch(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = s;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    rt::add_launches(1);
     return RECON_OK;
 }
 
@@ -797,8 +805,7 @@ int ensure_staging(recon_tsdf *v, size_t bytes) {
 int rebuild_flags(recon_tsdf *v, float2 *grid, uint8_t *flags) {
     TCK(cudaMemsetAsync(flags, 0, n_flag_bytes(v->p), v->stream));
     Geom g = make_geom(v->p, nullptr, nullptr);
-    k_flags<<<1216, 256, 0, v->stream>>>(grid, flags, g);
-    return launched(1);
+    return launch(k_flags, dim3(1216), dim3(256), v->stream, grid, flags, g);
 }
 
 }  // namespace
@@ -834,7 +841,7 @@ int recon_tsdf_create(const recon_tsdf_params *p, void *stream, recon_tsdf **out
     if (!(p->min_dist >= 0.0f && p->max_dist > p->min_dist)) return fail(RECON_ERR_INVALID_ARG, "need 0 <= min_dist < max_dist");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-        (void)cudaGetLastError();
+        (void)cudaGetLastError();  // this call's own error
         return fail(RECON_ERR_NO_DEVICE, "no CUDA device");
     }
     recon_tsdf *v = new recon_tsdf();
@@ -899,11 +906,9 @@ int recon_tsdf_destroy(recon_tsdf *v) {
 
 int recon_tsdf_reset(recon_tsdf *v) {
     if (!v) return fail(RECON_ERR_INVALID_ARG, "NULL grid");
-    (void)cudaGetLastError();
     Timed tm(v, 4);
     TCK(cudaMemsetAsync(v->flags, 0, n_flag_bytes(v->p), v->stream));
-    k_reset<<<152 * 8, 256, 0, v->stream>>>(reinterpret_cast<float4 *>(v->grid), n_voxels(v->p) / 2);
-    return launched(1);
+    return launch(k_reset, dim3(152 * 8), dim3(256), v->stream, reinterpret_cast<float4 *>(v->grid), n_voxels(v->p) / 2);
 }
 
 int recon_tsdf_set_dist_map(recon_tsdf *v, const float *dist, int32_t on_device) {
@@ -915,7 +920,6 @@ int recon_tsdf_set_dist_map(recon_tsdf *v, const float *dist, int32_t on_device)
 
 int recon_tsdf_set_dist_rgbd_float4(recon_tsdf *v, const float *rgbd, int32_t on_device) {
     if (!v || !rgbd) return fail(RECON_ERR_INVALID_ARG, "NULL argument");
-    (void)cudaGetLastError();
     const float4 *src = reinterpret_cast<const float4 *>(rgbd);
     if (!on_device) {
         int rc = ensure_staging(v, n_pixels(v->p) * sizeof(float4));
@@ -925,13 +929,11 @@ int recon_tsdf_set_dist_rgbd_float4(recon_tsdf *v, const float *rgbd, int32_t on
     }
     Timed tm(v, 3);
     dim3 blk(32, 8), grd((v->p.width + 31) / 32, (v->p.height + 7) / 8);
-    k_dist_rgbd<<<grd, blk, 0, v->stream>>>(src, v->p.width, v->p.height, v->p.min_dist, v->p.max_dist, v->dist);
-    return launched(1);
+    return launch(k_dist_rgbd, grd, blk, v->stream, src, v->p.width, v->p.height, v->p.min_dist, v->p.max_dist, v->dist);
 }
 
 int recon_tsdf_set_dist_depth16(recon_tsdf *v, const uint16_t *depth, int32_t on_device) {
     if (!v || !depth) return fail(RECON_ERR_INVALID_ARG, "NULL argument");
-    (void)cudaGetLastError();
     const uint16_t *src = depth;
     if (!on_device) {
         int rc = ensure_staging(v, n_pixels(v->p) * sizeof(uint16_t));
@@ -940,15 +942,14 @@ int recon_tsdf_set_dist_depth16(recon_tsdf *v, const uint16_t *depth, int32_t on
         src = reinterpret_cast<const uint16_t *>(v->staging);
     }
     Timed tm(v, 3);
-    k_dist_depth16<<<(unsigned)((n_pixels(v->p) + 255) / 256), 256, 0, v->stream>>>(src, n_pixels(v->p), v->dist);
-    return launched(1);
+    return launch(k_dist_depth16, dim3((unsigned)((n_pixels(v->p) + 255) / 256)), dim3(256), v->stream, src,
+                  n_pixels(v->p), v->dist);
 }
 
 int recon_tsdf_update(recon_tsdf *v, const float T[16], const float K[9]) {
     if (!v || !K) return fail(RECON_ERR_INVALID_ARG, "NULL argument");
     int rc = check_pose(T, K);
     if (rc) return rc;
-    (void)cudaGetLastError();
     float Tin[16], Tw2c[16];
     memcpy(Tin, T, sizeof(Tin));
     invert_rt4(Tin, Tw2c);
@@ -957,29 +958,26 @@ int recon_tsdf_update(recon_tsdf *v, const float T[16], const float K[9]) {
     dim3 grd((R + kTileX - 1) / kTileX, R / kTileY, R / kRunZ);
     Timed tm(v, 0);
     if (v->counting)
-        k_update<true><<<grd, kTileX * kTileY, 0, v->stream>>>(v->grid, v->flags, v->dist, g, v->counts);
-    else
-        k_update<false><<<grd, kTileX * kTileY, 0, v->stream>>>(v->grid, v->flags, v->dist, g, nullptr);
-    return launched(1);
+        return launch(k_update<true>, grd, dim3(kTileX * kTileY), v->stream, v->grid, v->flags, v->dist, g, v->counts);
+    return launch(k_update<false>, grd, dim3(kTileX * kTileY), v->stream, v->grid, v->flags, v->dist, g,
+                  (unsigned long long *)nullptr);
 }
 
 int recon_tsdf_raycast(recon_tsdf *v, const float T[16], const float K[9], int32_t cubic_filter) {
     if (!v || !K) return fail(RECON_ERR_INVALID_ARG, "NULL argument");
     int rc = check_pose(T, K);
     if (rc) return rc;
-    (void)cudaGetLastError();
     Geom g = make_geom(v->p, T, K);
     dim3 grd((v->p.width + kRayTileX - 1) / kRayTileX, (v->p.height + kRayTileY - 1) / kRayTileY);
     {
         Timed tm(v, 1);
-        k_raycast<<<grd, kRayTileX * kRayTileY, 0, v->stream>>>(v->grid, v->flags, g, cubic_filter ? 3 : 0, v->xyz);
-        rc = launched(1);
+        rc = launch(k_raycast, grd, dim3(kRayTileX * kRayTileY), v->stream, v->grid, v->flags, g, cubic_filter ? 3 : 0,
+                    v->xyz);
         if (rc) return rc;
     }
     Timed tm(v, 2);
     dim3 blk(32, 8), grd2((v->p.width + 31) / 32, (v->p.height + 7) / 8);
-    k_shade<<<grd2, blk, 0, v->stream>>>(v->xyz, v->p.width, v->p.height, v->shaded, v->normal);
-    return launched(1);
+    return launch(k_shade, grd2, blk, v->stream, v->xyz, v->p.width, v->p.height, v->shaded, v->normal);
 }
 
 int recon_tsdf_resample(recon_tsdf *dst, recon_tsdf *src, const float T[16]) {
@@ -988,7 +986,6 @@ int recon_tsdf_resample(recon_tsdf *dst, recon_tsdf *src, const float T[16]) {
         return fail(RECON_ERR_INVALID_ARG, "the grids have different parameters");
     int rc = check_pose(T, nullptr);
     if (rc) return rc;
-    (void)cudaGetLastError();
     if (src->stream != dst->stream) {
         cudaEvent_t e;
         TCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1000,8 +997,7 @@ int recon_tsdf_resample(recon_tsdf *dst, recon_tsdf *src, const float T[16]) {
     const int R = dst->p.grid_resolution;
     {
         Timed tm(dst, 4);
-        k_resample<<<dim3((R + 127) / 128, R, R), 128, 0, dst->stream>>>(dst->grid, src->grid, g);
-        rc = launched(1);
+        rc = launch(k_resample, dim3((R + 127) / 128, R, R), dim3(128), dst->stream, dst->grid, src->grid, g);
         if (rc) return rc;
     }
     rc = rebuild_flags(dst, dst->grid, dst->flags);
@@ -1049,7 +1045,6 @@ int64_t recon_tsdf_get(recon_tsdf *v, const char *name, void *host_dst, int64_t 
 
 int recon_tsdf_set_grid(recon_tsdf *v, const float *grid, int32_t on_device) {
     if (!v || !grid) return fail(RECON_ERR_INVALID_ARG, "NULL argument");
-    (void)cudaGetLastError();
     TCK(cudaMemcpyAsync(v->grid, grid, n_voxels(v->p) * sizeof(float2),
                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, v->stream));
     return rebuild_flags(v, v->grid, v->flags);
@@ -1076,7 +1071,6 @@ int recon_tsdf_get_timing(recon_tsdf *v, double ms[5], int64_t launches[5], int3
         v->spare.push_back(pe.second.second);
     }
     v->pending.clear();
-    (void)cudaGetLastError();
     for (int k = 0; k < kKinds; k++) {
         if (ms) ms[k] = v->ms[k];
         if (launches) launches[k] = v->launches[k];
