@@ -1345,13 +1345,43 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     // copy frame f into its slot on the copy stream (ev_copied[f & 1] marks it;
     // frame f's copies are issued after frame f - 1's, so the event recorded
     // later on the same stream also covers the earlier frames)
+    // one 2-D copy per image kind when the instances' host images of a frame
+    // and their slots are evenly spaced with one size (frames picked from one
+    // stack at a fixed step), else one copy per image
+    auto strided = [&](const void *const *src, int f, int kind, size_t bytes, size_t *spitch, size_t *dpitch) {
+        if (n < 2) return false;
+        const char *s0 = (const char *)src[(size_t)f * n], *d0 = (const char *)b->h_seqptr[(size_t)f * 3 * n + kind * n];
+        const char *s1 = (const char *)src[(size_t)f * n + 1], *d1 = (const char *)b->h_seqptr[(size_t)f * 3 * n + kind * n + 1];
+        if (s1 <= s0 || d1 <= d0) return false;
+        size_t sp = (size_t)(s1 - s0), dp = (size_t)(d1 - d0);
+        if (sp < bytes || dp < bytes) return false;
+        for (int i = 0; i < n; i++) {
+            if (px[i] != px[0]) return false;
+            if ((const char *)src[(size_t)f * n + i] != s0 + i * sp) return false;
+            if ((const char *)b->h_seqptr[(size_t)f * 3 * n + kind * n + i] != d0 + i * dp) return false;
+        }
+        *spitch = sp;
+        *dpitch = dp;
+        return true;
+    };
     auto stage = [&](int f) -> int {
         if (on_device) return RECON_OK;
-        for (int i = 0; i < n; i++) {
-            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + i], gray[(size_t)f * n + i], px[i],
-                               cudaMemcpyHostToDevice, b->copy_stream));
-            CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + n + i], depth[(size_t)f * n + i],
-                               2 * px[i], cudaMemcpyHostToDevice, b->copy_stream));
+        size_t sp, dp;
+        if (strided((const void *const *)gray, f, 0, px[0], &sp, &dp)) {
+            CK(cudaMemcpy2DAsync((void *)b->h_seqptr[(size_t)f * 3 * n], dp, gray[(size_t)f * n], sp, px[0], n,
+                                 cudaMemcpyHostToDevice, b->copy_stream));
+        } else {
+            for (int i = 0; i < n; i++)
+                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + i], gray[(size_t)f * n + i], px[i],
+                                   cudaMemcpyHostToDevice, b->copy_stream));
+        }
+        if (strided((const void *const *)depth, f, 1, 2 * px[0], &sp, &dp)) {
+            CK(cudaMemcpy2DAsync((void *)b->h_seqptr[(size_t)f * 3 * n + n], dp, depth[(size_t)f * n], sp, 2 * px[0], n,
+                                 cudaMemcpyHostToDevice, b->copy_stream));
+        } else {
+            for (int i = 0; i < n; i++)
+                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + n + i], depth[(size_t)f * n + i],
+                                   2 * px[i], cudaMemcpyHostToDevice, b->copy_stream));
         }
         CK(cudaEventRecord(b->ev_copied[f & 1], b->copy_stream));
         return RECON_OK;
