@@ -5,9 +5,12 @@
  *
  * Everything is computed in FP64.  With exact = 0 the values the GPU stores in
  * BF16 (convolution weights and activations) are rounded to BF16 (round to
- * nearest even) at the same points, so GPU and oracle agree to FP32
- * accumulation-order rounding; with exact = 1 nothing is rounded and the
- * gradient is the exact derivative of the FP64 loss (for finite differences).
+ * nearest even) at the same points, and so are the pre-activation gradients
+ * where the backward pass multiplies them on the tensor cores (the weight and
+ * input gradients; the bias gradient sums them unrounded), so GPU and oracle
+ * agree to FP32 accumulation-order rounding; with exact = 1 nothing is rounded
+ * and the gradient is the exact derivative of the FP64 loss (for finite
+ * differences).
  */
 #include <math.h>
 #include <stdint.h>
@@ -207,11 +210,12 @@ double orc_net_loss_grad(const float *params, const uint16_t *in, const float *t
                         double d = dz[(((int64_t)nn * Ho + oy) * Wo + ox) * Cout + co];
                         if (d == 0.0) continue;
                         grad[o.b[l] + co] += d;
+                        double dr = rbf(d, exact);
                         for (int k = 0; k < 9 * Cin; k++) {
                             int tap = k / Cin, c = k % Cin, ky = tap / 3, kx = tap % 3;
                             int iy = 2 * oy - 1 + ky, ix = 2 * ox - 1 + kx;
                             if (iy < 0 || iy >= H || ix < 0 || ix >= W) continue;
-                            grad[o.w[l] + co * Kp + k] += d * lin[(((int64_t)nn * H + iy) * W + ix) * Cin + c];
+                            grad[o.w[l] + co * Kp + k] += dr * lin[(((int64_t)nn * H + iy) * W + ix) * Cin + c];
                         }
                     }
         if (l == 0) break;
@@ -222,6 +226,7 @@ double orc_net_loss_grad(const float *params, const uint16_t *in, const float *t
                     for (int co = 0; co < Cout; co++) {
                         double d = dz[(((int64_t)nn * Ho + oy) * Wo + ox) * Cout + co];
                         if (d == 0.0) continue;
+                        d = rbf(d, exact);
                         for (int k = 0; k < 9 * Cin; k++) {
                             int tap = k / Cin, c = k % Cin, ky = tap / 3, kx = tap % 3;
                             int iy = 2 * oy - 1 + ky, ix = 2 * ox - 1 + kx;

@@ -1,6 +1,7 @@
 // initnet.cu -- the learned initialisation network (include/recon_initnet.h):
 // BF16 tensor-core convolutions (mma.sync m16n8k16, FP32 accumulation) for the
-// forward pass, FP32 CUDA-core kernels for the backward pass and Adam.
+// forward pass and for the backward pass's weight and input gradients, FP32
+// CUDA-core kernels for the head and Adam.
 //
 // Every kernel reduces in a fixed order (no floating-point atomics), so a
 // training run is deterministic.  The shapes are small (about 10 MFLOP per
@@ -323,32 +324,137 @@ __global__ void k_head_back(const float *y, const float *t, const float *wfc, co
     }
 }
 
-// weight and bias gradients of a convolution, split over the output pixels:
-// partial[s][co][k] for k < Kp (k = Kp: the bias)
-__global__ void k_conv_wgrad(const float *dz, const __nv_bfloat16 *in, int N, int H, int W, int Cin, int Kp, int Cout,
-                             int Ho, int Wo, int nsplit, float *partial) {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    int s = blockIdx.y;
-    int row = Kp + 1;
-    if (idx >= Cout * row) return;
-    int co = idx / row, k = idx % row;
+// two FP32 values rounded to BF16 (round to nearest even) in one 32-bit word,
+// the first in the low half (the mma.sync operand order)
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Weight and bias gradients of a convolution on the tensor cores:
+// gW[co][k] = sum_m dz[m][co] X[m][k], X the 3x3 / stride 2 / pad 1 patches
+// of the layer input (k = tap * Cin + c), a GEMM whose reduction runs over
+// the output pixels m, with BF16 operands (dz rounded to nearest even) and
+// FP32 accumulation (mma.sync m16n8k16).  CTA (x, s) computes columns
+// [64 x, 64 x + 64) for every co over split s of the pixels, staging 64 pixels
+// at a time in shared memory transposed (two consecutive pixels per 32-bit
+// word, rows padded so that fragment loads hit distinct banks).  Warp w owns
+// fragment tiles [w FPW, (w + 1) FPW) of the (co / 16) x (column / 8) grid.
+// Writes partial[s][co][k] for k < Kp and, from CTA column 0, the bias
+// gradient at k = Kp: the split's FP32 sum of dz (each thread adds its pixel
+// pairs in order, the threads of a co are then added in thread order).
+constexpr int kWgKT = 64, kWgMS = 64, kWgThreads = 128;
+template <int COUT>
+__global__ void __launch_bounds__(kWgThreads) k_conv_wgrad_tc(const float *dz, const __nv_bfloat16 *in, int N,
+                                                              int H, int W, int Cin, int Kp, int Ho, int Wo,
+                                                              int nsplit, float *partial) {
+    constexpr int RT = COUT / 16, FPW = RT * 2;  // 8 column fragments per row tile, over 4 warps
+    constexpr int LD = kWgMS / 2 + 4;            // words per staged row
+    constexpr int TPC = kWgThreads / COUT;       // threads per co in the staging of dz
+    static_assert(kWgThreads % COUT == 0 && RT * 8 == 4 * FPW, "tile split");
+    __shared__ uint32_t sD[COUT][LD];
+    __shared__ uint32_t sX[kWgKT][LD];
+    __shared__ int s_n[kWgMS], s_oy[kWgMS], s_ox[kWgMS];
+    __shared__ int s_c[kWgKT], s_ky[kWgKT], s_kx[kWgKT];
+    __shared__ float s_bias[kWgThreads];
+    const uint16_t *inb = reinterpret_cast<const uint16_t *>(in);
+    int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    int K = 9 * Cin, kb = blockIdx.x * kWgKT, s = blockIdx.y;
     long long M = (long long)N * Ho * Wo;
     long long per = (M + nsplit - 1) / nsplit;
     long long mb = per * s, me = mb + per < M ? mb + per : M;
-    float acc = 0.0f;
-    if (k == Kp) {
-        for (long long m = mb; m < me; m++) acc += dz[m * Cout + co];
-    } else if (k < 9 * Cin) {
-        int tap = k / Cin, c = k - tap * Cin;
-        int ky = tap / 3, kx = tap - ky * 3;
-        for (long long m = mb; m < me; m++) {
-            int ox = (int)(m % Wo), oy = (int)((m / Wo) % Ho), n = (int)(m / ((long long)Wo * Ho));
-            int iy = 2 * oy - 1 + ky, ix = 2 * ox - 1 + kx;
-            if (iy >= 0 && iy < H && ix >= 0 && ix < W)
-                acc += dz[m * Cout + co] * bf(in + (((long long)n * H + iy) * W + ix) * Cin + c);
+    if (tid < kWgKT) {
+        int k = kb + tid;
+        int tap = k / Cin;
+        s_c[tid] = k < K ? k - tap * Cin : -1;
+        s_ky[tid] = tap / 3;
+        s_kx[tid] = tap - (tap / 3) * 3;
+    }
+    float acc[FPW][4];
+#pragma unroll
+    for (int q = 0; q < FPW; q++) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.0f;
+    float bsum = 0.0f;
+    for (long long m0 = mb; m0 < me; m0 += kWgMS) {
+        __syncthreads();  // the previous stage is consumed
+        if (tid < kWgMS) {
+            long long m = m0 + tid;
+            s_n[tid] = -1;
+            if (m < me) {
+                s_ox[tid] = (int)(m % Wo);
+                s_oy[tid] = (int)((m / Wo) % Ho);
+                s_n[tid] = (int)(m / ((long long)Wo * Ho));
+            }
+        }
+        // dz^T: thread tid always stages co = tid % COUT
+        for (int e = tid; e < COUT * (kWgMS / 2); e += kWgThreads) {
+            int co = e % COUT, mp = e / COUT;
+            long long m = m0 + 2 * mp;
+            float v0 = m < me ? dz[m * COUT + co] : 0.0f;
+            float v1 = m + 1 < me ? dz[(m + 1) * COUT + co] : 0.0f;
+            bsum += v0;
+            bsum += v1;
+            sD[co][mp] = pack_bf16(v0, v1);
+        }
+        __syncthreads();  // the pixel decode is visible
+        for (int e = tid; e < kWgKT * (kWgMS / 2); e += kWgThreads) {
+            int kk = e % kWgKT, mp = e / kWgKT;
+            int c = s_c[kk];
+            uint32_t word = 0;
+            if (c >= 0) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    int i = 2 * mp + h, n = s_n[i];
+                    if (n < 0) continue;
+                    int iy = 2 * s_oy[i] - 1 + s_ky[kk], ix = 2 * s_ox[i] - 1 + s_kx[kk];
+                    if (iy >= 0 && iy < H && ix >= 0 && ix < W)
+                        word |= (uint32_t)inb[(((long long)n * H + iy) * W + ix) * Cin + c] << (16 * h);
+                }
+            }
+            sX[kk][mp] = word;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < kWgMS / 16; ks++) {
+#pragma unroll
+            for (int q = 0; q < FPW; q++) {
+                int qq = warp * FPW + q, r = qq / 8, f = qq % 8;
+                uint32_t a[4] = {sD[16 * r + g][ks * 8 + t], sD[16 * r + g + 8][ks * 8 + t],
+                                 sD[16 * r + g][ks * 8 + t + 4], sD[16 * r + g + 8][ks * 8 + t + 4]};
+                mma_bf16(acc[q], a, sX[8 * f + g][ks * 8 + t], sX[8 * f + g][ks * 8 + t + 4]);
+            }
         }
     }
-    partial[((long long)s * Cout + co) * row + k] = acc;
+    int row = Kp + 1;
+#pragma unroll
+    for (int q = 0; q < FPW; q++) {
+        int qq = warp * FPW + q, r = qq / 8, f = qq % 8;
+        int k = kb + 8 * f + 2 * t;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            int co = 16 * r + g + 8 * h;
+            float *dst = partial + ((long long)s * COUT + co) * row;
+            if (k < Kp) dst[k] = acc[q][2 * h];
+            if (k + 1 < Kp) dst[k + 1] = acc[q][2 * h + 1];
+        }
+    }
+    if (blockIdx.x == 0) {
+        s_bias[tid] = bsum;
+        __syncthreads();
+        if (tid < COUT) {
+            float b = 0.0f;
+#pragma unroll
+            for (int j = 0; j < TPC; j++) b += s_bias[tid + j * COUT];
+            partial[((long long)s * COUT + tid) * row + Kp] = b;
+        }
+    }
 }
 
 // sums the splits in order into the flat gradient (weights, then the bias)
@@ -363,37 +469,109 @@ __global__ void k_wgrad_reduce(const float *partial, int nsplit, int Cout, int K
     else gw[co * Kp + k] = s;
 }
 
-// gradient at the previous layer's pre-activation: the transposed convolution
-// of dz, masked by that layer's ReLU output a_prev
-__global__ void k_conv_dgrad(const float *dz, const __nv_bfloat16 *w, const __nv_bfloat16 *a_prev, int N, int H, int W,
-                             int Cin, int Kp, int Cout, int Ho, int Wo, float *dz_prev) {
-    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long tot = (long long)N * H * W * Cin;
-    if (idx >= tot) return;
-    int c = (int)(idx % Cin);
-    long long pix = idx / Cin;
-    int x = (int)(pix % W), y = (int)((pix / W) % H), n = (int)(pix / ((long long)W * H));
-    if (!(bf(a_prev + idx) > 0.0f)) {
-        dz_prev[idx] = 0.0f;
-        return;
-    }
-    float acc = 0.0f;
-    for (int ky = 0; ky < 3; ky++) {
-        int ty = y + 1 - ky;
-        if (ty < 0 || (ty & 1)) continue;
-        int oy = ty >> 1;
-        if (oy >= Ho) continue;
-        for (int kx = 0; kx < 3; kx++) {
-            int tx = x + 1 - kx;
-            if (tx < 0 || (tx & 1)) continue;
-            int ox = tx >> 1;
-            if (ox >= Wo) continue;
-            int k = (ky * 3 + kx) * Cin + c;
-            const float *d = dz + (((long long)n * Ho + oy) * Wo + ox) * Cout;
-            for (int co = 0; co < Cout; co++) acc += bf(w + (long long)co * Kp + k) * d[co];
+// Input gradient of a convolution on the tensor cores (the transposed
+// convolution of dz, masked by the previous layer's ReLU output a_prev):
+// dprev[p][c] = sum over the taps and co of W[co][tap Cin + c] dz[o(p, tap)][co],
+// o(p, tap) the output pixel that pixel p feeds through the tap (stride 2: by
+// the parity of p's coordinates only 1, 2 or 4 of the 9 taps exist).  A GEMM
+// of the input pixels (rows) by Cin (columns) with BF16 operands (dz rounded to
+// nearest even, the weights as [9][Cin][Cout] in wt) and FP32 accumulation,
+// the taps and co in ascending order.  The rows are the input pixels in parity
+// class order ((y & 1, x & 1) outermost, then image, row, column), so the 16
+// rows of a warp almost always share their taps and a tap that none of them
+// has is skipped.  4 warps of 16 rows per CTA.
+template <int CIN>
+__global__ void __launch_bounds__(128) k_conv_dgrad_tc(const float *dz, const __nv_bfloat16 *wt,
+                                                       const __nv_bfloat16 *a_prev, int N, int H, int W, int Cout,
+                                                       int Ho, int Wo, float *dz_prev) {
+    constexpr int NF = CIN / 8;
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    long long rbase = ((long long)blockIdx.x * 4 + warp) * 16;
+    long long pix[2];
+    int yy[2], xx[2], nn[2];
+    bool ok[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        long long r = rbase + g + 8 * h;
+        ok[h] = false;
+        pix[h] = 0;
+        yy[h] = xx[h] = nn[h] = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            int py = q >> 1, px = q & 1;
+            int hq = (H + 1 - py) / 2, wq = (W + 1 - px) / 2;
+            long long cnt = (long long)N * hq * wq;
+            if (!ok[h] && r >= 0 && r < cnt) {
+                int n = (int)(r / ((long long)hq * wq));
+                int rem = (int)(r - (long long)n * hq * wq);
+                nn[h] = n;
+                yy[h] = 2 * (rem / wq) + py;
+                xx[h] = 2 * (rem % wq) + px;
+                pix[h] = ((long long)n * H + yy[h]) * W + xx[h];
+                ok[h] = true;
+            }
+            r -= cnt;
         }
     }
-    dz_prev[idx] = acc;
+    float acc[NF][4];
+#pragma unroll
+    for (int f = 0; f < NF; f++) acc[f][0] = acc[f][1] = acc[f][2] = acc[f][3] = 0.0f;
+    for (int tap = 0; tap < 9; tap++) {
+        int ky = tap / 3, kx = tap - ky * 3;
+        long long o[2];
+        bool v[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            int ty = yy[h] + 1 - ky, tx = xx[h] + 1 - kx;
+            v[h] = ok[h] && ty >= 0 && tx >= 0 && !(ty & 1) && !(tx & 1) && (ty >> 1) < Ho && (tx >> 1) < Wo;
+            o[h] = v[h] ? (((long long)nn[h] * Ho + (ty >> 1)) * Wo + (tx >> 1)) * Cout : 0;
+        }
+        if (!__any_sync(0xffffffffu, v[0] || v[1])) continue;
+        const uint32_t *wtap = reinterpret_cast<const uint32_t *>(wt + (long long)tap * CIN * Cout);
+        for (int co0 = 0; co0 < Cout; co0 += 16) {
+            uint32_t a[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                int h = q & 1, col = co0 + 2 * t + ((q >> 1) ? 8 : 0);
+                float2 d = v[h] ? *reinterpret_cast<const float2 *>(dz + o[h] + col) : make_float2(0.0f, 0.0f);
+                a[q] = pack_bf16(d.x, d.y);
+            }
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+                int wi = ((8 * f + g) * Cout + co0 + 2 * t) >> 1;
+                mma_bf16(acc[f], a, __ldg(wtap + wi), __ldg(wtap + wi + 4));
+            }
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        if (!ok[h]) continue;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            int c = 8 * f + 2 * t;
+            long long idx = pix[h] * CIN + c;
+            float2 out;
+            out.x = bf(a_prev + idx) > 0.0f ? acc[f][2 * h] : 0.0f;
+            out.y = bf(a_prev + idx + 1) > 0.0f ? acc[f][2 * h + 1] : 0.0f;
+            *reinterpret_cast<float2 *>(dz_prev + idx) = out;
+        }
+    }
+}
+
+// The convolution weights of every layer as [9][Cin][Cout] (BF16) for the
+// input-gradient kernel: wt[tap][c][co] = w[co][tap Cin + c].
+struct WtLayout {
+    int64_t src[kLayers], dst[kLayers];
+    int cin[kLayers], cout[kLayers];
+};
+__global__ void k_wt_transpose(const __nv_bfloat16 *pbf, __nv_bfloat16 *wt, WtLayout lay) {
+    int l = blockIdx.y;
+    int Cin = lay.cin[l], Cout = lay.cout[l], Kp = (9 * Cin + 15) / 16 * 16;
+    int tot = 9 * Cin * Cout;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
+        int co = e % Cout, k = e / Cout;  // k = tap * Cin + c
+        wt[lay.dst[l] + e] = pbf[lay.src[l] + (int64_t)co * Kp + k];
+    }
 }
 
 __global__ void k_adam(float *p, const float *g, float *m, float *v, int64_t n, float lr, float bc1, float bc2) {
@@ -461,6 +639,8 @@ struct recon_initnet {
     Offsets off;
     float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
     __nv_bfloat16 *pbf = nullptr;
+    __nv_bfloat16 *wt = nullptr;  // the convolution weights as [9][Cin][Cout] per layer
+    WtLayout wt_lay;
     __nv_bfloat16 *act[kLayers] = {nullptr};
     float *dz[kLayers] = {nullptr};
     float *feat = nullptr, *y = nullptr, *partial = nullptr, *loss = nullptr;
@@ -484,9 +664,11 @@ int net_fail(int code, const std::string &msg) {
 
 int64_t act_count(int l, int n) { return (int64_t)n * kHt[l + 1] * kWd[l + 1] * kCout[l]; }
 
+// pixel splits of layer l's weight gradient for a batch of n (about 256
+// output pixels each)
 int nsplit_for(int l, int n) {
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
-    long long s = M / 512;
+    long long s = (M + 255) / 256;
     return (int)(s < 1 ? 1 : (s > kMaxSplit ? kMaxSplit : s));
 }
 
@@ -571,14 +753,27 @@ int backward(recon_initnet *net, const __nv_bfloat16 *in, const float *target, i
         const __nv_bfloat16 *lin = l ? net->act[l - 1] : in;
         int ns = nsplit_for(l, n);
         int row = Kp + 1;
-        dim3 g1((Cout * row + 127) / 128, ns);
-        k_conv_wgrad<<<g1, 128, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Cout, Ho, Wo, ns, net->partial);
+        dim3 g1((Kp + kWgKT - 1) / kWgKT, ns);
+        switch (Cout) {
+            case 16: k_conv_wgrad_tc<16><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
+            case 32: k_conv_wgrad_tc<32><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
+            case 64: k_conv_wgrad_tc<64><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
+            default: k_conv_wgrad_tc<128><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
+        }
         k_wgrad_reduce<<<(Cout * row + 127) / 128, 128, 0, net->stream>>>(net->partial, ns, Cout, Kp,
                                                                            grad + net->off.w[l], grad + net->off.b[l]);
         if (l > 0) {
-            long long tot = (long long)n * H * W * Cin;
-            k_conv_dgrad<<<(unsigned)((tot + 255) / 256), 256, 0, net->stream>>>(
-                net->dz[l], net->pbf + net->off.w[l], net->act[l - 1], n, H, W, Cin, Kp, Cout, Ho, Wo, net->dz[l - 1]);
+            long long rows = (long long)n * H * W;
+            unsigned blocks = (unsigned)((rows + 63) / 64);
+            const __nv_bfloat16 *wt = net->wt + net->wt_lay.dst[l];
+            const __nv_bfloat16 *ap = net->act[l - 1];
+            float *dp = net->dz[l - 1];
+            switch (Cin) {
+                case 16: k_conv_dgrad_tc<16><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
+                case 32: k_conv_dgrad_tc<32><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
+                case 64: k_conv_dgrad_tc<64><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
+                default: k_conv_dgrad_tc<128><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
+            }
         }
     }
     NCK(cudaMemsetAsync(grad + net->off.scale, 0, kOut * sizeof(float), net->stream));
@@ -595,6 +790,7 @@ int check_batch(recon_initnet *net, int n) {
 void refresh_bf16(recon_initnet *net) {
     int64_t tot = net->off.total;
     k_to_bf16<<<(unsigned)((tot + 255) / 256), 256, 0, net->stream>>>(net->params, net->pbf, tot);
+    k_wt_transpose<<<dim3(64, kLayers), 256, 0, net->stream>>>(net->pbf, net->wt, net->wt_lay);
 }
 
 }  // namespace
@@ -634,6 +830,14 @@ int recon_initnet_create(int32_t max_batch, void *stream, recon_initnet **out) {
     net->off = offsets();
     net->stream = (cudaStream_t)stream;  // NULL: the legacy default stream
     int64_t P = net->off.total;
+    int64_t nwt = 0;
+    for (int l = 0; l < kLayers; l++) {
+        net->wt_lay.src[l] = net->off.w[l];
+        net->wt_lay.dst[l] = nwt;
+        net->wt_lay.cin[l] = kCin[l];
+        net->wt_lay.cout[l] = kCout[l];
+        nwt += 9LL * kCin[l] * kCout[l];
+    }
     int64_t part = 0;
     for (int l = 0; l < kLayers; l++) {
         int64_t s = (int64_t)nsplit_for(l, max_batch) * kCout[l] * (kpad(kCin[l]) + 1);
@@ -648,7 +852,7 @@ int recon_initnet_create(int32_t max_batch, void *stream, recon_initnet **out) {
         }
     bool ok = cudaMalloc(&net->params, P * 4) == cudaSuccess && cudaMalloc(&net->grad, P * 4) == cudaSuccess &&
               cudaMalloc(&net->m, P * 4) == cudaSuccess && cudaMalloc(&net->v, P * 4) == cudaSuccess &&
-              cudaMalloc(&net->pbf, P * 2) == cudaSuccess &&
+              cudaMalloc(&net->pbf, P * 2) == cudaSuccess && cudaMalloc(&net->wt, nwt * 2) == cudaSuccess &&
               cudaMalloc(&net->feat, (int64_t)max_batch * kFeat * 4) == cudaSuccess &&
               cudaMalloc(&net->y, (int64_t)max_batch * kOut * 4) == cudaSuccess &&
               cudaMalloc(&net->partial, part * 4) == cudaSuccess && cudaMalloc(&net->fpart, fpart * 4) == cudaSuccess &&
@@ -682,6 +886,7 @@ int recon_initnet_destroy(recon_initnet *net) {
     cudaFree(net->m);
     cudaFree(net->v);
     cudaFree(net->pbf);
+    cudaFree(net->wt);
     cudaFree(net->feat);
     cudaFree(net->y);
     cudaFree(net->partial);
