@@ -32,7 +32,6 @@ constexpr int kHt[kLayers + 1] = {60, 30, 15, 8, 4, 2, 1};
 constexpr int kWd[kLayers + 1] = {80, 40, 20, 10, 5, 3, 2};
 constexpr int kFeat = 128;
 constexpr int kOut = RECON_NET_OUT;
-constexpr int kMaxSplit = 256;
 
 constexpr int kpad(int cin) { return (9 * cin + 15) / 16 * 16; }
 
@@ -284,29 +283,46 @@ __global__ void k_head_fwd(const __nv_bfloat16 *a6, int P, const float *wfc, con
     }
 }
 
-// loss, and the gradients of the linear layer (one CTA of kOut*kFeat threads)
+// loss, and the gradients of the linear layer (one CTA of kOut*kFeat
+// threads): the output gradients of kHeadChunk samples at a time are staged
+// in shared memory, thread (j, c) adds its products over the samples in order,
+// and the loss is every thread's squared errors (its entries in order) added
+// by a fixed tree.
+constexpr int kHeadChunk = 128;
 __global__ void k_head_grad(const float *y, const float *t, const float *feat, int N, float *gwfc, float *gbfc,
                             float *loss) {
+    static_assert(kOut * kFeat == 768, "the loss tree folds 3 x 256 partial sums");
+    __shared__ float sdy[kHeadChunk * kOut];
+    __shared__ float red[kOut * kFeat];
     int i = threadIdx.x;  // j * kFeat + c
     int j = i / kFeat, c = i % kFeat;
     float inv = 2.0f / (float)(kOut * N);
-    float s = 0.0f, sb = 0.0f;
-    for (int n = 0; n < N; n++) {
-        float dy = (y[n * kOut + j] - t[n * kOut + j]) * inv;
-        s += dy * feat[(long long)n * kFeat + c];
-        sb += dy;
+    float s = 0.0f, sb = 0.0f, l = 0.0f;
+    for (int n0 = 0; n0 < N; n0 += kHeadChunk) {
+        int cnt = N - n0 < kHeadChunk ? N - n0 : kHeadChunk;
+        __syncthreads();  // the previous chunk is consumed
+        for (int e = i; e < cnt * kOut; e += blockDim.x) {
+            float d = y[(long long)n0 * kOut + e] - t[(long long)n0 * kOut + e];
+            l += d * d;
+            sdy[e] = d * inv;
+        }
+        __syncthreads();
+        for (int n = 0; n < cnt; n++) {
+            float dy = sdy[n * kOut + j];
+            s += dy * feat[(long long)(n0 + n) * kFeat + c];
+            sb += dy;
+        }
     }
     gwfc[i] = s;
     if (c == 0) gbfc[j] = sb;
-    if (i == 0) {
-        float l = 0.0f;
-        for (int n = 0; n < N; n++)
-            for (int k = 0; k < kOut; k++) {
-                float d = y[n * kOut + k] - t[n * kOut + k];
-                l += d * d;
-            }
-        *loss = l / (float)(kOut * N);
+    red[i] = l;
+    __syncthreads();
+    if (i < 256) red[i] = (red[i] + red[i + 256]) + red[i + 512];
+    for (int w = 128; w > 0; w >>= 1) {
+        __syncthreads();
+        if (i < w) red[i] += red[i + w];
     }
+    if (i == 0) *loss = red[0] / (float)(kOut * N);
 }
 
 // gradient at the last convolution's pre-activation: d feat / P through the
@@ -348,14 +364,15 @@ __device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, uint32_t b
 // at a time in shared memory transposed (two consecutive pixels per 32-bit
 // word, rows padded so that fragment loads hit distinct banks).  Warp w owns
 // fragment tiles [w FPW, (w + 1) FPW) of the (co / 16) x (column / 8) grid.
-// Writes partial[s][co][k] for k < Kp and, from CTA column 0, the bias
+// Split s covers pixels [s per, (s + 1) per).  Writes partial[e][s] for the
+// entries e = co (Kp + 1) + k, k < Kp, and, from CTA column 0, the bias
 // gradient at k = Kp: the split's FP32 sum of dz (each thread adds its pixel
 // pairs in order, the threads of a co are then added in thread order).
 constexpr int kWgKT = 64, kWgMS = 64, kWgThreads = 128;
 template <int COUT>
 __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad_tc(const float *dz, const __nv_bfloat16 *in, int N,
                                                               int H, int W, int Cin, int Kp, int Ho, int Wo,
-                                                              int nsplit, float *partial) {
+                                                              int nsplit, int per, float *partial) {
     constexpr int RT = COUT / 16, FPW = RT * 2;  // 8 column fragments per row tile, over 4 warps
     constexpr int LD = kWgMS / 2 + 4;            // words per staged row
     constexpr int TPC = kWgThreads / COUT;       // threads per co in the staging of dz
@@ -369,8 +386,7 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad_tc(const float *dz, c
     int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
     int K = 9 * Cin, kb = blockIdx.x * kWgKT, s = blockIdx.y;
     long long M = (long long)N * Ho * Wo;
-    long long per = (M + nsplit - 1) / nsplit;
-    long long mb = per * s, me = mb + per < M ? mb + per : M;
+    long long mb = (long long)per * s, me = mb + per < M ? mb + per : M;
     if (tid < kWgKT) {
         int k = kb + tid;
         int tap = k / Cin;
@@ -440,9 +456,9 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad_tc(const float *dz, c
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             int co = 16 * r + g + 8 * h;
-            float *dst = partial + ((long long)s * COUT + co) * row;
-            if (k < Kp) dst[k] = acc[q][2 * h];
-            if (k + 1 < Kp) dst[k + 1] = acc[q][2 * h + 1];
+            long long e = (long long)co * row + k;
+            if (k < Kp) partial[e * nsplit + s] = acc[q][2 * h];
+            if (k + 1 < Kp) partial[(e + 1) * nsplit + s] = acc[q][2 * h + 1];
         }
     }
     if (blockIdx.x == 0) {
@@ -452,21 +468,36 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad_tc(const float *dz, c
             float b = 0.0f;
 #pragma unroll
             for (int j = 0; j < TPC; j++) b += s_bias[tid + j * COUT];
-            partial[((long long)s * COUT + tid) * row + Kp] = b;
+            partial[((long long)tid * row + Kp) * nsplit + s] = b;
         }
     }
 }
 
-// sums the splits in order into the flat gradient (weights, then the bias)
+// Sums the splits of every entry of partial[e][s] (e = co (Kp + 1) + k) in a
+// fixed order into the flat gradient (weights, then the bias): with few
+// splits a thread per entry adds them in order; with many a warp per entry,
+// lane q adding splits q, q + 32, ... in order and the lanes then added by a
+// fixed butterfly.
 __global__ void k_wgrad_reduce(const float *partial, int nsplit, int Cout, int Kp, float *gw, float *gb) {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
     int row = Kp + 1;
-    if (idx >= Cout * row) return;
-    float s = 0.0f;
-    for (int q = 0; q < nsplit; q++) s += partial[(long long)q * Cout * row + idx];
-    int co = idx / row, k = idx % row;
-    if (k == Kp) gb[co] = s;
-    else gw[co * Kp + k] = s;
+    long long ne = (long long)Cout * row;
+    long long e;
+    float v = 0.0f;
+    if (nsplit <= 8) {
+        e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        if (e >= ne) return;
+        for (int q = 0; q < nsplit; q++) v += partial[e * nsplit + q];
+    } else {
+        e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        int lane = threadIdx.x & 31;
+        if (e >= ne) return;  // uniform over the warp
+        for (int q = lane; q < nsplit; q += 32) v += partial[e * nsplit + q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane) return;
+    }
+    int co = (int)(e / row), k = (int)(e % row);
+    if (k == Kp) gb[co] = v;
+    else gw[(long long)co * Kp + k] = v;
 }
 
 // Input gradient of a convolution on the tensor cores (the transposed
@@ -479,14 +510,20 @@ __global__ void k_wgrad_reduce(const float *partial, int nsplit, int Cout, int K
 // the taps and co in ascending order.  The rows are the input pixels in parity
 // class order ((y & 1, x & 1) outermost, then image, row, column), so the 16
 // rows of a warp almost always share their taps and a tap that none of them
-// has is skipped.  4 warps of 16 rows per CTA.
-template <int CIN>
+// has is skipped.  A CTA has 4 warps: 4 / KS row tiles of 16 rows, each
+// reduced by KS warps (warp group kg takes the co steps kg, kg + KS, ... of
+// every tap), whose tiles are then added in group order (the deep layers
+// have few rows and long reductions).
+template <int CIN, int KS>
 __global__ void __launch_bounds__(128) k_conv_dgrad_tc(const float *dz, const __nv_bfloat16 *wt,
                                                        const __nv_bfloat16 *a_prev, int N, int H, int W, int Cout,
                                                        int Ho, int Wo, float *dz_prev) {
     constexpr int NF = CIN / 8;
+    static_assert(KS == 1 || KS == 2 || KS == 4, "4 warps per CTA");
+    __shared__ float red[KS > 1 ? 4 : 1][KS > 1 ? 16 : 1][KS > 1 ? CIN : 1];
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    long long rbase = ((long long)blockIdx.x * 4 + warp) * 16;
+    int kg = warp % KS, tile = warp / KS;
+    long long rbase = ((long long)blockIdx.x * (4 / KS) + tile) * 16;
     long long pix[2];
     int yy[2], xx[2], nn[2];
     bool ok[2];
@@ -528,7 +565,7 @@ __global__ void __launch_bounds__(128) k_conv_dgrad_tc(const float *dz, const __
         }
         if (!__any_sync(0xffffffffu, v[0] || v[1])) continue;
         const uint32_t *wtap = reinterpret_cast<const uint32_t *>(wt + (long long)tap * CIN * Cout);
-        for (int co0 = 0; co0 < Cout; co0 += 16) {
+        for (int co0 = 16 * kg; co0 < Cout; co0 += 16 * KS) {
             uint32_t a[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -542,6 +579,26 @@ __global__ void __launch_bounds__(128) k_conv_dgrad_tc(const float *dz, const __
                 mma_bf16(acc[f], a, __ldg(wtap + wi), __ldg(wtap + wi + 4));
             }
         }
+    }
+    if (KS > 1) {
+        // groups 1.. leave their tiles in shared memory, group 0 adds them in order
+#pragma unroll
+        for (int k = 1; k < KS; k++) {
+            if (kg == k) {
+#pragma unroll
+                for (int f = 0; f < NF; f++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) red[warp][g + 8 * (q >> 1)][8 * f + 2 * t + (q & 1)] = acc[f][q];
+            }
+        }
+        __syncthreads();
+        if (kg != 0) return;
+#pragma unroll
+        for (int k = 1; k < KS; k++)
+#pragma unroll
+            for (int f = 0; f < NF; f++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[f][q] += red[warp + k][g + 8 * (q >> 1)][8 * f + 2 * t + (q & 1)];
     }
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -664,18 +721,26 @@ int net_fail(int code, const std::string &msg) {
 
 int64_t act_count(int l, int n) { return (int64_t)n * kHt[l + 1] * kWd[l + 1] * kCout[l]; }
 
-// pixel splits of layer l's weight gradient for a batch of n (about 256
-// output pixels each)
+// Output pixels per split of layer l's weight gradient for a batch of n: a
+// multiple of the 64-pixel stage, so that the layer's CTAs (splits x 64-column
+// tiles) number about 1024.
+int wg_per_split(int l, int n) {
+    long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
+    long long kt = (kpad(kCin[l]) + kWgKT - 1) / kWgKT;
+    long long per = (M * kt + 1023) / 1024;
+    per = (per + kWgMS - 1) / kWgMS * kWgMS;
+    return (int)(per < kWgMS ? kWgMS : per);
+}
 int nsplit_for(int l, int n) {
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
-    long long s = (M + 255) / 256;
-    return (int)(s < 1 ? 1 : (s > kMaxSplit ? kMaxSplit : s));
+    int per = wg_per_split(l, n);
+    return (int)((M + per - 1) / per);
 }
 
 // K splits of layer l's forward convolution for a batch of n: enough CTAs for
 // about two per SM when the layer has few output pixels (the deep layers), at
 // least one 16-wide K step per warp and split.
-bool pixel_parallel(int l);
+bool pixel_parallel(int l, int n);
 int fsplit_for(int l, int n) {
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
     long long ctas = (M + 15) / 16;
@@ -688,17 +753,20 @@ int fsplit_for(int l, int n) {
 }
 
 // Layers whose 16 warps would mostly idle in k_conv_fwd (fewer K steps than the
-// warps it spreads over K) run as k_conv_fwd_px.
-bool pixel_parallel(int l) {
+// warps it spreads over K), and layers of a batch with at least 4096 tiles of
+// 16 output pixels (a training batch: enough warps to fill the GPU many times
+// over without splitting K), run as k_conv_fwd_px.
+bool pixel_parallel(int l, int n) {
     int NF = kCout[l] / 8, NG = NF < 8 ? NF : 8, KS = kConvWarps / NG;
-    return kpad(kCin[l]) / 16 < KS;
+    long long tiles = ((long long)n * kHt[l + 1] * kWd[l + 1] + 15) / 16;
+    return kpad(kCin[l]) / 16 < KS || tiles >= 4096;
 }
 
 template <int COUT>
 void conv_launch(recon_initnet *net, int l, const __nv_bfloat16 *in, int n) {
     int Cin = kCin[l], Kp = kpad(Cin);
     long long M = (long long)n * kHt[l + 1] * kWd[l + 1];
-    if (pixel_parallel(l)) {
+    if (pixel_parallel(l, n)) {
         long long tiles = (M + 15) / 16;
         k_conv_fwd_px<COUT><<<(unsigned)((tiles + kConvPxWarps - 1) / kConvPxWarps), kConvPxWarps * 32, 0,
                                net->stream>>>(in, n, kHt[l], kWd[l], Cin, Kp, net->pbf + net->off.w[l],
@@ -751,29 +819,40 @@ int backward(recon_initnet *net, const __nv_bfloat16 *in, const float *target, i
         int Cin = kCin[l], Cout = kCout[l], Kp = kpad(Cin);
         int H = kHt[l], W = kWd[l], Ho = kHt[l + 1], Wo = kWd[l + 1];
         const __nv_bfloat16 *lin = l ? net->act[l - 1] : in;
-        int ns = nsplit_for(l, n);
+        int ns = nsplit_for(l, n), per = wg_per_split(l, n);
         int row = Kp + 1;
         dim3 g1((Kp + kWgKT - 1) / kWgKT, ns);
         switch (Cout) {
-            case 16: k_conv_wgrad_tc<16><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
-            case 32: k_conv_wgrad_tc<32><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
-            case 64: k_conv_wgrad_tc<64><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
-            default: k_conv_wgrad_tc<128><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, net->partial); break;
+            case 16: k_conv_wgrad_tc<16><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, per, net->partial); break;
+            case 32: k_conv_wgrad_tc<32><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, per, net->partial); break;
+            case 64: k_conv_wgrad_tc<64><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, per, net->partial); break;
+            default: k_conv_wgrad_tc<128><<<g1, kWgThreads, 0, net->stream>>>(net->dz[l], lin, n, H, W, Cin, Kp, Ho, Wo, ns, per, net->partial); break;
         }
-        k_wgrad_reduce<<<(Cout * row + 127) / 128, 128, 0, net->stream>>>(net->partial, ns, Cout, Kp,
-                                                                           grad + net->off.w[l], grad + net->off.b[l]);
+        long long red_threads = (long long)Cout * row * (ns <= 8 ? 1 : 32);
+        k_wgrad_reduce<<<(unsigned)((red_threads + 127) / 128), 128, 0, net->stream>>>(
+            net->partial, ns, Cout, Kp, grad + net->off.w[l], grad + net->off.b[l]);
         if (l > 0) {
-            long long rows = (long long)n * H * W;
-            unsigned blocks = (unsigned)((rows + 63) / 64);
+            // rows of 16 per tile; the reduction split over 2 or 4 warps when the
+            // layer has fewer than 8 or 4 tiles per SM (and co steps to share)
+            long long rows = (long long)n * H * W, tiles = (rows + 15) / 16;
+            int ks = 1;
+            if (tiles < 8 * 152) ks = 2;
+            if (tiles < 4 * 152) ks = 4;
+            while (ks > 1 && Cout / 16 < ks) ks >>= 1;
+            unsigned blocks = (unsigned)((tiles + 4 / ks - 1) / (4 / ks));
             const __nv_bfloat16 *wt = net->wt + net->wt_lay.dst[l];
             const __nv_bfloat16 *ap = net->act[l - 1];
             float *dp = net->dz[l - 1];
+#define RECON_DGRAD(CI, K) k_conv_dgrad_tc<CI, K><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp)
+#define RECON_DGRAD_KS(CI) (ks == 4 ? RECON_DGRAD(CI, 4) : ks == 2 ? RECON_DGRAD(CI, 2) : RECON_DGRAD(CI, 1))
             switch (Cin) {
-                case 16: k_conv_dgrad_tc<16><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
-                case 32: k_conv_dgrad_tc<32><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
-                case 64: k_conv_dgrad_tc<64><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
-                default: k_conv_dgrad_tc<128><<<blocks, 128, 0, net->stream>>>(net->dz[l], wt, ap, n, H, W, Cout, Ho, Wo, dp); break;
+                case 16: RECON_DGRAD_KS(16); break;
+                case 32: RECON_DGRAD_KS(32); break;
+                case 64: RECON_DGRAD_KS(64); break;
+                default: RECON_DGRAD_KS(128); break;
             }
+#undef RECON_DGRAD_KS
+#undef RECON_DGRAD
         }
     }
     NCK(cudaMemsetAsync(grad + net->off.scale, 0, kOut * sizeof(float), net->stream));
@@ -813,7 +892,7 @@ const float *scale_dev(recon_initnet *net) { return net->params + net->off.scale
 // split-K finishing kernels and the pooling + linear layer
 int forward_kernels(int n) {
     int k = kLayers + 1;
-    for (int l = 0; l < kLayers; l++) k += (!pixel_parallel(l) && fsplit_for(l, n) > 1) ? 1 : 0;
+    for (int l = 0; l < kLayers; l++) k += (!pixel_parallel(l, n) && fsplit_for(l, n) > 1) ? 1 : 0;
     return k;
 }
 }  // namespace nn
@@ -840,8 +919,10 @@ int recon_initnet_create(int32_t max_batch, void *stream, recon_initnet **out) {
     }
     int64_t part = 0;
     for (int l = 0; l < kLayers; l++) {
-        int64_t s = (int64_t)nsplit_for(l, max_batch) * kCout[l] * (kpad(kCin[l]) + 1);
-        if (s > part) part = s;
+        for (int nb = 1; nb <= max_batch; nb++) {
+            int64_t s = (int64_t)nsplit_for(l, nb) * kCout[l] * (kpad(kCin[l]) + 1);
+            if (s > part) part = s;
+        }
     }
     net->partial_floats = part;
     int64_t fpart = 1;

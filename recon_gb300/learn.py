@@ -8,7 +8,9 @@ label is that pose's twist in the tracker's SE(3) convention.  The network is
 trained on the GPU by the library's own forward / backward / Adam kernels.
 
 Run as a module to train and save parameters:
-    python -m recon_gb300.learn --pairs 200000 --epochs 8 --out <file.npz>
+    python -m recon_gb300.learn --pairs 200000 --epochs 10 --out <file.npz>
+or to time the training step alone (random inputs, CUDA events):
+    python -m recon_gb300.learn --time-steps 20 [--batch 256]
 """
 from __future__ import annotations
 
@@ -191,15 +193,54 @@ def twist_errors(pred: np.ndarray, label: np.ndarray):
     return out[:, 0], out[:, 1]
 
 
+def time_steps(steps: int, batch: int = 256, warmup: int = 3) -> dict:
+    """Milliseconds per training step (forward, backward, Adam) and per
+    forward pass of a batch, on random inputs, timed with CUDA events on the
+    network's stream after `warmup` steps."""
+    import torch
+
+    from . import initnet as IN
+
+    rng = np.random.default_rng(0)
+    net = IN.InitNet(max_batch=batch)
+    net.set_params(IN.init_params(1))
+    x = torch.from_numpy(rng.uniform(0, 1, size=(batch, 60, 80, 4)).astype(np.float32))
+    x = x.to(torch.bfloat16).cuda().contiguous()
+    t = torch.from_numpy(rng.normal(size=(batch, 6)).astype(np.float32)).cuda()
+    loss = torch.zeros(1, device="cuda")
+    for _ in range(warmup):
+        net.train_step(x, t, 1e-4, loss)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    return {"batch": batch, "train_step_ms": timed(lambda: net.train_step(x, t, 1e-4, loss)),
+            "forward_ms": timed(lambda: net.forward(x))}
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--time-steps", type=int, default=0, help="only time this many training steps")
+    ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--pairs", type=int, default=200000)
     ap.add_argument("--val", type=int, default=2048)
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--seed", type=int, default=20000)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--out", required=True)
+    ap.add_argument("--out", default=None)
     a = ap.parse_args()
+    if a.time_steps > 0:
+        print(time_steps(a.time_steps, a.batch))
+        return
+    if not a.out:
+        ap.error("--out is required to train")
     t0 = time.time()
     x, tw, _ = make_pairs(a.pairs, a.seed)
     xv, twv, _ = make_pairs(a.val, a.seed + 500000)

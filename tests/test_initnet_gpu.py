@@ -99,6 +99,31 @@ def test_gradient_matches_oracle_per_block():
     assert np.all(g[sc:] == 0)
 
 
+def test_large_batch_matches_oracle():
+    """A batch of 64: the layer-1 forward runs pixel-parallel (at least 4096
+    tiles of 16 output pixels), the input gradients of layers 1-2 reduce in
+    one warp per row tile or split over two, and the layer-0 weight gradient
+    adds 600 pixel splits by warps -- paths a batch of 4 does not take."""
+    _need_gpu()
+    n = 64
+    params, inp, inp_np, target = _problem(11, n)
+    net = IN.InitNet(max_batch=n)
+    net.set_params(params)
+    y = net.forward(inp).cpu().numpy().astype(np.float64)
+    want = np.zeros((n, 6))
+    O.lib().orc_net_forward(p(params), p(inp_np), n, 0, p(want))
+    assert np.linalg.norm(y - want) <= FWD_RTOL * np.linalg.norm(want)
+    g, loss = net.gradient(inp, torch.from_numpy(target).cuda())
+    g = g.cpu().numpy().astype(np.float64)
+    wg = np.zeros(params.size)
+    lw = O.lib().orc_net_loss_grad(p(params), p(inp_np), p(target), n, 0, p(wg))
+    assert abs(float(loss.item()) - lw) <= 1e-3 * lw
+    for name, a, b in _blocks():
+        err = np.linalg.norm(g[a:b] - wg[a:b])
+        ref = np.linalg.norm(wg[a:b])
+        assert err <= GRAD_RTOL * ref + 1e-9, (name, err, ref)
+
+
 def test_gradient_is_deterministic():
     _need_gpu()
     params, inp, _, target = _problem(9, 16)
