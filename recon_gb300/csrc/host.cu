@@ -292,6 +292,36 @@ int ensure_stage(recon_batch *b, size_t bytes) {
 }
 
 // uploads host images to staging (if needed) and fills the device pointer table
+// Host-to-device copies of one image per instance, dst[i] <- src[i] (bytes[i];
+// a null src copies nothing): one 2-D copy when every instance has an image,
+// all of one size, and the sources and the destinations are each evenly
+// spaced (frames picked from one host stack at a fixed step into one device
+// arena), else one copy per image.
+cudaError_t copy_images(const void *const *src, void *const *dst, const size_t *bytes, int n, cudaStream_t s) {
+    bool one = n >= 2;
+    size_t sp = 0, dp = 0;
+    if (one) {
+        const char *s0 = (const char *)src[0], *s1 = (const char *)src[1];
+        const char *d0 = (const char *)dst[0], *d1 = (const char *)dst[1];
+        one = s0 && s1 && s1 > s0 && d1 > d0;
+        if (one) {
+            sp = (size_t)(s1 - s0);
+            dp = (size_t)(d1 - d0);
+            one = sp >= bytes[0] && dp >= bytes[0];
+        }
+        for (int i = 0; one && i < n; i++)
+            one = src[i] && bytes[i] == bytes[0] && (const char *)src[i] == s0 + i * sp &&
+                  (const char *)dst[i] == d0 + i * dp;
+    }
+    if (one) return cudaMemcpy2DAsync(dst[0], dp, src[0], sp, bytes[0], n, cudaMemcpyHostToDevice, s);
+    for (int i = 0; i < n; i++) {
+        if (!src[i]) continue;
+        cudaError_t e = cudaMemcpyAsync(dst[i], src[i], bytes[i], cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *const *depth, const float *const *rgbd,
                  int on_device, const float *const *opts = nullptr, const float *const *onrm = nullptr) {
     int n = b->n;
@@ -308,46 +338,41 @@ int stage_inputs(recon_batch *b, const uint8_t *const *gray, const uint16_t *con
         int rc = ensure_stage(b, need ? need : 256);
         if (rc) return rc;
     }
+    // the staging arena holds, per instance, its images one after the other;
+    // the copies go out per image kind (5 kinds: gray, depth, RGB-D, points,
+    // normals) so that evenly spaced images take one 2-D copy each
+    std::vector<const void *> src(5 * (size_t)n, nullptr);
+    std::vector<void *> dst(5 * (size_t)n, nullptr);
+    std::vector<size_t> bytes(5 * (size_t)n, 0);
     size_t off = 0;
+    auto place = [&](int kind, int i, const void *p, size_t nb) -> const void * {
+        if (on_device) return p;
+        size_t k = (size_t)kind * n + i;
+        src[k] = p;
+        dst[k] = b->d_stage + off;
+        bytes[k] = nb;
+        off += align256(nb);
+        return dst[k];
+    };
     for (int i = 0; i < n; i++) {
         size_t px = (size_t)b->cfg[i].width * b->cfg[i].height;
         if (rgbd && rgbd[i]) {
-            const void *p = rgbd[i];
-            if (!on_device) {
-                CK(cudaMemcpyAsync(b->d_stage + off, rgbd[i], px * 16, cudaMemcpyHostToDevice, b->stream));
-                p = b->d_stage + off;
-                off += align256(px * 16);
-            }
-            b->h_inptr[2 * (size_t)n + i] = p;
+            b->h_inptr[2 * (size_t)n + i] = place(2, i, rgbd[i], px * 16);
             active[i] = 1;
         } else if (gray && depth && gray[i] && depth[i]) {
-            const void *pg = gray[i], *pd = depth[i];
-            if (!on_device) {
-                CK(cudaMemcpyAsync(b->d_stage + off, gray[i], px, cudaMemcpyHostToDevice, b->stream));
-                pg = b->d_stage + off;
-                off += align256(px);
-                CK(cudaMemcpyAsync(b->d_stage + off, depth[i], px * 2, cudaMemcpyHostToDevice, b->stream));
-                pd = b->d_stage + off;
-                off += align256(px * 2);
-            }
-            b->h_inptr[i] = pg;
-            b->h_inptr[(size_t)n + i] = pd;
+            b->h_inptr[i] = place(0, i, gray[i], px);
+            b->h_inptr[(size_t)n + i] = place(1, i, depth[i], px * 2);
             active[i] = 1;
         }
         if (active[i] && opts && onrm && opts[i] && onrm[i]) {
-            const void *pp = opts[i], *pn = onrm[i];
-            if (!on_device) {
-                CK(cudaMemcpyAsync(b->d_stage + off, opts[i], px * 16, cudaMemcpyHostToDevice, b->stream));
-                pp = b->d_stage + off;
-                off += align256(px * 16);
-                CK(cudaMemcpyAsync(b->d_stage + off, onrm[i], px * 16, cudaMemcpyHostToDevice, b->stream));
-                pn = b->d_stage + off;
-                off += align256(px * 16);
-            }
-            b->h_inptr[3 * (size_t)n + i] = pp;
-            b->h_inptr[4 * (size_t)n + i] = pn;
+            b->h_inptr[3 * (size_t)n + i] = place(3, i, opts[i], px * 16);
+            b->h_inptr[4 * (size_t)n + i] = place(4, i, onrm[i], px * 16);
         }
     }
+    if (!on_device)
+        for (int kind = 0; kind < 5; kind++)
+            CK(copy_images(src.data() + (size_t)kind * n, dst.data() + (size_t)kind * n,
+                           bytes.data() + (size_t)kind * n, n, b->stream));
     CK(cudaMemcpyAsync(b->d_inptr, b->h_inptr.data(), 5 * (size_t)n * sizeof(void *), cudaMemcpyHostToDevice,
                        b->stream));
     CK(cudaMemcpyAsync(b->d_active, active.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
@@ -1346,43 +1371,17 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     // frame f's copies are issued after frame f - 1's, so the event recorded
     // later on the same stream also covers the earlier frames)
     // one 2-D copy per image kind when the instances' host images of a frame
-    // and their slots are evenly spaced with one size (frames picked from one
-    // stack at a fixed step), else one copy per image
-    auto strided = [&](const void *const *src, int f, int kind, size_t bytes, size_t *spitch, size_t *dpitch) {
-        if (n < 2) return false;
-        const char *s0 = (const char *)src[(size_t)f * n], *d0 = (const char *)b->h_seqptr[(size_t)f * 3 * n + kind * n];
-        const char *s1 = (const char *)src[(size_t)f * n + 1], *d1 = (const char *)b->h_seqptr[(size_t)f * 3 * n + kind * n + 1];
-        if (s1 <= s0 || d1 <= d0) return false;
-        size_t sp = (size_t)(s1 - s0), dp = (size_t)(d1 - d0);
-        if (sp < bytes || dp < bytes) return false;
-        for (int i = 0; i < n; i++) {
-            if (px[i] != px[0]) return false;
-            if ((const char *)src[(size_t)f * n + i] != s0 + i * sp) return false;
-            if ((const char *)b->h_seqptr[(size_t)f * 3 * n + kind * n + i] != d0 + i * dp) return false;
-        }
-        *spitch = sp;
-        *dpitch = dp;
-        return true;
-    };
+    // and their slots are evenly spaced with one size (copy_images)
+    std::vector<size_t> gbytes(n), dbytes(n);
+    for (int i = 0; i < n; i++) {
+        gbytes[i] = px[i];
+        dbytes[i] = 2 * px[i];
+    }
     auto stage = [&](int f) -> int {
         if (on_device) return RECON_OK;
-        size_t sp, dp;
-        if (strided((const void *const *)gray, f, 0, px[0], &sp, &dp)) {
-            CK(cudaMemcpy2DAsync((void *)b->h_seqptr[(size_t)f * 3 * n], dp, gray[(size_t)f * n], sp, px[0], n,
-                                 cudaMemcpyHostToDevice, b->copy_stream));
-        } else {
-            for (int i = 0; i < n; i++)
-                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + i], gray[(size_t)f * n + i], px[i],
-                                   cudaMemcpyHostToDevice, b->copy_stream));
-        }
-        if (strided((const void *const *)depth, f, 1, 2 * px[0], &sp, &dp)) {
-            CK(cudaMemcpy2DAsync((void *)b->h_seqptr[(size_t)f * 3 * n + n], dp, depth[(size_t)f * n], sp, 2 * px[0], n,
-                                 cudaMemcpyHostToDevice, b->copy_stream));
-        } else {
-            for (int i = 0; i < n; i++)
-                CK(cudaMemcpyAsync((void *)b->h_seqptr[(size_t)f * 3 * n + n + i], depth[(size_t)f * n + i],
-                                   2 * px[i], cudaMemcpyHostToDevice, b->copy_stream));
-        }
+        void *const *slots = (void *const *)(b->h_seqptr + (size_t)f * 3 * n);
+        CK(copy_images((const void *const *)(gray + (size_t)f * n), slots, gbytes.data(), n, b->copy_stream));
+        CK(copy_images((const void *const *)(depth + (size_t)f * n), slots + n, dbytes.data(), n, b->copy_stream));
         CK(cudaEventRecord(b->ev_copied[f & 1], b->copy_stream));
         return RECON_OK;
     };
