@@ -161,11 +161,18 @@ struct recon_batch {
     size_t Tseq_cap = 0;
     int seq_frames = 0;  // frames of the last recon_batch_track_sequence call (their poses are in d_Tseq)
     // host-input sequences: one device slot per frame of the call (kept after
-    // the call, so that recon_batch_fuse_sequence can read the frames)
+    // the call, so that recon_batch_fuse_sequence can read the frames), in two
+    // sets used by alternate calls: a call's copies need not wait for a
+    // fusion that still reads the previous call's frames
     uint8_t *d_slots = nullptr;
-    size_t slots_bytes = 0;
+    size_t set_bytes = 0;  // bytes of one set
+    int next_set = 0;
+    int seq_set = -1;  // the set of the last sequence (-1: device frames)
     cudaStream_t copy_stream = nullptr;
-    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr};
+    // the last reads of each set: the tracking of the call that used it (batch
+    // stream) and a fusion of its frames (reconstruction stream)
+    cudaEvent_t ev_set_read[2] = {nullptr, nullptr}, ev_set_fused[2] = {nullptr, nullptr};
     // keyframe fusion runs on a second stream (the reference's reconstruction GPU)
     cudaStream_t recon_stream = nullptr;
     cudaEvent_t ev_pose = nullptr, ev_fused = nullptr;
@@ -954,7 +961,8 @@ int recon_batch_destroy(recon_batch *b) {
     if (b->d_slots) cudaFree(b->d_slots);
     for (int k = 0; k < 2; k++) {
         if (b->ev_copied[k]) cudaEventDestroy(b->ev_copied[k]);
-        if (b->ev_free[k]) cudaEventDestroy(b->ev_free[k]);
+        if (b->ev_set_read[k]) cudaEventDestroy(b->ev_set_read[k]);
+        if (b->ev_set_fused[k]) cudaEventDestroy(b->ev_set_fused[k]);
     }
     if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
     for (int k = 0; k < 2; k++) {
@@ -1308,7 +1316,7 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     // a keyframe fusion may still read the last sequence's poses and slots:
     // let it finish before any buffer is reallocated
     if (b->recon_stream && (need_ptr > b->seqptr_cap || need_T > b->Tseq_cap ||
-                            (!on_device && frame_bytes * nf > b->slots_bytes)))
+                            (!on_device && frame_bytes * nf > b->set_bytes)))
         CK(cudaStreamSynchronize(b->recon_stream));
     if (need_ptr > b->seqptr_cap) {
         if (b->d_seqptr) cudaFree(b->d_seqptr);
@@ -1328,26 +1336,34 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
         b->Tseq_cap = need_T;
     }
     b->seq_frames = 0;
+    b->seq_set = -1;
+    int set = 0;
     if (!on_device) {
-        if (frame_bytes * nf > b->slots_bytes) {
+        if (frame_bytes * nf > b->set_bytes) {
+            // the previous calls' tracking has been waited for (their poses
+            // were read back) and the fusion above
             if (b->d_slots) cudaFree(b->d_slots);
             b->d_slots = nullptr;
-            b->slots_bytes = 0;
-            CK(cudaMalloc(&b->d_slots, frame_bytes * nf));
-            b->slots_bytes = frame_bytes * nf;
+            b->set_bytes = 0;
+            CK(cudaMalloc(&b->d_slots, 2 * frame_bytes * nf));
+            b->set_bytes = frame_bytes * nf;
         }
         if (!b->copy_stream) CK(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
         for (int k = 0; k < 2; k++) {
             if (!b->ev_copied[k]) CK(cudaEventCreateWithFlags(&b->ev_copied[k], cudaEventDisableTiming));
-            if (!b->ev_free[k]) CK(cudaEventCreateWithFlags(&b->ev_free[k], cudaEventDisableTiming));
+            if (!b->ev_set_read[k]) CK(cudaEventCreateWithFlags(&b->ev_set_read[k], cudaEventDisableTiming));
+            if (!b->ev_set_fused[k]) CK(cudaEventCreateWithFlags(&b->ev_set_fused[k], cudaEventDisableTiming));
         }
-        // work already queued on the batch stream (a keyframe fusion reading the
-        // previous call's slots) ends before the copies into the slots begin
-        CK(cudaEventRecord(b->ev_free[0], b->stream));
-        CK(cudaStreamWaitEvent(b->copy_stream, b->ev_free[0], 0));
+        // this call's set was last read by the call before the previous one and
+        // by a fusion of its frames: the copies into it wait for both (an event
+        // never recorded is no wait)
+        set = b->next_set;
+        b->next_set ^= 1;
+        CK(cudaStreamWaitEvent(b->copy_stream, b->ev_set_read[set], 0));
+        CK(cudaStreamWaitEvent(b->copy_stream, b->ev_set_fused[set], 0));
         // frame f is copied into slot f, the only source of row f of the pointer table
         for (int f = 0; f < nf; f++) {
-            size_t off = frame_bytes * f;
+            size_t off = b->set_bytes * set + frame_bytes * f;
             for (int i = 0; i < n; i++) {
                 b->h_seqptr[(size_t)f * 3 * n + i] = b->d_slots + off;
                 off += align256(px[i]);
@@ -1435,6 +1451,10 @@ int recon_batch_track_sequence(recon_batch *b, int32_t nf, const uint8_t *const 
     // the last frame's pose (the earlier ones were stored by the next frame's pyramid launch)
     k_store_pose<<<dim3(1, n), 32, 0, b->stream>>>(b->d_desc, b->d_Tseq + (size_t)(nf - 1) * n * 16);
     g_launches += 1;
+    if (!on_device) {
+        CK(cudaEventRecord(b->ev_set_read[set], b->stream));
+        b->seq_set = set;
+    }
     b->have_cur = true;
     b->seq_frames = nf;
     if (T_out) CK(cudaMemcpyAsync(T_out, b->d_Tseq, need_T * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
@@ -1541,7 +1561,11 @@ int recon_batch_fuse_sequence(recon_batch *b, int32_t nframes, float gate_mm) {
     CK(cudaStreamWaitEvent(b->recon_stream, b->ev_pose, 0));
     CK(cudaMemcpyAsync(b->d_fuse_ptr, b->h_fuse_ptr, 2 * cnt * sizeof(void *), cudaMemcpyHostToDevice,
                        b->recon_stream));
-    return fuse_launch(b, nframes, true, b->d_Tseq, gate_mm);
+    rc = fuse_launch(b, nframes, true, b->d_Tseq, gate_mm);
+    if (rc) return rc;
+    // the frames of a host-input sequence live in its slot set until this fusion is done
+    if (b->seq_set >= 0) CK(cudaEventRecord(b->ev_set_fused[b->seq_set], b->recon_stream));
+    return RECON_OK;
 }
 
 int recon_batch_fuse_keyframe_rgbd(recon_batch *b, int32_t nframes, const uint8_t *const *gray,
