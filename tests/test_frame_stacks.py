@@ -99,3 +99,42 @@ def test_frame_stacks_track_like_lists(learned):
     b2.set_current([g[i] for i in seq[0]], [d[i] for i in seq[0]])
     T2, _ = b2.track()
     assert_bitexact(T1, T2, "set_current_frames vs set_current")
+
+
+@pytest.mark.gpu
+def test_host_stack_steps_with_fusion_match_device_stack():
+    """Two steps of: keyframes, five tracked frames, their fusion into the
+    keyframes, two more tracked frames -- from a pinned host stack (the
+    library copies host frames into slot sets that alternate by call, so a
+    call's copies overlap the fusion of the previous call's frames) and from
+    the same frames on the device: poses and fused keyframes bit-identical."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from test_gpu_parity import _trajectory_frames, assert_bitexact
+    W, H, L = 320, 240, 3
+    cal, poses, g, d = _trajectory_frames(W, H, 9, seed=97)
+    gd = torch.from_numpy(np.stack(g)).cuda()
+    dd = torch.from_numpy(np.stack([x.view(np.int16) for x in d])).cuda()
+    gh = torch.from_numpy(np.stack(g)).pin_memory().numpy()
+    dh = torch.from_numpy(np.stack(d).view(np.int16)).pin_memory().numpy().view(np.uint16)
+    ref = np.array([0, 1])
+    seq1 = np.array([[f, f + 1] for f in range(1, 6)])
+    seq2 = np.array([[6, 7], [7, 8]])
+    out = {}
+    for gs, ds, what in ((gd, dd, "device"), (gh, dh, "host")):
+        cfg = rg.make_config(W, H, L, mode=rg.BIOBJECTIVE, iters=(2, 3, 4))
+        b = rg.Batch([cfg, cfg], [cal.calib, cal.calib])
+        res = []
+        for _ in range(2):
+            b.set_reference_frames(gs, ds, ref)
+            T1, _ = b.track_sequence_frames(gs, ds, seq1)
+            b.fuse_sequence(5, gate_mm=30.0)
+            T2, _ = b.track_sequence_frames(gs, ds, seq2)
+            res.append((T1, T2, b.get_array(1, "ref_z", 0, np.float32, W * H),
+                        b.get_array(1, "ref_col", 0, np.float32, W * H)))
+        out[what] = res
+    for k in range(2):
+        for a, c, name in zip(out["host"][k], out["device"][k], ("poses before", "poses after", "depth", "colour")):
+            assert_bitexact(a, c, f"step {k}: {name} of the fusion, host vs device stack")
+    assert_bitexact(out["host"][1][1], out["host"][0][1], "the second step repeats the first")
