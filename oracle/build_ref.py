@@ -39,13 +39,16 @@ FRAGMENTS = {
     "tracker/kernels/d2z.cu": [
         "xyz2CloudKernel", "genPointsCloud6Kernel", "computeNormalsCudaKernel", "downSampleCloud6Kernel",
         "extractGradientKernel", "addVertexAttributesWithoutNormalsKernel3", "addVertexAttributesWithoutNormalsKernel4",
-        "genOrientedPoints6Kernel",
+        "genOrientedPoints6Kernel", "undistortDisparityKernel", "d2ZLowKernel", "d2ZLowHdrKernel",
     ],
     "tracker/kernels/rgb2gray.cu": [
         "icpResidualKernel2", "icpResidualIndexKernel2", "packIndexKernel", "initWeightsKernel",
         "updateWeightsKernel", "clampWeightsKernel", "convertZMapToXYZKernel", "convertZMapToXYZ6Kernel",
-        "rgbTex2GrayHdrZKernel", "rgbdTex2DepthKernel",
+        "rgbTex2GrayHdrZKernel", "rgbdTex2DepthKernel", "rgb2GrayHdrKernel", "rgbF2GrayHdrKernel",
+        "convertHdrRGBKernel",
     ],
+    # the GPU capture path's RGB undistortion
+    "tracker/kernels/undistort.cu": ["undistortHdrRGBKernel"],
     "tracker/kernels/downSample2Cuda.cu": ["fastDownSampleHdrKernel"],
     # one-block kernels with shared memory and __syncthreads (run as 512 host threads)
     "tracker/kernels/filterIndex256.cu": ["seekThreshold256Kernel2", "filterIndexKernel4"],

@@ -213,6 +213,15 @@ void orc_kinect_d2z(const uint16_t *disp, int W, int H, float c0, float c1, floa
 void orc_kinect_d2z_low(const uint16_t *disp, int Wl, int Hl, float c0, float c1, float min_dist, float max_dist,
                         float x_off, float y_off, float *z);
 void orc_kinect_rgb2gray(const uint8_t *rgb, int W, int H, uint8_t *gray);
+/* the GPU capture path (tracker/kernels/d2z.cu, rgb2gray.cu, undistort.cu) */
+void orc_kinect_disparity_to_float(const uint16_t *disp, int n, float *out);
+void orc_kinect_depth_normalized(const uint16_t *disp_u16, const float *disp_f32, int W, int H, float c0, float c1,
+                                 float min_dist, float max_dist, float x_off, float y_off, float *z_low);
+void orc_kinect_rgb_to_hdr(const uint8_t *rgb, int n, float *rgb_hdr);
+void orc_kinect_rgb_to_gray_hdr(const uint8_t *rgb, int n, float *gray);
+void orc_kinect_rgb_hdr_to_gray(const float *rgb_hdr, int n, float *gray);
+void orc_kinect_undistort_rgb_hdr(const uint8_t *rgb, int W, int H, const float *K, const float *iK, const float *kc,
+                                  float *rgb_hdr);
 void orc_kinect_undistort(const uint8_t *src, int W, int H, const float *K, const float *iK, const float *kc,
                           uint8_t *dst);
 

@@ -73,6 +73,7 @@ namespace refk {
 #include "frag_rgb2gray.inc"
 #include "frag_downSample2Cuda.inc"
 #include "frag_filterIndex256.inc"
+#include "frag_undistort.inc"
 }  // namespace refk
 
 #include "frag_phototracker.inc"
@@ -217,6 +218,38 @@ void ref_genPointsCloud6(float *z, int W, int H, float *calib, float *pts, int *
 
 void ref_genOrientedPoints6(float *xyz4, float *nrm4, int W, int H, float *calib, float *pts, int *mask) {
     launch2d(W, H, [&] { refk::genOrientedPoints6Kernel((float4 *)xyz4, (float4 *)nrm4, W, H, calib, pts, mask); });
+}
+
+// the GPU capture path (d2z.cu, rgb2gray.cu, undistort.cu).  Compiled for the
+// host, a negative float converted to unsigned wraps instead of saturating as
+// on the GPU, so the disparity kernels differ from the GPU where 2x + x_off or
+// 2y + y_off is negative.
+void ref_undistortDisparity(unsigned short *d, float *u, int W, int H, float *calib) {
+    launch2d(W, H, [&] { refk::undistortDisparityKernel(d, u, W, H, calib); });
+}
+
+void ref_d2ZLowGpu(unsigned short *d, float *z, int W, int H, float *calib, float xoff, float yoff) {
+    launch2d(W / 2, H / 2, [&] { refk::d2ZLowKernel(d, z, W, H, calib, xoff, yoff); });
+}
+
+void ref_d2ZLowHdrGpu(float *d, float *z, int W, int H, float *calib, float xoff, float yoff) {
+    launch2d(W / 2, H / 2, [&] { refk::d2ZLowHdrKernel(d, z, W, H, calib, xoff, yoff); });
+}
+
+void ref_convertHdrRGB(unsigned char *src, float *dst, int W, int H) {
+    launch2d(W, H, [&] { refk::convertHdrRGBKernel(src, dst, (unsigned)W, (unsigned)H); });
+}
+
+void ref_rgb2GrayHdr(unsigned char *rgb, float *gray, int W, int H) {
+    launch2d(W, H, [&] { refk::rgb2GrayHdrKernel(rgb, gray, W); });
+}
+
+void ref_rgbF2GrayHdr(float *rgb, float *gray, int W, int H) {
+    launch2d(W, H, [&] { refk::rgbF2GrayHdrKernel(rgb, gray, W); });
+}
+
+void ref_undistortHdrRGB(unsigned char *src, float *dst, int W, int H, float *calib) {
+    launch2d(W, H, [&] { refk::undistortHdrRGBKernel(src, dst, (unsigned)W, (unsigned)H, calib); });
 }
 
 void ref_computeNormals(float *pts, int *mask, int W, int H) {

@@ -157,6 +157,11 @@ def lib() -> ctypes.CDLL:
             L.recon_kinect_disparity_to_depth.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, i32, vp, vp]
             L.recon_kinect_rgb_to_gray.argtypes = [vp, i32, i32, vp, vp]
             L.recon_kinect_undistort_gray.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp]
+            L.recon_kinect_disparity_to_float.argtypes = [vp, i32, i32, vp, vp]
+            L.recon_kinect_depth_normalized.argtypes = [vp, vp, i32, i32, f32, f32, f32, f32, f32, f32, vp, vp]
+            L.recon_kinect_rgb_to_hdr.argtypes = [vp, i32, i32, vp, vp]
+            L.recon_kinect_rgb_to_gray_hdr.argtypes = [vp, vp, i32, i32, vp, vp]
+            L.recon_kinect_undistort_rgb_hdr.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp]
             L.recon_trajectory_save.argtypes = [ctypes.c_char_p, vp, i32, i32, i32]
             L.recon_trajectory_load.argtypes = [ctypes.c_char_p, vp, i32, i32]
             L.recon_trajectory_load.restype = i32
@@ -949,4 +954,67 @@ def kinect_undistort_gray(src, K, iK, kc, out=None):
     iKf = np.ascontiguousarray(np.asarray(iK, np.float32).reshape(9))
     kcf = np.ascontiguousarray(np.asarray(kc, np.float32).reshape(-1)[:5])
     check(lib().recon_kinect_undistort_gray(_ptr(src), W, H, _ptr(Kf), _ptr(iKf), _ptr(kcf), _ptr(out), _stream_now()))
+    return out
+
+
+# the reference's GPU capture path (d2z.cu, rgb2gray.cu, undistort.cu)
+
+def kinect_disparity_to_float(disp, out=None):
+    """undistortDisparityCuda: uint16 disparity [H, W] -> float, 65535 where >= 2047."""
+    import torch
+    H, W = disp.shape
+    if out is None:
+        out = torch.empty((H, W), dtype=torch.float32, device=disp.device)
+    check(lib().recon_kinect_disparity_to_float(_ptr(disp), W, H, _ptr(out), _stream_now()))
+    return out
+
+
+def kinect_depth_normalized(disp, c0: float, c1: float, min_dist: float, max_dist: float, x_off: float = 0.0,
+                            y_off: float = 0.0, out=None):
+    """d2ZCuda (16-bit disparity) / d2ZCudaHdr (float disparity): [H, W] ->
+    the [H/2, W/2] depth normalised by (z - min_dist) / (max_dist - min_dist)."""
+    import torch
+    H, W = disp.shape
+    if out is None:
+        out = torch.empty((H // 2, W // 2), dtype=torch.float32, device=disp.device)
+    is_f = disp.dtype == torch.float32
+    check(lib().recon_kinect_depth_normalized(None if is_f else _ptr(disp), _ptr(disp) if is_f else None, W, H, c0, c1,
+                                              min_dist, max_dist, x_off, y_off, _ptr(out), _stream_now()))
+    return out
+
+
+def kinect_rgb_to_hdr(rgb, out=None):
+    """convertToHDRCuda: uint8 [H, W, 3] -> float [H, W, 3], every byte / 255."""
+    import torch
+    H, W = rgb.shape[:2]
+    if out is None:
+        out = torch.empty((H, W, 3), dtype=torch.float32, device=rgb.device)
+    check(lib().recon_kinect_rgb_to_hdr(_ptr(rgb), W, H, _ptr(out), _stream_now()))
+    return out
+
+
+def kinect_rgb_to_gray_hdr(rgb, out=None):
+    """rgb2GrayCuda: uint8 [H, W, 3] (integer weights) or float [H, W, 3]
+    (0.3 r + 0.59 g + 0.11 b) -> float gray [H, W]."""
+    import torch
+    H, W = rgb.shape[:2]
+    if out is None:
+        out = torch.empty((H, W), dtype=torch.float32, device=rgb.device)
+    is_f = rgb.dtype == torch.float32
+    check(lib().recon_kinect_rgb_to_gray_hdr(None if is_f else _ptr(rgb), _ptr(rgb) if is_f else None, W, H, _ptr(out),
+                                             _stream_now()))
+    return out
+
+
+def kinect_undistort_rgb_hdr(rgb, K, iK, kc, out=None):
+    """undistortRGBCuda: uint8 [H, W, 3] -> undistorted float RGB [H, W, 3]."""
+    import torch
+    H, W = rgb.shape[:2]
+    if out is None:
+        out = torch.empty((H, W, 3), dtype=torch.float32, device=rgb.device)
+    Kf = np.ascontiguousarray(np.asarray(K, np.float32).reshape(9))
+    iKf = np.ascontiguousarray(np.asarray(iK, np.float32).reshape(9))
+    kcf = np.ascontiguousarray(np.asarray(kc, np.float32).reshape(-1)[:5])
+    check(lib().recon_kinect_undistort_rgb_hdr(_ptr(rgb), W, H, _ptr(Kf), _ptr(iKf), _ptr(kcf), _ptr(out),
+                                               _stream_now()))
     return out

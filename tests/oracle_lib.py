@@ -150,6 +150,12 @@ def lib() -> ctypes.CDLL:
             L.orc_kinect_d2z_low.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, vp]
             L.orc_kinect_rgb2gray.argtypes = [vp, i32, i32, vp]
             L.orc_kinect_undistort.argtypes = [vp, i32, i32, vp, vp, vp, vp]
+            L.orc_kinect_disparity_to_float.argtypes = [vp, i32, vp]
+            L.orc_kinect_depth_normalized.argtypes = [vp, vp, i32, i32, f32, f32, f32, f32, f32, f32, vp]
+            L.orc_kinect_rgb_to_hdr.argtypes = [vp, i32, vp]
+            L.orc_kinect_rgb_to_gray_hdr.argtypes = [vp, i32, vp]
+            L.orc_kinect_rgb_hdr_to_gray.argtypes = [vp, i32, vp]
+            L.orc_kinect_undistort_rgb_hdr.argtypes = [vp, i32, i32, vp, vp, vp, vp]
             L.orc_gen_oriented_points6.argtypes = [vp, vp, i32, i32, vp, vp]
             L.orc_set_reference_oriented.argtypes = [vp, vp, vp, vp, vp]
             L.orc_tsdf_invert_rt4.argtypes = [vp, vp]

@@ -54,6 +54,13 @@ def lib() -> ctypes.CDLL:
         L.ref_d2ZLow.argtypes = [vp, i32, i32, f32, f32, f32, f32, f32, f32, vp]
         L.ref_convert2Gray.argtypes = [vp, i32, i32, vp]
         L.ref_undistort.argtypes = [vp, i32, i32, vp, vp, vp, i32, vp]
+        L.ref_undistortDisparity.argtypes = [vp, vp, i32, i32, vp]
+        L.ref_d2ZLowGpu.argtypes = [vp, vp, i32, i32, vp, f32, f32]
+        L.ref_d2ZLowHdrGpu.argtypes = [vp, vp, i32, i32, vp, f32, f32]
+        L.ref_convertHdrRGB.argtypes = [vp, vp, i32, i32]
+        L.ref_rgb2GrayHdr.argtypes = [vp, vp, i32, i32]
+        L.ref_rgbF2GrayHdr.argtypes = [vp, vp, i32, i32]
+        L.ref_undistortHdrRGB.argtypes = [vp, vp, i32, i32, vp]
         L.ref_result_save.argtypes = [ctypes.c_char_p, vp, i32, i32, i32, i32]
         L.ref_track_params_get.argtypes = [ctypes.c_char_p, i32, vp, vp, vp]
         L.ref_tsdf_reset.argtypes = [vp, i32]
