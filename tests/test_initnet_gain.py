@@ -9,11 +9,11 @@ the first five frames, bi-objective 640x480 -- with the learned start pose
 the start, the reference tracker's rule, on the same shortened schedule.
 Both are scored against the FP64 oracle run of the same trajectories on the
 full schedule.  Measured on a GB300 (200 frames): on the benchmark's schedule
-1/2/2/1 the network keeps 95.5% of the frames within 1 mm / 0.05 deg against
-91.5% and lowers the 99th-percentile error (3.0 against 3.4 mm) at an equal
-median (0.24 against 0.23 mm); on the shorter 0/1/2/1 it keeps 92.5% against
-84% and lowers the median (0.27 against 0.30 mm) and the 99th percentile
-(4.3 against 9.2 mm).  The test asserts those directions.
+1/2/2/1 the network keeps 96.5% of the frames within 1 mm / 0.05 deg against
+91.5% and lowers the 99th-percentile error (3.0 against 3.4 mm) at a similar
+median (0.24 against 0.23 mm); on the shorter 0/1/2/1 it keeps 95.5% against
+84% and lowers the median (0.23 against 0.30 mm) and the 99th percentile
+(3.6 against 9.2 mm).  The test asserts those directions.
 """
 import os
 import sys
