@@ -235,7 +235,7 @@ int64_t recon_launch_count(void);         /* kernels launched by the library so 
 
 /* Copies an internal device array of instance `inst` to host memory (tests).
  * Names: ref_gray, cur_gray, ref_z, ref_col, cur_z, ref_pts, ref_nrm, cur_pts, sel_idx,
- * sel_xyz, sel_I, sel_J, vtx, grad_hist, icp_nsel, and icp_mask (uint8) /
+ * sel_xyz, sel_I, sel_J, gmag, grad_hist, icp_nsel, and icp_mask (uint8) /
  * icp_w (float) per pixel of the last level the ICP term prepared (`level`
  * gives its size; icp_w is 0 where the pixel is not a correspondence).
  * Returns bytes. */

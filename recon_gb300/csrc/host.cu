@@ -262,7 +262,7 @@ size_t layout(InstDesc &d, char *base) {
     d.ref_z = a.take<float>(n);
     d.ref_col = a.take<float>(n);
     d.cur_z = a.take<float>(n);
-    d.vtx = a.take<float>((size_t)kVtxPlanes * n);
+    d.gmag = a.take<float>(n);
     d.grad_hist = a.take<int>(1024);
     d.seg = a.take<int>(3076);
     d.sel_idx = a.take<int>(P);
@@ -466,8 +466,8 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
     else
         k_ref_from_z<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
     k_normals<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
-    // the photometric vertex records take the level-0 points of the depth
-    // (both reference paths); only then may oriented points replace them for ICP
+    // the photometric vertex records take the points of the keyframe depth
+    // (ref_z), not the level-0 ICP points that oriented points may replace
     k_clear_ref<<<dim3(1, n), 256, 0, s>>>(D, active);
     k_xyz2cloud<<<grid_pix(b->max_pix, n), 256, 0, s>>>(D, active);
     if (oriented) {
@@ -1246,7 +1246,7 @@ int64_t recon_batch_get_array(recon_batch *b, int32_t inst, const char *name, in
     else if (nm == "sel_xyz") { src = d.sel_xyz; sz = (int64_t)P * 12; }
     else if (nm == "sel_I") { src = d.sel_I[level]; sz = (int64_t)P * 4; }
     else if (nm == "sel_J") { src = d.sel_J[level]; sz = (int64_t)P * 24; }
-    else if (nm == "vtx") { src = d.vtx; sz = (int64_t)n0 * 4 * kVtxPlanes; }
+    else if (nm == "gmag") { src = d.gmag; sz = (int64_t)n0 * 4; }
     else if (nm == "grad_hist") { src = d.grad_hist; sz = (int64_t)d.select_bins * 4; }
     else if (nm == "T") { src = d.T; sz = 64; }
     else if (nm == "icp_nsel") { src = d.icp_nsel; sz = 16; }

@@ -454,9 +454,64 @@ __global__ void k_normals(const InstDesc *D, const int *active) {
 // photometric reference: vertex records, gradient histogram, selection
 // ------------------------------------------------------------------
 
-// xyz2CloudKernel, d2z.cu:235-331, plus the 256-bin gradient-magnitude
-// histogram (gpu_hist.cu:136, cuda_hist.cu:100-152) with privatised
-// shared-memory integer atomics.
+// The vertex record of keyframe pixel i (xyz2CloudKernel, d2z.cu:235-331):
+// v = x y z px py gx gy gmag gray, zero with z = -maxDist where the point is
+// invalid or projects within 10 pixels of the border.  The keyframe kernels
+// evaluate it twice with the same operations: for every pixel to find the
+// gradient magnitude that selects the points, and again for the selected
+// points only (so that the other eight planes are never stored).  The point
+// is the back-projection of the keyframe depth ref_z, formed as
+// k_convert_level0 and k_ref_from_z form the level-0 ICP points (zero out of
+// range: xyz alone carries the validity), so a filtered reference's oriented
+// points, which later replace those, do not enter it.
+__device__ __forceinline__ void vertex_record(const InstDesc &d, int i, int W, int H, float *v) {
+    for (int k = 0; k < kVtxPlanes; k++) v[k] = 0.0f;
+    v[2] = -d.calib[RC_MAXD];
+    float p3x = 0.0f, p3y = 0.0f, p3z = 0.0f;
+    {
+        float z = d.ref_z[i];
+        float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
+        if (z < -minDist && z > -maxDist) {
+            float fx = d.calib[RC_KL], fy = d.calib[RC_KL + 4];
+            float cx = d.calib[RC_KL + 2], cy = d.calib[RC_KL + 5];
+            p3x = ((float)(i % W) - cx) * z / fx;
+            p3y = ((float)(i / W) - cy) * z / fy;
+            p3z = z;
+        }
+    }
+    if (p3z < 0) {
+        const float *T = d.calib + RC_TLR;
+        float rx, ry, rz;
+        mul4(T, p3x, p3y, p3z, rx, ry, rz);
+        float pux = rx / rz, puy = ry / rz;
+        float px, py;
+        distort(pux, puy, d.calib + RC_KCR, d.calib + RC_KR, px, py);
+        if (in_bounds10(px, py, W, H)) {
+            const float *img = d.ref_gray[0];
+            int xdi = ftoi(px), ydi = ftoi(py);
+            float fx = px - xdi, fy = py - ydi;
+            float color1 = bilin(xdi, ydi, fx, fy, W, img);
+            float fused = d.ref_col[i];  // the keyframe fusion's vertex colour, if any
+            if (fused >= 0.0f) color1 = fused;
+            float colorN = bilin(ftoi(px), ftoi(py - 1.0f), fx, fy, W, img);
+            float colorE = bilin(ftoi(px + 1.0f), ftoi(py), fx, fy, W, img);
+            float colorW = bilin(ftoi(px - 1.0f), ftoi(py), fx, fy, W, img);
+            float colorS = bilin(ftoi(px), ftoi(py + 1.0f), fx, fy, W, img);
+            float gradX1 = (colorE - colorW) / 2.0f;
+            float gradY1 = (colorS - colorN) / 2.0f;
+            float gm = fabsf(gradY1) + fabsf(gradX1);
+            v[0] = p3x; v[1] = p3y; v[2] = p3z;
+            v[3] = px; v[4] = py;
+            v[5] = gradX1; v[6] = gradY1;
+            v[7] = gm < 1.0f ? gm : 1.0f;
+            v[8] = color1;
+        }
+    }
+}
+
+// The gradient magnitude of every keyframe pixel (xyz2CloudKernel's gmag
+// plane) and its 256-bin histogram (gpu_hist.cu:136, cuda_hist.cu:100-152)
+// with privatised shared-memory integer atomics.
 __global__ void k_xyz2cloud(const InstDesc *D, const int *active) {
     INST_DESC;
     if (!active[blockIdx.y]) return;
@@ -467,43 +522,9 @@ __global__ void k_xyz2cloud(const InstDesc *D, const int *active) {
     int W = d.W, H = d.H, n = W * H;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        float4 pt = d.ref_pts[0][i];
-        float *vp = d.vtx;
         float v[kVtxPlanes];
-        for (int k = 0; k < kVtxPlanes; k++) v[k] = 0.0f;
-        v[2] = -d.calib[RC_MAXD];
-        // convertZMapToXYZKernel zeroes out-of-range pixels, so xyz alone carries
-        // the validity (ref_pts.w is later narrowed by the normal test)
-        float p3x = pt.x, p3y = pt.y, p3z = pt.z;
-        if (p3z < 0) {
-            const float *T = d.calib + RC_TLR;
-            float rx, ry, rz;
-            mul4(T, p3x, p3y, p3z, rx, ry, rz);
-            float pux = rx / rz, puy = ry / rz;
-            float px, py;
-            distort(pux, puy, d.calib + RC_KCR, d.calib + RC_KR, px, py);
-            if (in_bounds10(px, py, W, H)) {
-                const float *img = d.ref_gray[0];
-                int xdi = ftoi(px), ydi = ftoi(py);
-                float fx = px - xdi, fy = py - ydi;
-                float color1 = bilin(xdi, ydi, fx, fy, W, img);
-                float fused = d.ref_col[i];  // the keyframe fusion's vertex colour, if any
-                if (fused >= 0.0f) color1 = fused;
-                float colorN = bilin(ftoi(px), ftoi(py - 1.0f), fx, fy, W, img);
-                float colorE = bilin(ftoi(px + 1.0f), ftoi(py), fx, fy, W, img);
-                float colorW = bilin(ftoi(px - 1.0f), ftoi(py), fx, fy, W, img);
-                float colorS = bilin(ftoi(px), ftoi(py + 1.0f), fx, fy, W, img);
-                float gradX1 = (colorE - colorW) / 2.0f;
-                float gradY1 = (colorS - colorN) / 2.0f;
-                float gm = fabsf(gradY1) + fabsf(gradX1);
-                v[0] = p3x; v[1] = p3y; v[2] = p3z;
-                v[3] = px; v[4] = py;
-                v[5] = gradX1; v[6] = gradY1;
-                v[7] = gm < 1.0f ? gm : 1.0f;
-                v[8] = color1;
-            }
-        }
-        for (int k = 0; k < kVtxPlanes; k++) vp[(size_t)k * n + i] = v[k];
+        vertex_record(d, i, W, H, v);
+        d.gmag[i] = v[7];
         unsigned int bin = (unsigned int)(v[7] * (nb - 1) + 0.5f);
         if (bin < (unsigned)nb) atomicAdd(&sh[bin], 1);
     }
@@ -542,7 +563,7 @@ __global__ void k_seg_count(const InstDesc *D, const int *active) {
     int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     int lane = threadIdx.x & 31;
     if (warp >= kSegments) return;
-    const float *grad = d.vtx + (size_t)7 * n;
+    const float *grad = d.gmag;
     unsigned int thr = s_thr;
     int cnt = 0, mcnt = 0;
     for (int base = warp * ppt; base < warp * ppt + ppt; base += 32) {
@@ -597,7 +618,7 @@ __global__ void k_seg_scatter(const InstDesc *D, const int *active) {
     int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     int lane = threadIdx.x & 31;
     if (warp >= kSegments) return;
-    const float *grad = d.vtx + (size_t)7 * n;
+    const float *grad = d.gmag;
     unsigned int thr = (unsigned int)d.seg[3072];
     int pos_a = d.seg[1024 + warp];
     int pos_m = d.seg[1536 + warp];
@@ -636,12 +657,13 @@ __global__ void k_attr_jac(const InstDesc *D, const int *active) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= P) return;
     int pix = d.sel_idx[k];
-    const float *v = d.vtx;
-    float p3x = v[pix], p3y = v[(size_t)n + pix], p3z = v[(size_t)2 * n + pix];
+    float v[kVtxPlanes];
+    vertex_record(d, pix, W, H, v);
+    float p3x = v[0], p3y = v[1], p3z = v[2];
     float gx[kMaxLevels] = {0, 0, 0, 0}, gy[kMaxLevels] = {0, 0, 0, 0}, col[kMaxLevels] = {0, 0, 0, 0};
-    gx[0] = v[(size_t)5 * n + pix];
-    gy[0] = v[(size_t)6 * n + pix];
-    col[0] = v[(size_t)8 * n + pix];
+    gx[0] = v[5];
+    gy[0] = v[6];
+    col[0] = v[8];
     const float *T = d.calib + RC_TLR;
     const float *kc = d.calib + RC_KCR;
     const float *KR = d.calib + RC_KR;

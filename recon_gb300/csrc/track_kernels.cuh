@@ -14,7 +14,7 @@ constexpr int kMaxLevels = 4;
 constexpr int kChunk = 1024;     // canonical reduction chunk (points)
 constexpr int kLanes = 256;      // lanes per chunk, 4 points each
 constexpr int kSegments = 512;   // pixel-selection segments (filterIndex256.cu:183)
-constexpr int kVtxPlanes = 9;    // x y z px py gx gy gmag gray
+constexpr int kVtxPlanes = 9;    // a vertex record: x y z px py gx gy gmag gray
 constexpr int kIterCluster = 8;  // CTAs of the photometric cluster of the GN iteration kernel
 constexpr int kIterBlock = 256;  // threads of a GN iteration CTA
 constexpr int kIterCtaSlots = 4 * 152;  // GN iteration CTAs resident on a 152-SM GB300
@@ -38,7 +38,7 @@ struct InstDesc {
     float *ref_col;               // W*H fused vertex colour (keyframe fusion), -1 where none
     float4 *ref_pts[kMaxLevels];  // x y z mask
     float4 *ref_nrm[kMaxLevels];  // nx ny nz 0
-    float *vtx;                   // kVtxPlanes planes of W*H
+    float *gmag;                  // W*H: the keyframe pixels' gradient magnitudes
     int *grad_hist;               // select_bins
     int *seg;                     // segment tables, 6 * kSegments + 4
     int *sel_idx;                 // P
