@@ -478,7 +478,7 @@ int prepare_reference(recon_batch *b, bool from_inputs = true, bool reset_pose =
     for (int l = 1; l < b->max_L; l++)
         k_downsample<<<grid_pix(b->max_pix >> (2 * l), n), 256, 0, s>>>(D, l, active);
     k_seg_count<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, active);
-    k_seg_scan<<<dim3(1, n), 32, 0, s>>>(D, active);
+    k_seg_scan<<<dim3(1, n), kSegments, 0, s>>>(D, active);
     k_seg_scatter<<<dim3(kSegments / 8, n), 256, 0, s>>>(D, active);
     k_attr_jac<<<grid_pix(b->max_P, n), 256, 0, s>>>(D, active);
     if (reset_pose) k_reset_pose<<<dim3(1, n), 32, 0, s>>>(D, active);

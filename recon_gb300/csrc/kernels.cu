@@ -543,11 +543,16 @@ __global__ void k_seg_count(const InstDesc *D, const int *active) {
     int nb = d.select_bins, P = d.P;
     __shared__ unsigned int s_thr;
     __shared__ int s_excess;
+    __shared__ int s_hist[1024];
+    // the histogram in shared memory in one parallel load; the threshold
+    // search (from the top bin down) then reads shared memory only
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) s_hist[k] = __ldcg(d.grad_hist + k);
+    __syncthreads();
     if (threadIdx.x == 0) {
         unsigned int thr = 0;
         int sel = 0;
         for (int k = nb - 1; k >= 0; k--) {
-            sel += d.grad_hist[k];
+            sel += s_hist[k];
             if (sel > P) { thr = (unsigned)k; break; }
         }
         s_thr = thr;
@@ -581,31 +586,72 @@ __global__ void k_seg_count(const InstDesc *D, const int *active) {
     }
 }
 
+// Exclusive prefix sum of kSegments (512) values in shared memory by the
+// CTA's 512 threads: warp scans by shuffles, then the warps' totals.
+__device__ __forceinline__ int block_exclusive_scan512(int v, int *warp_tot) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int t = lane < kSegments / 32 ? warp_tot[lane] : 0;
+        int ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= o) ti += u;
+        }
+        if (lane < kSegments / 32) warp_tot[lane] = ti - t;  // exclusive warp offsets
+    }
+    __syncthreads();
+    return warp_tot[w] + incl - v;
+}
+
 // segment start offsets and the reference's sequential trimming of surplus
-// threshold-bin points (filterIndex256.cu:136-157), one CTA per instance
+// threshold-bin points (filterIndex256.cu:136-157), one CTA of kSegments
+// threads per instance: the start offsets are an exclusive prefix sum of the
+// counts; the trimming walks the segments in order only while a surplus is
+// left (after that it changes nothing), then the threshold-bin offsets are
+// an exclusive prefix sum of what was kept, after the last start.
 __global__ void k_seg_scan(const InstDesc *D, const int *active) {
     INST_DESC;
     if (!active[blockIdx.y]) return;
-    if (threadIdx.x != 0) return;
+    __shared__ int s_kept[kSegments];
+    __shared__ int warp_tot[kSegments / 32];
+    int t = threadIdx.x;
     int *cnt = d.seg, *mcnt = d.seg + 512, *start = d.seg + 1024, *mstart = d.seg + 1536, *kept = d.seg + 2048;
-    int tooMuch = d.seg[3073];
-    start[0] = 0;
-    for (int i = 1; i < kSegments; i++) start[i] = start[i - 1] + cnt[i - 1];
-    for (int i = 0; i < kSegments; i++) kept[i] = mcnt[i];
-    mstart[0] = start[kSegments - 1] + cnt[kSegments - 1];
-    for (int i = 1; i < kSegments; i++) {
-        if (tooMuch > 0 && kept[i - 1] > 0) {
-            kept[i - 1] -= tooMuch;
-            if (kept[i - 1] < 0) {
-                tooMuch += kept[i - 1];
-                kept[i - 1] = 0;
-            } else {
-                tooMuch = 0;
+    int c = __ldcg(cnt + t);
+    s_kept[t] = __ldcg(mcnt + t);
+    int st = block_exclusive_scan512(c, warp_tot);  // synchronises: s_kept is complete
+    start[t] = st;
+    if (t == 0) {
+        int tooMuch = __ldcg(d.seg + 3073);
+        for (int i = 1; i < kSegments && tooMuch > 0; i++) {
+            if (s_kept[i - 1] > 0) {
+                s_kept[i - 1] -= tooMuch;
+                if (s_kept[i - 1] < 0) {
+                    tooMuch += s_kept[i - 1];
+                    s_kept[i - 1] = 0;
+                } else {
+                    tooMuch = 0;
+                }
             }
         }
-        mstart[i] = mstart[i - 1] + kept[i - 1];
     }
-    d.seg[3074] = mstart[kSegments - 1] + kept[kSegments - 1];
+    __syncthreads();
+    // the total of the counts (the last start plus the last count) begins the threshold-bin offsets
+    __shared__ int s_base;
+    if (t == kSegments - 1) s_base = st + c;
+    int k = s_kept[t];
+    int ms = block_exclusive_scan512(k, warp_tot);  // synchronises: s_base is visible
+    mstart[t] = s_base + ms;
+    kept[t] = k;
+    if (t == kSegments - 1) d.seg[3074] = s_base + ms + k;
 }
 
 // filterIndexKernel4's scatter (filterIndex256.cu:159-168): one warp per segment
