@@ -1384,12 +1384,14 @@ void orc_fuse_depth(const float *zkey, int W, int H, const float *calib, int nfr
 
 /* Gray value the RGB camera sees at point q of its rig's IR frame: TLR,
  * distortPoint and the bilinear tap of xyz2CloudKernel's color1
- * (d2z.cu:235-331).  -1 where the 2x2 taps leave the image. */
+ * (d2z.cu:235-331), the perspective division as one reciprocal and two
+ * products.  -1 where the 2x2 taps leave the image.  Fusion only. */
 static inline float rgb_sample(const float *calib, const float *q, const float *img, int W, int H) {
     float r3[3];
     mul4(&calib[TLR_OFFSET], q, r3);
-    float pux = r3[0] / r3[2];
-    float puy = r3[1] / r3[2];
+    float irz = 1.0f / r3[2];
+    float pux = r3[0] * irz;
+    float puy = r3[1] * irz;
     float px, py;
     distort(pux, puy, &calib[KCR_OFFSET], &calib[KR_OFFSET], &px, &py);
     int xdi = ftoi(px), ydi = ftoi(py);
@@ -1413,6 +1415,8 @@ void orc_fuse_rgbd(const float *zkey, const float *gkey, int W, int H, const flo
     float maxDist = calib[MAXD_OFFSET];
     const float *KL = &calib[KL_OFFSET];
     float fx = KL[0], fy = KL[4], cx = KL[2], cy = KL[5];
+    /* the divisions as products with reciprocals, as the GPU kernel states them */
+    float ifx = 1.0f / fx, ify = 1.0f / fy;
     int colour = gkey && gframes && cout;
     float Tinv[8][16];
     for (int f = 0; f < nframes && f < 8; f++) invert_rt4f(&Tframes[16 * f], Tinv[f]);
@@ -1426,7 +1430,7 @@ void orc_fuse_rgbd(const float *zkey, const float *gkey, int W, int H, const flo
             if (colour) cout[idx] = -1.0f;
             continue;
         }
-        float p[3] = {((float)xi - cx) * z / fx, ((float)yi - cy) * z / fy, z};
+        float p[3] = {((float)xi - cx) * z * ifx, ((float)yi - cy) * z * ify, z};
         float zsum = z, wsum = 1.0f;
         float csum = 0.0f, cw = 0.0f;
         if (colour) {
@@ -1439,14 +1443,15 @@ void orc_fuse_rgbd(const float *zkey, const float *gkey, int W, int H, const flo
         for (int f = 0; f < nframes && f < 8; f++) {
             float q[3];
             mul4(&Tframes[16 * f], p, q);
-            float qx = q[0] / q[2], qy = q[1] / q[2];
+            float iqz = 1.0f / q[2];
+            float qx = q[0] * iqz, qy = q[1] * iqz;
             float px = KL[0] * qx + KL[1] * qy + KL[2];
             float py = KL[3] * qx + KL[4] * qy + KL[5];
             int xd = ftoi(px + 0.5f), yd = ftoi(py + 0.5f);
             if (xd < 0 || yd < 0 || xd >= W || yd >= H) continue;
             float zf = zframes[f][xd + yd * W];
             if (!(zf < -minDist && zf > -maxDist)) continue;
-            float m[3] = {((float)xd - cx) * zf / fx, ((float)yd - cy) * zf / fy, zf};
+            float m[3] = {((float)xd - cx) * zf * ifx, ((float)yd - cy) * zf * ify, zf};
             float mk[3];
             mul4(Tinv[f], m, mk);
             float dz = mk[2] - z;

@@ -511,7 +511,8 @@ static R rgb_sample(const R *c, const R *q, const uint8_t *img8, const R *img, i
     R r3[3];
     mul4(&c[TLR], q, r3);
     R px, py;
-    distort(r3[0] / r3[2], r3[1] / r3[2], &c[KCR], &c[KR], &px, &py);
+    R irz = 1.0 / r3[2];
+    distort(r3[0] * irz, r3[1] * irz, &c[KCR], &c[KR], &px, &py);
     int xdi = dtoi(px), ydi = dtoi(py);
     if (!(xdi >= 0 && ydi >= 0 && xdi < W - 1 && ydi < H - 1)) return -1.0;
     R fx = px - xdi, fy = py - ydi;
@@ -527,6 +528,7 @@ int orc64_fuse_keyframe(orc64_tracker *t, int nframes, const uint8_t *const *gra
     int W = t->W, H = t->H;
     const R *c = t->calib, *KL = &c[KLo];
     R fx = KL[0], fy = KL[4], cx = KL[2], cy = KL[5];
+    R ifx = 1.0 / fx, ify = 1.0 / fy;  /* the FP32 fusion's reciprocals, in double */
     R Tinv[8][16];
     for (int f = 0; f < nframes; f++) invert_rt4(&Tframes[16 * f], Tinv[f]);
     R *zout = (R *)xcalloc((size_t)W * H * sizeof(R));
@@ -537,7 +539,7 @@ int orc64_fuse_keyframe(orc64_tracker *t, int nframes, const uint8_t *const *gra
         zout[idx] = z;
         if (gray) t->ref_col[idx] = -1.0;
         if (!(z < -c[MIND] && z > -c[MAXD])) continue;
-        R p[3] = {((R)xi - cx) * z / fx, ((R)yi - cy) * z / fy, z};
+        R p[3] = {((R)xi - cx) * z * ifx, ((R)yi - cy) * z * ify, z};
         R zsum = z, wsum = 1, csum = 0, cw = 0;
         if (gray) {
             R c0 = rgb_sample(c, p, NULL, t->ref_gray[0], W, H);
@@ -546,13 +548,14 @@ int orc64_fuse_keyframe(orc64_tracker *t, int nframes, const uint8_t *const *gra
         for (int f = 0; f < nframes; f++) {
             R q[3];
             mul4(&Tframes[16 * f], p, q);
-            R qx = q[0] / q[2], qy = q[1] / q[2];
+            R iqz = 1.0 / q[2];
+            R qx = q[0] * iqz, qy = q[1] * iqz;
             int xd = dtoi(KL[0] * qx + KL[1] * qy + KL[2] + 0.5), yd = dtoi(KL[3] * qx + KL[4] * qy + KL[5] + 0.5);
             if (xd < 0 || yd < 0 || xd >= W || yd >= H) continue;
             uint16_t dm = depth[f][xd + yd * W];
             R zf = dm ? -(R)dm : 0.0;
             if (!(zf < -c[MIND] && zf > -c[MAXD])) continue;
-            R m[3] = {((R)xd - cx) * zf / fx, ((R)yd - cy) * zf / fy, zf}, mk[3];
+            R m[3] = {((R)xd - cx) * zf * ifx, ((R)yd - cy) * zf * ify, zf}, mk[3];
             mul4(Tinv[f], m, mk);
             if (fabs(mk[2] - z) < gate) {
                 zsum += mk[2];

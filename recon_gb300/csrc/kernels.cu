@@ -274,14 +274,16 @@ __global__ void k_downsample(const InstDesc *D, int level, const int *active) {
 
 // Gray value the RGB camera sees at point (qx, qy, qz) of its rig's IR frame
 // (TLR, distortPoint and the bilinear color1 tap of xyz2CloudKernel,
-// d2z.cu:235-331), from a float image or a uint8 image scaled by 1/255; -1
-// where the 2x2 taps leave the image.
+// d2z.cu:235-331, with the perspective division as one reciprocal and two
+// products), from a float image or a uint8 image scaled by 1/255; -1 where
+// the 2x2 taps leave the image.  Used by the keyframe fusion only.
 template <typename TImg>
 __device__ __forceinline__ float rgb_sample(const float *calib, float qx, float qy, float qz, const TImg *img, int W,
                                             int H) {
     float rx, ry, rz;
     mul4(calib + RC_TLR, qx, qy, qz, rx, ry, rz);
-    float pux = rx / rz, puy = ry / rz;
+    float irz = 1.0f / rz;
+    float pux = rx * irz, puy = ry * irz;
     float px, py;
     distort(pux, puy, calib + RC_KCR, calib + RC_KR, px, py);
     int xdi = ftoi(px), ydi = ftoi(py);
@@ -296,7 +298,9 @@ __device__ __forceinline__ float rgb_sample(const float *calib, float qx, float 
 // the nearest IR pixel (the zWeight tap of warp.cu:306-327), mapped back with
 // the inverse pose (as filterDepthIIRKernel does, warp.cu:398-467), gated on
 // |dz| < gate and averaged with unit weights (the running mean of
-// updateVoxelsKernel, VoxelGrid_cuda.cu:1005-1013).  With gray images the
+// updateVoxelsKernel, VoxelGrid_cuda.cu:1005-1013).  The divisions are
+// written as products with reciprocals (of fx, fy per instance, of the
+// depth once per projection); the oracle states the same.  With gray images the
 // vertex colour is fused under the same gate: the mean of the keyframe's own
 // sample at the point and the accepted frames' samples at T_f p
 // (KeyFrameModel::integrateDepthMaps warps the neighbours' RGB images into the
@@ -331,6 +335,7 @@ __global__ void __launch_bounds__(256, RECON_FUSE_MIN_BLOCKS) k_fuse_depth(const
     float minDist = d.calib[RC_MIND], maxDist = d.calib[RC_MAXD];
     const float *KL = d.calib + RC_KL;
     float fx = KL[0], fy = KL[4], cx = KL[2], cy = KL[5];
+    float ifx = 1.0f / fx, ify = 1.0f / fy;
     int xi = idx % W, yi = idx / W;
     float z = d.ref_z[idx];
     const bool colour = gray != nullptr;
@@ -338,7 +343,7 @@ __global__ void __launch_bounds__(256, RECON_FUSE_MIN_BLOCKS) k_fuse_depth(const
         if (colour) d.ref_col[idx] = -1.0f;
         return;
     }
-    float px3 = ((float)xi - cx) * z / fx, py3 = ((float)yi - cy) * z / fy, pz3 = z;
+    float px3 = ((float)xi - cx) * z * ifx, py3 = ((float)yi - cy) * z * ify, pz3 = z;
     float zsum = z, wsum = 1.0f;
     float csum = 0.0f, cw = 0.0f;
     if (colour) {
@@ -351,7 +356,8 @@ __global__ void __launch_bounds__(256, RECON_FUSE_MIN_BLOCKS) k_fuse_depth(const
     for (int f = 0; f < nframes && f < 8; f++) {
         float qx, qy, qz;
         mul4(sT[f], px3, py3, pz3, qx, qy, qz);
-        float q2x = qx / qz, q2y = qy / qz;
+        float iqz = 1.0f / qz;
+        float q2x = qx * iqz, q2y = qy * iqz;
         float pxl = KL[0] * q2x + KL[1] * q2y + KL[2];
         float pyl = KL[3] * q2x + KL[4] * q2y + KL[5];
         int xd = ftoi(pxl + 0.5f), yd = ftoi(pyl + 0.5f);
@@ -359,7 +365,7 @@ __global__ void __launch_bounds__(256, RECON_FUSE_MIN_BLOCKS) k_fuse_depth(const
         uint16_t dm = depth[(size_t)f * n_inst + blockIdx.y][xd + yd * W];
         float zf = dm ? -(float)dm : 0.0f;
         if (!(zf < -minDist && zf > -maxDist)) continue;
-        float mx = ((float)xd - cx) * zf / fx, my = ((float)yd - cy) * zf / fy, mz = zf;
+        float mx = ((float)xd - cx) * zf * ifx, my = ((float)yd - cy) * zf * ify, mz = zf;
         float kx, ky, kz;
         mul4(sTi[f], mx, my, mz, kx, ky, kz);
         float dz = kz - z;

@@ -146,6 +146,8 @@ def test_colour_fusion_properties():
     has = co >= 0
     assert has[valid].mean() > 0.9 and not has[~valid].any()
     # the mean of four equal samples is the keyframe's own sample, xyz2CloudKernel's color1
+    # (to the float rounding of the point: the fusion forms it with reciprocals
+    # of fx, fy and the depth where xyz2CloudKernel's inputs divide)
     xyz = np.zeros(4 * n, np.float32)
     L.orc_zmap_to_xyz(O.ptr(z), W, H, O.ptr(cal), O.ptr(xyz))
     vdata = np.zeros(24 * n, np.float32)
@@ -153,7 +155,7 @@ def test_colour_fusion_properties():
     col1 = vdata.reshape(n, 24)[:, 14]
     inb = vdata.reshape(n, 24)[:, 2] < 0
     inb &= vdata.reshape(n, 24)[:, 6] != 0
-    np.testing.assert_allclose(co[inb], col1[inb], rtol=2e-6, atol=1e-7)
+    np.testing.assert_allclose(co[inb], col1[inb], rtol=2e-5, atol=1e-6)
     # a frame whose depth is 100 mm off fails the 30 mm gate
     zfar = np.where(z != 0, z - 100.0, 0.0).astype(np.float32)
     zo2, wo2, co2 = fuse([zfar], [gk])
