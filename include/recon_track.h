@@ -61,7 +61,12 @@ typedef struct recon_config {
     float opt_scale_in;            /* 1e-3 (phototracker.cpp:50) */
     float opt_scale_out;           /* 1e3  (phototracker.cpp:51) */
     int32_t precision;             /* RECON_PRECISION_* */
-    int32_t reserved[7];
+    float settle_mm;               /* > 0: a level ends early once one GN iteration moves every
+                                      translation entry of the pose by <= settle_mm (mm) and every
+                                      rotation entry by <= settle_rot; 0 (default): the fixed
+                                      schedule of the reference */
+    float settle_rot;
+    int32_t reserved[5];
 } recon_config;
 
 typedef struct recon_track_stats {
@@ -204,6 +209,13 @@ int recon_batch_fuse_keyframe(recon_batch *b, int32_t nframes, const uint16_t *c
 
 int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters[RECON_MAX_LEVELS]);
 int recon_batch_set_mode(recon_batch *b, int32_t inst, int32_t mode, float lambda);
+/* Settle rule of instance `inst` (recon_config.settle_mm / settle_rot): with
+ * tol_mm > 0 the instance leaves a pyramid level once one GN iteration has
+ * moved every translation entry of its pose by at most tol_mm and every
+ * rotation entry by at most tol_rot; the level's iteration count is the cap.
+ * tol_mm = 0 restores the reference's fixed schedule (gpuEstimateIncrement,
+ * phototracker.cpp:666-689, has no early exit).  Both must be finite, >= 0. */
+int recon_batch_set_settle(recon_batch *b, int32_t inst, float tol_mm, float tol_rot);
 
 /* Tile shape of the linearisation kernel at each pyramid level: ICP chunks of
  * 1024 pixels per CTA, 1..64, or 0 for the built-in choice.  Poses and sums do
@@ -298,6 +310,7 @@ int recon_set_current(recon_tracker *t, const uint8_t *gray, const uint16_t *dep
 int recon_track(recon_tracker *t, float T_io[16], recon_track_stats *stats);
 int recon_set_iterations(recon_tracker *t, const int32_t iters[RECON_MAX_LEVELS]);
 int recon_set_mode(recon_tracker *t, int32_t mode, float lambda);
+int recon_set_settle(recon_tracker *t, float tol_mm, float tol_rot); /* recon_batch_set_settle */
 /* getRelativePose / getGlobalPose / resetTracking (phototracker.cpp:223-262).
  * After each recon_track the host pose bookkeeping follows applyIncrement
  * (phototracker.cpp:514-531): the relative pose T is the tracked pose

@@ -1801,6 +1801,15 @@ void orc_get_pose(orc_tracker *t, float T[16]) { memcpy(T, t->T, sizeof(t->T)); 
 
 static int padded_len(int n) { return ((n + ORC_CHUNK - 1) / ORC_CHUNK) * ORC_CHUNK; }
 
+int orc_pose_settled(const float Ta[16], const float Tb[16], float tol_mm, float tol_rot) {
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++) {
+            float dv = fabsf(Tb[r * 4 + c] - Ta[r * 4 + c]);
+            if (!(dv <= (c == 3 ? tol_mm : tol_rot))) return 0;
+        }
+    return 1;
+}
+
 /* PhotoTracker::gpuEstimateIncrement (phototracker.cpp:666-689) with
  * updateLinearSystem (505-511), ShapeTracker::updateLinearSystem
  * (shapetracker.cpp:357-382) and estimateIncrement (646-664).  T is the pose
@@ -1888,6 +1897,8 @@ int orc_track(orc_tracker *t, float *Tio, orc_iter_trace *trace, int max_trace) 
                                     t->nsel[layer]);
             }
             int status = 0;
+            float T_before[16];
+            memcpy(T_before, t->T, sizeof(T_before));
             if (ok) {
                 double x[6];
                 if (t->cfg.solver == ORC_SOLVER_CG) {
@@ -1917,6 +1928,9 @@ int orc_track(orc_tracker *t, float *Tio, orc_iter_trace *trace, int max_trace) 
                 tr->median_bin = median;
             }
             ntr++;
+            /* the level ends early once the pose has settled (off at settle_mm 0) */
+            if (t->cfg.settle_mm > 0.0f && orc_pose_settled(T_before, t->T, t->cfg.settle_mm, t->cfg.settle_rot))
+                break;
         }
     }
     if (Tio) memcpy(Tio, t->T, sizeof(t->T));

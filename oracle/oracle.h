@@ -57,6 +57,10 @@ typedef struct orc_config {
     int32_t precision;             /* 0 FP32; 1 mixed: FP16 current images and reference
                                       intensities, BF16 photometric Jacobians (values rounded
                                       to nearest even on storage, FP32 arithmetic) */
+    float settle_mm;               /* > 0: a level ends early once one iteration moves every
+                                      translation entry by <= settle_mm and every rotation entry
+                                      by <= settle_rot (orc_pose_settled); 0: fixed schedule */
+    float settle_rot;
 } orc_config;
 
 /* float -> nearest binary16 / bfloat16 value (ties to even), widened back to float */
@@ -155,6 +159,10 @@ void orc_fuse_rgbd(const float *zkey, const float *gkey, int W, int H, const flo
 
 /* ---- whole tracker (operator level, phototracker.cpp / shapetracker.cpp) ---- */
 orc_tracker *orc_create(const orc_config *cfg, const float *calib);
+/* 1 if no translation entry of the pose moved by more than tol_mm and no
+ * rotation entry by more than tol_rot between Ta and Tb (float differences,
+ * exact comparisons: the GPU takes the same decision from the same poses) */
+int orc_pose_settled(const float Ta[16], const float Tb[16], float tol_mm, float tol_rot);
 void orc_destroy(orc_tracker *t);
 int orc_set_reference(orc_tracker *t, const uint8_t *gray, const uint16_t *depth);
 int orc_set_reference_float(orc_tracker *t, const float *gray0, const float *z0);

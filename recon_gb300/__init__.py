@@ -46,7 +46,8 @@ class Config(ctypes.Structure):
         ("n_select", ctypes.c_int32), ("hist_bins", ctypes.c_int32), ("select_bins", ctypes.c_int32),
         ("solver", ctypes.c_int32), ("mode", ctypes.c_int32), ("lambda_", ctypes.c_float),
         ("iters", ctypes.c_int32 * 4), ("opt_scale_in", ctypes.c_float), ("opt_scale_out", ctypes.c_float),
-        ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
+        ("precision", ctypes.c_int32), ("settle_mm", ctypes.c_float), ("settle_rot", ctypes.c_float),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
 
@@ -72,9 +73,12 @@ class IterTrace(ctypes.Structure):
 
 def make_config(width: int, height: int, levels: int | None = None, mode: int = PHOTOMETRIC,
                 iters=(1, 3, 10, 5), n_select: int = 8192, hist_bins: int = 64, select_bins: int = 256,
-                solver: int = SOLVER_CHOLESKY, lam: float = 0.5, precision: int = PRECISION_FP32) -> Config:
+                solver: int = SOLVER_CHOLESKY, lam: float = 0.5, precision: int = PRECISION_FP32,
+                settle=(0.0, 0.0)) -> Config:
     """Tracker configuration; defaults follow phototracker.cpp (8192 points,
-    iterations {1,3,10,5} coarse->fine, 3 levels at 320 wide and 4 at 640)."""
+    iterations {1,3,10,5} coarse->fine, 3 levels at 320 wide and 4 at 640).
+    `settle` = (mm, rotation entry) tolerances of the early level exit
+    (recon_batch_set_settle); (0, 0) keeps the reference's fixed schedule."""
     if levels is None:
         levels = 4 if width >= 640 else 3
     c = Config()
@@ -85,6 +89,7 @@ def make_config(width: int, height: int, levels: int | None = None, mode: int = 
     c.iters[:] = it[:4]
     c.opt_scale_in, c.opt_scale_out = 1e-3, 1e3
     c.precision = precision
+    c.settle_mm, c.settle_rot = settle
     return c
 
 
@@ -116,6 +121,8 @@ def lib() -> ctypes.CDLL:
             L.recon_batch_track_async.argtypes = [vp, vp]
             L.recon_batch_get_poses.argtypes = [vp, vp, vp]
             L.recon_batch_set_iterations.argtypes = [vp, i32, vp]
+            L.recon_batch_set_settle.argtypes = [vp, i32, ctypes.c_float, ctypes.c_float]
+            L.recon_set_settle.argtypes = [vp, ctypes.c_float, ctypes.c_float]
             L.recon_batch_set_mode.argtypes = [vp, i32, i32, f32]
             L.recon_batch_set_icp_chunks_per_cta.argtypes = [vp, vp]
             L.recon_batch_get_icp_chunks_per_cta.argtypes = [vp, vp]
@@ -533,6 +540,10 @@ class Batch:
 
     def set_mode(self, inst: int, mode: int, lam: float):
         check(lib().recon_batch_set_mode(self.h, inst, mode, lam))
+
+    def set_settle(self, inst: int, tol_mm: float, tol_rot: float):
+        """Early level exit of an instance once its pose has settled (0, 0: off)."""
+        check(lib().recon_batch_set_settle(self.h, inst, tol_mm, tol_rot))
 
     def set_icp_chunks_per_cta(self, per_level):
         """ICP chunks of 1024 pixels per linearisation CTA at each level (0: built-in)."""

@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <atomic>
 #include <mutex>
@@ -237,6 +238,8 @@ int validate(const recon_config &c) {
     if (!(c.lambda >= 0.0f && c.lambda <= 1.0f)) return fail(RECON_ERR_INVALID_ARG, "lambda must be in [0,1]");
     if (c.precision != RECON_PRECISION_FP32 && c.precision != RECON_PRECISION_MIXED)
         return fail(RECON_ERR_INVALID_ARG, "bad precision");
+    if (!(c.settle_mm >= 0.0f && c.settle_mm <= FLT_MAX && c.settle_rot >= 0.0f && c.settle_rot <= FLT_MAX))
+        return fail(RECON_ERR_INVALID_ARG, "settle tolerances must be finite and >= 0");
     return RECON_OK;
 }
 
@@ -901,6 +904,8 @@ int recon_batch_create(int32_t n, const recon_config *cfgs, const float *calibs,
         d.opt_out = c.opt_scale_out;
         d.precision = c.precision;
         for (int l = 0; l < kMaxLevels; l++) d.iters[l] = c.iters[l];
+        d.settle_mm = c.settle_mm;
+        d.settle_rot = c.settle_rot;
         memcpy(d.calib, calibs + (size_t)RECON_CALIB_SIZE * i, sizeof(d.calib));
         size_t bytes = layout(d, nullptr);
         void *mem = nullptr;
@@ -1145,6 +1150,20 @@ int recon_batch_set_iterations(recon_batch *b, int32_t inst, const int32_t iters
     for (int l = 0; l < kMaxLevels; l++) b->desc[inst].iters[l] = iters[l];
     b->graph_dirty = true;
     return upload_desc(b);
+}
+
+int recon_batch_set_settle(recon_batch *b, int32_t inst, float tol_mm, float tol_rot) {
+    clear_stale_error();
+    if (!b || inst < 0 || inst >= b->n) return fail(RECON_ERR_INVALID_ARG, "bad argument");
+    recon_config c = b->cfg[inst];
+    c.settle_mm = tol_mm;
+    c.settle_rot = tol_rot;
+    int rc = validate(c);
+    if (rc) return rc;
+    b->cfg[inst] = c;
+    b->desc[inst].settle_mm = tol_mm;
+    b->desc[inst].settle_rot = tol_rot;
+    return upload_desc(b);  // the launches do not change: the kernels read the rule from the descriptor
 }
 
 int recon_batch_set_icp_chunks_per_cta(recon_batch *b, const int32_t per_level[RECON_MAX_LEVELS]) {
@@ -1752,6 +1771,7 @@ int recon_set_iterations(recon_tracker *t, const int32_t iters[RECON_MAX_LEVELS]
     return recon_batch_set_iterations(t, 0, iters);
 }
 int recon_set_mode(recon_tracker *t, int32_t mode, float lambda) { return recon_batch_set_mode(t, 0, mode, lambda); }
+int recon_set_settle(recon_tracker *t, float tol_mm, float tol_rot) { return recon_batch_set_settle(t, 0, tol_mm, tol_rot); }
 int recon_get_relative_pose(recon_tracker *t, float T[16]) {
     if (!t || !T) return fail(RECON_ERR_INVALID_ARG, "null argument");
     memcpy(T, t->T_host, sizeof(t->T_host));

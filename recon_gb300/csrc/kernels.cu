@@ -1530,7 +1530,17 @@ __device__ __forceinline__ void finalize_iter(const InstDesc &d, SolveShared &sh
     if (t >= 32) return;
     int lane = t;
     int st = 0;
+    float T_before = lane < 16 ? sh.T[lane] : 0.0f;
     if (ok) st = wsolve_update(S, d.solver, sh.T, (double)d.opt_out, lane);
+    __syncwarp();
+    if (d.settle_mm > 0.0f) {
+        // settle rule (orc_pose_settled): every translation entry moved by at
+        // most settle_mm and every rotation entry by at most settle_rot; the
+        // instance's remaining iterations of this level are skipped
+        bool small = true;
+        if (lane < 12) small = fabsf(sh.T[lane] - T_before) <= ((lane & 3) == 3 ? d.settle_mm : d.settle_rot);
+        if (__all_sync(0xffffffffu, small) && lane == 0) d.stats[ST_SETTLED] = level + 1;
+    }
     if (lane < 16) d.T[lane] = sh.T[lane];
     if (tr && lane < 16) tr->T[lane] = sh.T[lane];
     if (lane == 0) {
@@ -1606,6 +1616,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kIterThreads,
         if (jj < nall) icp_prefetch_chunk(d, level, (rev ? nall - 1 - jj : jj) * icp_per_cta, np);
     }
     pdl_wait();
+    // the instance left this level early (settle rule; uniform over a cluster)
+    if (d.settle_mm > 0.0f && __ldcg(d.stats + ST_SETTLED) == level + 1) return;
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
     int nsel = use_icp ? __ldcg(d.icp_nsel + level) : 0;
@@ -1650,6 +1662,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int 
     if (level >= d.L) return;
     if (it >= d.iters[d.L - 1 - level]) return;
     pdl_wait();
+    if (d.settle_mm > 0.0f && __ldcg(d.stats + ST_SETTLED) == level + 1) return;
     bool use_ph = d.mode != RECON_GEOMETRIC;
     bool use_icp = d.mode != RECON_PHOTOMETRIC;
     __shared__ SolveShared sh;

@@ -22,7 +22,8 @@ constexpr int kSolveThreads = 64;        // threads of the per-instance solve CT
 constexpr int kFxLimbs = 4;      // limbs of a fixed-point sum (fx.cuh)
 constexpr int kNetW = 80, kNetH = 60;  // coarse image of the learned initialisation
 
-enum StatSlot { ST_ITERS = 0, ST_SOLVES, ST_NONSPD, ST_STATUS, ST_MEDIAN, ST_ICPSEL0, ST_COUNT = 16 };
+// ST_SETTLED: level + 1 of the level the instance left early (settle rule), 0 if none this frame
+enum StatSlot { ST_ITERS = 0, ST_SOLVES, ST_NONSPD, ST_STATUS, ST_MEDIAN, ST_ICPSEL0, ST_SETTLED = 9, ST_COUNT = 16 };
 
 struct InstDesc {
     int W, H, L, P;
@@ -31,6 +32,7 @@ struct InstDesc {
     int precision;
     double fuse_c1;  // (double)(1 - lambda) / P, the photometric weight of the fused system
     int iters[kMaxLevels];
+    float settle_mm, settle_rot;  // settle rule (recon_config); off at settle_mm 0
     float calib[RECON_CALIB_SIZE];
     // reference (keyframe)
     float *ref_gray[kMaxLevels];

@@ -29,7 +29,7 @@ class OrcConfig(ctypes.Structure):
         ("n_select", ctypes.c_int32), ("hist_bins", ctypes.c_int32), ("select_bins", ctypes.c_int32),
         ("solver", ctypes.c_int32), ("mode", ctypes.c_int32), ("lambda_", ctypes.c_float),
         ("iters", ctypes.c_int32 * 4), ("opt_scale_in", ctypes.c_float), ("opt_scale_out", ctypes.c_float),
-        ("precision", ctypes.c_int32),
+        ("precision", ctypes.c_int32), ("settle_mm", ctypes.c_float), ("settle_rot", ctypes.c_float),
     ]
 
 
@@ -165,6 +165,8 @@ def lib() -> ctypes.CDLL:
             L.orc_tsdf_raycast.argtypes = [vp, ctypes.POINTER(OrcTsdfParams), vp, vp, i32, vp]
             L.orc_tsdf_shade.argtypes = [vp, i32, i32, vp, vp]
             L.orc_tsdf_resample.argtypes = [vp, vp, ctypes.POINTER(OrcTsdfParams), vp]
+            L.orc_pose_settled.argtypes = [vp, vp, f32, f32]
+            L.orc_pose_settled.restype = i32
             L.orc_num_threads.restype = i32
             L.orc_set_threads.argtypes = [i32]
             _lib = L
@@ -188,7 +190,7 @@ def ptrs(arrays) -> ctypes.Array:
 
 
 def make_config(width, height, levels, mode=PHOTOMETRIC, iters=(1, 3, 10, 5), n_select=8192, hist_bins=64,
-                select_bins=256, solver=CHOLESKY, lam=0.5, precision=0) -> OrcConfig:
+                select_bins=256, solver=CHOLESKY, lam=0.5, precision=0, settle=(0.0, 0.0)) -> OrcConfig:
     c = OrcConfig()
     c.width, c.height, c.levels = width, height, levels
     c.n_select, c.hist_bins, c.select_bins = n_select, hist_bins, select_bins
@@ -197,6 +199,7 @@ def make_config(width, height, levels, mode=PHOTOMETRIC, iters=(1, 3, 10, 5), n_
     c.iters[:] = it[:4]
     c.opt_scale_in, c.opt_scale_out = 1e-3, 1e3
     c.precision = precision
+    c.settle_mm, c.settle_rot = settle
     return c
 
 
