@@ -36,7 +36,7 @@ constexpr int kPyrTile = 32;  // level-0 tile of k_prep_current_pyramid
 __global__ void k_prep_current_pyramid(const InstDesc *D, const uint8_t *const *in_gray,
                                        const uint16_t *const *in_depth, const float *const *in_rgbd, int tiles_x,
                                        float *store_prev, int begin);
-__global__ void k_icp_student3(const InstDesc *D, int level);
+__global__ void k_icp_student_pass(const InstDesc *D, int level, int pass, int blocks_per_cta);
 __global__ void k_icp_prepare(const InstDesc *D, int level);
 __global__ void k_iter(const InstDesc *D, int level, int it, int icp_per_cta, int n_inst, int icp_ctas);
 __global__ void k_solve(const InstDesc *D, int level, int it);
@@ -279,6 +279,7 @@ size_t layout(InstDesc &d, char *base) {
     int nblk = (n + kChunk - 1) / kChunk;
     d.icp_blkcnt = a.take<int>(nblk);
     d.icp_blkvar = a.take<long long>(nblk);
+    d.icp_part = a.take<long long>(nblk);
     d.icp_var = a.take<unsigned long long>(4);
     d.icp_nsel = a.take<int>(kMaxLevels);
     d.fuse_c2 = a.take<double>(kMaxLevels);
@@ -513,9 +514,9 @@ int prepare_current(recon_batch *b, const void **in = nullptr, float *store_prev
 
 // Levels with at most this many pixels per instance prepare their ICP
 // correspondences and weights in one cluster launch (k_icp_prepare, at most 4
-// pixels per thread); larger ones use the wide mask grid + k_icp_student3,
-// whose many small CTAs hide the gathers' latency better (at 320x240 with 30
-// instances the two launches beat the fused one by 1% of the frame).
+// pixels per thread); larger ones use the wide mask grid and one wide launch
+// per Student-t pass (k_icp_student_pass), whose many small CTAs hide the
+// gathers' latency better and keep every SM busy.
 #ifndef RECON_PREPARE_FUSED_MAX_PIX
 #define RECON_PREPARE_FUSED_MAX_PIX (4 * 8 * 1024)
 #endif
@@ -577,10 +578,14 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
                 CK(launch_pdl(k_icp_mask, dim3(nchunk, n), dim3(kLanes), s, D, level));
             }
             {
+                // about one wave of CTAs over the batch's blocks
+                int per = std::max(1, (n * nchunk + kPassCtaSlots - 1) / kPassCtaSlots);
+                int gx = (nchunk + per - 1) / per;
                 TimedScope ts(b, s, TK_ICP_STUDENT, in_graph);
-                CK(launch_pdl(k_icp_student3, dim3(kIterCluster, n), dim3(1024), s, D, level));
+                for (int pass = 1; pass <= 3; pass++)
+                    CK(launch_pdl(k_icp_student_pass, dim3(gx, n), dim3(kLanes), s, D, level, pass, per));
             }
-            b->graph_kernels += 2;
+            b->graph_kernels += 4;
         }
         int per_cta = icp_per_cta(b, level, nchunk);
         int ncta = any_icp ? (nchunk + per_cta - 1) / per_cta : 0;

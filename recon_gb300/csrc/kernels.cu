@@ -856,6 +856,26 @@ __device__ __forceinline__ uint8_t icp_mask_pixel(const InstDesc &d, const float
     return 1;
 }
 
+// Whether this CTA is the last of the instance's `nblk` CTAs of the launch to
+// finish its partial total (written by thread 0 before the call): thread 0 makes
+// the total visible, then takes a ticket from the instance's counter; the CTA
+// holding the last ticket resets the counter for the next launch and may read
+// every partial total.  No CTA waits for another.
+__device__ __forceinline__ bool icp_last_block(const InstDesc &d, int nblk) {
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int k = atomicAdd(d.counter + 1, 1u);
+        s_last = (k == (unsigned int)nblk - 1u);
+        if (s_last) {
+            atomicExch(d.counter + 1, 0u);
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    return s_last != 0;
+}
+
 // icpResidualKernel2 (rgb2gray.cu:223-260) with initWeightsKernel's first
 // Student-t weight (rgb2gray.cu:827-850): per pixel of the level, whether it is
 // a correspondence at the level's start pose and its squared residual; per
@@ -934,6 +954,152 @@ __global__ void __launch_bounds__(kLanes, RECON_MASK_MIN_BLOCKS) k_icp_mask(cons
         }
         d.icp_blkcnt[blockIdx.x] = c;
         d.icp_blkvar[blockIdx.x] = v;
+    }
+}
+
+// Student-t pass `pass` (1..3) of a level (updateWeightsKernel /
+// clampWeightsKernel, rgb2gray.cu:549-569) over the level's pixel grid: CTA x
+// of instance blockIdx.y takes the 1024-pixel blocks [x K, (x+1) K) of the
+// instance, K = blocks_per_cta (about one wave of CTAs over the batch), a
+// thread four consecutive pixels of each block with the loads of four blocks
+// in flight.  Every correspondence is weighed with the variance of the
+// previous pass; passes 1 and 2 add the truncated products r^2 w into the
+// CTA's partial sum (icp_part) and the instance's last CTA forms the total
+// icp_var[pass]; pass 3 clamps at 1 and writes every pixel's weight (0 where
+// the pixel is not a correspondence).  Pass 1 first adds up k_icp_mask's block
+// totals (every CTA, from L2): the correspondence count and the first
+// variance sum, which CTA 0 stores.  The sums are exact int64 sums, so the
+// result does not depend on how the pixels are split; one launch per pass
+// keeps every SM busy without any CTA waiting on another.  48 registers: five
+// CTAs per SM (kPassCtaSlots).
+__global__ void __launch_bounds__(kLanes) k_icp_student_pass(const InstDesc *D, int level, int pass,
+                                                             int blocks_per_cta) {
+    pdl_trigger();
+    __shared__ InstDesc sd;
+    __shared__ long long s_var[kLanes / 32];
+    __shared__ int s_cnt[kLanes / 32];
+    load_desc(sd, D + blockIdx.y);
+    __syncthreads();
+    const InstDesc &d = sd;
+    if (level >= d.L || d.mode == RECON_PHOTOMETRIC) return;
+    if (d.iters[d.L - 1 - level] <= 0) return;
+    int n = (d.W >> level) * (d.H >> level);
+    int nblk = (n + kChunk - 1) / kChunk;
+    int nctas = (nblk + blocks_per_cta - 1) / blocks_per_cta;
+    if ((int)blockIdx.x >= nctas) return;
+    int b_first = blockIdx.x * blocks_per_cta;
+    int b_last = min(b_first + blocks_per_cta, nblk);
+    int wid = threadIdx.x >> 5;
+    pdl_wait();
+    int nsel;
+    long long var;
+    if (pass == 1) {
+        int c = 0;
+        long long v = 0;
+        for (int k = threadIdx.x; k < nblk; k += kLanes) {
+            c += __ldcg(d.icp_blkcnt + k);
+            v += __ldcg(d.icp_blkvar + k);
+        }
+        c = __reduce_add_sync(0xffffffffu, c);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) {
+            s_cnt[wid] = c;
+            s_var[wid] = v;
+        }
+        __syncthreads();
+        nsel = 0;
+        var = 0;
+        for (int k = 0; k < kLanes / 32; k++) {
+            nsel += s_cnt[k];
+            var += s_var[k];
+        }
+        __syncthreads();  // s_var is reused for this pass's sum
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            d.icp_nsel[level] = nsel;
+            // ICP weight of the fused system, kept off the iteration's critical path
+            d.fuse_c2[level] = (double)d.lambda / (double)nsel;
+            d.icp_var[0] = (unsigned long long)var;
+        }
+    } else {
+        nsel = __ldcg(d.icp_nsel + level);
+        var = (long long)__ldcg(d.icp_var + pass - 1);
+    }
+    float Sf = (float)var;
+    float minVal = (float)nsel;
+    float vv = (nsel <= 1024) ? Sf : (Sf < minVal ? minVal : Sf);
+    float sigma2 = vv / (float)nsel;
+    long long vsum = 0;
+    for (int b0 = b_first; b0 < b_last; b0 += 4) {
+        float4 r[4];
+        uchar4 m[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            int i = (b0 + u) * kChunk + 4 * threadIdx.x;
+            r[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            m[u] = make_uchar4(0, 0, 0, 0);
+            if (b0 + u >= b_last || i >= n) continue;
+            if (i + 3 < n) {
+                // 16- and 4-byte aligned: the arrays start on 256-byte boundaries
+                r[u] = __ldg(reinterpret_cast<const float4 *>(d.icp_r2 + i));
+                m[u] = __ldg(reinterpret_cast<const uchar4 *>(d.icp_mask + i));
+            } else {
+                // the instance's last pixels (n not a multiple of 4)
+                r[u].x = __ldg(d.icp_r2 + i);
+                m[u].x = __ldg(d.icp_mask + i);
+                if (i + 1 < n) {
+                    r[u].y = __ldg(d.icp_r2 + i + 1);
+                    m[u].y = __ldg(d.icp_mask + i + 1);
+                }
+                if (i + 2 < n) {
+                    r[u].z = __ldg(d.icp_r2 + i + 2);
+                    m[u].z = __ldg(d.icp_mask + i + 2);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            int i = (b0 + u) * kChunk + 4 * threadIdx.x;
+            if (b0 + u >= b_last || i >= n) continue;
+            if (pass == 3) {
+                float4 w = make_float4(m[u].x ? fminf(student_w(r[u].x, sigma2), 1.0f) : 0.0f,
+                                       m[u].y ? fminf(student_w(r[u].y, sigma2), 1.0f) : 0.0f,
+                                       m[u].z ? fminf(student_w(r[u].z, sigma2), 1.0f) : 0.0f,
+                                       m[u].w ? fminf(student_w(r[u].w, sigma2), 1.0f) : 0.0f);
+                if (i + 3 < n) {
+                    *reinterpret_cast<float4 *>(d.icp_w + i) = w;
+                } else {
+                    d.icp_w[i] = w.x;
+                    if (i + 1 < n) d.icp_w[i + 1] = w.y;
+                    if (i + 2 < n) d.icp_w[i + 2] = w.z;
+                }
+            } else {
+                // pixels past the end have mask 0
+                if (m[u].x) vsum += trunc_prod(r[u].x, student_w(r[u].x, sigma2));
+                if (m[u].y) vsum += trunc_prod(r[u].y, student_w(r[u].y, sigma2));
+                if (m[u].z) vsum += trunc_prod(r[u].z, student_w(r[u].z, sigma2));
+                if (m[u].w) vsum += trunc_prod(r[u].w, student_w(r[u].w, sigma2));
+            }
+        }
+    }
+    if (pass == 3) return;
+    for (int o = 16; o > 0; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
+    if ((threadIdx.x & 31) == 0) s_var[wid] = vsum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long v = 0;
+        for (int k = 0; k < kLanes / 32; k++) v += s_var[k];
+        d.icp_part[blockIdx.x] = v;
+    }
+    if (!icp_last_block(d, nctas)) return;
+    long long v = 0;
+    for (int k = threadIdx.x; k < nctas; k += kLanes) v += __ldcg(d.icp_part + k);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s_var[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long tot = 0;
+        for (int k = 0; k < kLanes / 32; k++) tot += s_var[k];
+        d.icp_var[pass] = (unsigned long long)tot;
     }
 }
 
@@ -1669,25 +1835,20 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(const InstDesc *D, int 
     finalize_iter(d, sh, level, it, use_ph, use_icp);
 }
 
-// The three Student-t passes of a level in one launch (updateWeightsKernel /
-// clampWeightsKernel, rgb2gray.cu:549-569) over the level's pixel grid: each
-// pass weighs every correspondence with the variance of the previous pass; the
-// final pass clamps at 1 and writes every pixel's weight (0 where the pixel is
-// not a correspondence), the first two produce only their variance sums (exact
-// int64 sums of truncated products).  An 8-CTA cluster per instance
-// (blockIdx.y) splits the pixels and exchanges the CTAs' sums through
-// distributed shared memory, so no pass waits for a separate launch.  Two
-// CTAs fit on an SM, so a batch of up to 38 instances runs in one wave.  The
-// correspondence count and the first sum are k_icp_mask's block totals.
+// The whole ICP preparation of a small level in one launch: the level's
+// correspondences (k_icp_mask's per-pixel work), their count and first
+// variance sum, and the three Student-t passes (updateWeightsKernel /
+// clampWeightsKernel, rgb2gray.cu:549-569): each pass weighs every
+// correspondence with the variance of the previous pass; the final pass
+// clamps at 1 and writes every pixel's weight (0 where the pixel is not a
+// correspondence), the first two produce only their variance sums (exact int64
+// sums of truncated products).  An 8-CTA cluster per instance (blockIdx.y)
+// splits the pixels, every thread reading back only what it wrote, and
+// exchanges the CTAs' sums through distributed shared memory, so no pass waits
+// for a separate launch.  Two CTAs fit on an SM, so a batch of up to 38
+// instances runs in one wave.
 constexpr int kStudentThreads = 1024;
 
-
-// The body of the Student-t kernels.  With kMask the cluster first evaluates
-// the level's correspondences itself (k_icp_mask's per-pixel work, over the
-// same pixel-to-thread mapping as the passes, so every thread reads back only
-// what it wrote) and exchanges the count and first variance sum; without it
-// those come from k_icp_mask's block totals.
-template <bool kMask>
 __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
     __shared__ InstDesc sd;
     __shared__ float sT[16];
@@ -1708,7 +1869,7 @@ __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
     int stride = kIterCluster * kStudentThreads;
     int c = 0;
     long long v = 0;
-    if (kMask) {
+    {
         if (t < 16) sT[t] = __ldcg(d.T + t);
         if (rank == 0 && t == 0) d.work[2] += (unsigned long long)n;
         __syncthreads();
@@ -1736,12 +1897,6 @@ __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
                 c += ok;
             }
         }
-    } else {
-        int nblk = (n + kChunk - 1) / kChunk;
-        for (int k = t; k < nblk; k += kStudentThreads) {
-            c += __ldcg(d.icp_blkcnt + k);
-            v += __ldcg(d.icp_blkvar + k);
-        }
     }
     c = __reduce_add_sync(0xffffffffu, c);
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -1757,25 +1912,21 @@ __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
             cs += warp_cnt[w];
             vs += warp_sum[w];
         }
-        s_nsel = cs;
-        s_var0 = vs;
         part[2] = vs;
         part_cnt = cs;
     }
-    if (kMask) {
-        cluster_arrive();
-        cluster_wait();  // every CTA's count and first sum are in its shared memory
-        if (t == 0) {
-            int cs = 0;
-            long long vs = 0;
+    cluster_arrive();
+    cluster_wait();  // every CTA's count and first sum are in its shared memory
+    if (t == 0) {
+        int cs = 0;
+        long long vs = 0;
 #pragma unroll
-            for (int r = 0; r < kIterCluster; r++) {
-                cs += *cluster_peer(&part_cnt, r);
-                vs += *cluster_peer(&part[2], r);
-            }
-            s_nsel = cs;
-            s_var0 = vs;
+        for (int r = 0; r < kIterCluster; r++) {
+            cs += *cluster_peer(&part_cnt, r);
+            vs += *cluster_peer(&part[2], r);
         }
+        s_nsel = cs;
+        s_var0 = vs;
     }
     __syncthreads();
     int nsel = s_nsel;
@@ -1792,65 +1943,25 @@ __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
         float vv = (nsel <= 1024) ? Sf : (Sf < minVal ? minVal : Sf);
         float sigma2 = vv / (float)nsel;
         long long vsum = 0;
-        if (!kMask && (n & 3) == 0) {
-            // k_icp_mask wrote the grid: any thread may read any pixel, so each
-            // takes four consecutive pixels per vector load, two groups in
-            // flight (the passes are bound by load latency, not by bytes)
-            const float4 *r4 = reinterpret_cast<const float4 *>(d.icp_r2);
-            const uchar4 *m4 = reinterpret_cast<const uchar4 *>(d.icp_mask);
-            float4 *w4 = reinterpret_cast<float4 *>(d.icp_w);
-            int ng = n >> 2;
-            for (int g0 = rank * kStudentThreads + t; g0 < ng; g0 += 2 * stride) {
-                float4 r[2];
-                uchar4 m[2];
-#pragma unroll
-                for (int u = 0; u < 2; u++) {
-                    int g = g0 + u * stride;
-                    r[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    m[u] = make_uchar4(0, 0, 0, 0);
-                    if (g < ng) {
-                        r[u] = __ldg(r4 + g);
-                        m[u] = __ldg(m4 + g);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 2; u++) {
-                    int g = g0 + u * stride;
-                    if (g >= ng) continue;
-                    if (pass == 3) {
-                        w4[g] = make_float4(m[u].x ? fminf(student_w(r[u].x, sigma2), 1.0f) : 0.0f,
-                                            m[u].y ? fminf(student_w(r[u].y, sigma2), 1.0f) : 0.0f,
-                                            m[u].z ? fminf(student_w(r[u].z, sigma2), 1.0f) : 0.0f,
-                                            m[u].w ? fminf(student_w(r[u].w, sigma2), 1.0f) : 0.0f);
-                    } else {
-                        if (m[u].x) vsum += trunc_prod(r[u].x, student_w(r[u].x, sigma2));
-                        if (m[u].y) vsum += trunc_prod(r[u].y, student_w(r[u].y, sigma2));
-                        if (m[u].z) vsum += trunc_prod(r[u].z, student_w(r[u].z, sigma2));
-                        if (m[u].w) vsum += trunc_prod(r[u].w, student_w(r[u].w, sigma2));
-                    }
-                }
+        int i = rank * kStudentThreads + t;
+        float r_next = 0.0f;
+        uint8_t m_next = 0;
+        if (i < n) {
+            r_next = __ldg(d.icp_r2 + i);
+            m_next = __ldg(d.icp_mask + i);
+        }
+        for (; i < n; i += stride) {
+            // the next pixel's loads are in flight while this one is weighed
+            float r = r_next;
+            uint8_t mk = m_next;
+            if (i + stride < n) {
+                r_next = __ldg(d.icp_r2 + i + stride);
+                m_next = __ldg(d.icp_mask + i + stride);
             }
-        } else {
-            int i = rank * kStudentThreads + t;
-            float r_next = 0.0f;
-            uint8_t m_next = 0;
-            if (i < n) {
-                r_next = __ldg(d.icp_r2 + i);
-                m_next = __ldg(d.icp_mask + i);
-            }
-            for (; i < n; i += stride) {
-                // the next pixel's loads are in flight while this one is weighed
-                float r = r_next;
-                uint8_t mk = m_next;
-                if (i + stride < n) {
-                    r_next = __ldg(d.icp_r2 + i + stride);
-                    m_next = __ldg(d.icp_mask + i + stride);
-                }
-                if (pass == 3) {
-                    d.icp_w[i] = mk ? fminf(student_w(r, sigma2), 1.0f) : 0.0f;
-                } else if (mk) {
-                    vsum += trunc_prod(r, student_w(r, sigma2));
-                }
+            if (pass == 3) {
+                d.icp_w[i] = mk ? fminf(student_w(r, sigma2), 1.0f) : 0.0f;
+            } else if (mk) {
+                vsum += trunc_prod(r, student_w(r, sigma2));
             }
         }
         if (pass == 3) break;
@@ -1876,21 +1987,13 @@ __device__ __forceinline__ void student_body(const InstDesc *D, int level) {
     cluster_wait();
 }
 
-__global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads, 2)
-    k_icp_student3(const InstDesc *D, int level) {
-    pdl_trigger();
-    student_body<false>(D, level);
-}
-
-// The whole ICP preparation of a level in one launch (mask, count, first sum,
-// three Student-t passes): for the coarser levels, where the grid is small
-// enough for one cluster per instance to evaluate it.  Two CTAs per SM, as for
-// k_icp_student3 (a few registers spill in the mask phase; measured faster
-// than one CTA per SM at 30 instances).
+// The coarser levels' ICP preparation, where the grid is small enough for one
+// cluster per instance to evaluate it.  Two CTAs per SM (a few registers spill
+// in the mask phase; measured faster than one CTA per SM at 30 instances).
 __global__ void __cluster_dims__(kIterCluster, 1, 1) __launch_bounds__(kStudentThreads, 2)
     k_icp_prepare(const InstDesc *D, int level) {
     pdl_trigger();
-    student_body<true>(D, level);
+    student_body(D, level);
 }
 
 // ------------------------------------------------------------------

@@ -18,6 +18,7 @@ constexpr int kVtxPlanes = 9;    // a vertex record: x y z px py gx gy gmag gray
 constexpr int kIterCluster = 8;  // CTAs of the photometric cluster of the GN iteration kernel
 constexpr int kIterBlock = 256;  // threads of a GN iteration CTA
 constexpr int kIterCtaSlots = 4 * 152;  // GN iteration CTAs resident on a 152-SM GB300
+constexpr int kPassCtaSlots = 5 * 152;  // 256-thread Student-t pass CTAs resident on a 152-SM GB300
 constexpr int kSolveThreads = 64;        // threads of the per-instance solve CTA
 constexpr int kFxLimbs = 4;      // limbs of a fixed-point sum (fx.cuh)
 constexpr int kNetW = 80, kNetH = 60;  // coarse image of the learned initialisation
@@ -65,6 +66,7 @@ struct InstDesc {
     float *icp_w;            // W*H: its Student-t weight, 0 where not selected
     int *icp_blkcnt;         // per 1024-pixel block: correspondences
     long long *icp_blkvar;   // per 1024-pixel block: first variance sum
+    long long *icp_part;     // per Student-t pass CTA (at most one per block): its partial sum
     unsigned long long *icp_var;  // 4: the variance sums of the passes
     int *icp_nsel;           // kMaxLevels
     double *fuse_c2;         // kMaxLevels: lambda / (ICP correspondences) of the level
@@ -72,7 +74,7 @@ struct InstDesc {
     unsigned long long *fx;
     int *fx_bad;             // 2: an accumulated value was out of range
     unsigned long long *work; // [0] photometric point-iterations, [1] ICP point-iterations, [2] ICP mask pixels
-    unsigned int *counter;
+    unsigned int *counter;   // 4: [1] the Student-t passes' last-CTA ticket (k_icp_student_pass; reset by its last taker)
     float *T;                // 16, device pose (reference IR -> current IR)
     int *stats;              // ST_COUNT
     recon_iter_trace *trace;
