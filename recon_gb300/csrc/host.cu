@@ -578,8 +578,17 @@ int launch_schedule(recon_batch *b, cudaStream_t s, bool in_graph) {
                 CK(launch_pdl(k_icp_mask, dim3(nchunk, n), dim3(kLanes), s, D, level));
             }
             {
-                // about one wave of CTAs over the batch's blocks
-                int per = std::max(1, (n * nchunk + kPassCtaSlots - 1) / kPassCtaSlots);
+                // about one wave of CTAs over the blocks of the instances that
+                // run the level (sized by their actual blocks, so that a batch
+                // of mixed resolutions is spread as evenly as a uniform one)
+                long long blocks = 0;
+                for (int i = 0; i < n; i++) {
+                    const recon_config &c = b->cfg[i];
+                    if (level >= c.levels || c.mode == RECON_PHOTOMETRIC || c.iters[c.levels - 1 - level] <= 0)
+                        continue;
+                    blocks += ((c.width >> level) * (c.height >> level) + kChunk - 1) / kChunk;
+                }
+                int per = (int)std::max(1LL, (blocks + kPassCtaSlots - 1) / kPassCtaSlots);
                 int gx = (nchunk + per - 1) / per;
                 TimedScope ts(b, s, TK_ICP_STUDENT, in_graph);
                 for (int pass = 1; pass <= 3; pass++)
