@@ -177,3 +177,31 @@ def test_settle_rule_in_graph_replayed_sequences():
             assert np.array_equal(T[f - 1, inst].view(np.uint32), To.view(np.uint32)), (inst, f)
         o.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_settle_rule_through_the_tracker_entry_points():
+    """recon_tracker_create with a settle configuration, and recon_set_settle
+    switching it off and on again: poses and executed iterations equal the
+    oracle's with the same rule."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import ctypes
+    import recon_gb300 as rg
+    p = frame_pair(320, 240, seed=29)
+    iters, tol = (3, 6, 8), (0.05, 5e-5)
+    trk = rg.Tracker(rg.make_config(320, 240, 3, mode=rg.BIOBJECTIVE, iters=iters, settle=tol), p.cal.calib)
+    trk.set_reference(p.g0, p.d0)
+    trk.set_current(p.g1, p.d1)
+    I = np.eye(4, dtype=np.float32)
+    for settle in (tol, (0.0, 0.0), tol):
+        rg.check(rg.lib().recon_set_settle(trk.h, ctypes.c_float(settle[0]), ctypes.c_float(settle[1])))
+        T, st = trk.track(I)
+        To, tr = _oracle_run(p, iters, settle, I)
+        assert np.array_equal(np.asarray(T, np.float32).view(np.uint32), To.view(np.uint32)), settle
+        assert st.iterations == len(tr), (settle, st.iterations, len(tr))
+    assert len(_oracle_run(p, iters, tol, I)[1]) < sum(iters)
+    # invalid tolerances are refused
+    assert rg.lib().recon_set_settle(trk.h, ctypes.c_float(-1.0), ctypes.c_float(0.0)) < 0
+    assert rg.lib().recon_set_settle(trk.h, ctypes.c_float(float("nan")), ctypes.c_float(0.0)) < 0
